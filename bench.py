@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 MH/HMM phasing hot path.
+
+One step = one MH generation over all samples of the workload: C+1
+likelihood evaluations per sample (initial quadruple plus C proposals) over
+S sites, the MH accept chain, and the fused hmm_work haplotype sampling,
+exactly the work of GLPhase's RunHMMOnDevice + hmm_work loop
+(src/hmmLike.cu:399-572, src/insti.cpp:1433-1463).  Metric: HMM site-updates
+per second, one update = one (sample, proposal, site) forward step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Default workload: 10,000 samples x 4,096 sites, C = 100 (the batched
+configuration), seeded synthetic data generated on the host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_PER_UPDATE = 29  # impute.cpp:354-373: 12 mul + 8 add (b terms), 2 pair sums, 4 emission muls, 3 adds
+METRIC = "HMM site-updates/s (sample x proposal x site)"
+UNIT = "site-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="batched")
+    ap.add_argument("--samples", type=int, default=0, help="override N (tests)")
+    ap.add_argument("--sites", type=int, default=0, help="override S (tests)")
+    ap.add_argument("--cycles", type=int, default=100)
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per sample (0 = auto)")
+    ap.add_argument("--vq", action="store_true", help="score with 4-bit VQ GL codes")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(args, rank):
+    from glphase_gb300 import synth
+    w = synth.CONFIGS[args.config]
+    N = args.samples or w.N
+    S = args.sites or w.S
+    ds = synth.generate(w, N=N, S=S, seed=w.seed + 1000 * rank)
+    m, haps = synth.initial_state(ds, seed=7 + rank)
+    return w, m, haps
+
+
+def pen_for(gen, burnin):
+    p = min((gen + 1.0) / burnin, 1.0)
+    return p * p
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(m, haps, quad, props, C, pen, seconds, seed=1, gen=0):
+    """The CPU oracle (reference operation order, OpenMP over samples) on a
+    bounded number of samples of one generation."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build(ref=False)
+    threads = os.cpu_count() or 1
+    pb = O.OracleProblem(haps, m.emit, m.t, m.tran, m.pc, C)
+    tr = pb.trace(seed=seed, generation=gen)
+    n = min(m.N, max(threads * 2, 16))
+    t0 = time.perf_counter()
+    O.generation(pb, tr, quad, props, pen, 0, n, True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    n2 = int(min(m.N, max(n, n * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    O.generation(pb, tr, quad, props, pen, 0, n2, True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    ups = n2 * (C + 1) * m.S / dt
+    return {"value": ups, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n2} of {m.N} samples of one generation (C={C}, S={m.S}), "
+                      f"{dt:.1f} s on {threads} host threads"}, dt
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    w, m, haps = workload(args, 0)
+    C = args.cycles
+    rng = np.random.default_rng(5)
+    from glphase_gb300 import synth
+    quad, props = synth.uniform_proposals(m.N, haps.shape[0], C, rng)
+    per_step = max(args.cpu_seconds / max(args.steps, 1), 1.0)
+    base, _ = cpu_baseline(m, haps, quad, props, C, 1.0, per_step)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    threads = base["cores"]
+    pb = O.OracleProblem(haps, m.emit, m.t, m.tran, m.pc, C)
+    n = int(base["sample"].split()[0])
+    for g in range(args.warmup):
+        O.generation(pb, pb.trace(seed=1, generation=g), quad, props, pen_for(g, w.burnin), 0,
+                     min(n, 2 * threads), True, nthreads=threads)
+    t0 = time.perf_counter()
+    for g in range(args.steps):
+        O.generation(pb, pb.trace(seed=1, generation=args.warmup + g), quad, props,
+                     pen_for(args.warmup + g, w.burnin), 0, n, True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    value = args.steps * n * (C + 1) * m.S / dt
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"{args.config}: {m.N} samples x {m.S} sites, C={C}",
+                   "samples": m.N, "sites": m.S, "cycles": C,
+                   "sampler": "uniform over all other haplotypes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} of {m.N} samples per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C_
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from glphase_gb300 import native as nat, synth
+    from glphase_gb300.hmmlike import Engine
+
+    w, m, haps = workload(args, rank)
+    C = args.cycles
+    N, S = m.N, m.S
+    H, wn = haps.shape
+    rng = np.random.default_rng(5 + rank)
+    packed = codebook = None
+    if args.vq:
+        from glphase_gb300.glpack import GLPack
+        gp = GLPack(m.t, np.random.default_rng(1))
+        packed, codebook = gp.packed_gls(), gp.code_book()
+    eng = Engine(m.emit, m.t, m.tran, m.pc, haps, C, device=local, lanes=args.lanes,
+                 packed=packed, codebook=codebook)
+    dev = torch.device("cuda", local)
+    total = args.warmup + args.steps
+    # every step's inputs are staged in HBM before timing starts
+    quads, propss = [], []
+    for g in range(total):
+        q, p = synth.uniform_proposals(N, H, C, rng)
+        quads.append(torch.from_numpy(q.view(np.int32)).to(dev))
+        propss.append(torch.from_numpy(p.view(np.int32)).to(dev))
+    peak = C_.c_double()
+    eng.dev._c(eng.dev.L.glp_measure_fp32_peak(eng.dev.ctx, 200.0, C_.byref(peak)))
+    stream = eng.stream
+
+    def step(g):
+        a = eng.args(quads[g], propss[g], pen_for(g, w.burnin), seed=1234 + rank, generation=g)
+        eng.launch(a)
+        eng.swap()
+
+    for g in range(args.warmup):
+        step(g)
+    eng.finish()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.4)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
+        step(args.warmup + i)
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ck = clocks.stop()
+    eng.finish()
+    per = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    elapsed = evs[0].elapsed_time(evs[-1]) / 1e3
+    ev, rounds, lanes = eng.dev.stats()
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    updates_step = N * (C + 1) * S
+    value = world * args.steps * updates_step / elapsed
+    kernel_ms = float(np.mean(per))
+    achieved = updates_step * FLOPS_PER_UPDATE / (kernel_ms * 1e-3) / 1e12
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(eng, haps, N, S, C, H, wn, w, args, torch)
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        q0, p0 = synth.uniform_proposals(N, H, C, np.random.default_rng(99))
+        base, _ = cpu_baseline(m, haps, q0, p0, C, 1.0, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {
+                "workload": f"{args.config}: {N} samples x {S} sites x C={C} cycles per "
+                            "generation, uniform surrogates over all other haplotypes",
+                "samples": N, "sites": S, "cycles": C, "haplotypes": H,
+                "emission": "vq4" if args.vq else "f32",
+                "lanes_per_sample": lanes, "evaluations_per_step": ev,
+                "speculative_rounds": rounds,
+                "useful_fraction": round(N * (C + 1) / max(ev, 1), 4),
+                "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6),
+                "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value,
+                         "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
+                         "traffic": None,
+                         "note": "29 algorithmic FP32 flops per update; peak = measured FP32 "
+                                 "FMA rate on this GPU (glp_measure_fp32_peak)"},
+            "clocks": ck,
+            "gpu_launches": args.steps,
+            "kernel_ms": kernel_ms,
+        }
+        if e2e:
+            line["e2e"] = e2e
+        if base:
+            line["cpu_baseline"] = base
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(eng, haps, N, S, C, H, wn, w, args, torch):
+    """Same metric through the host-pointer C-ABI call: every step copies the
+    haplotypes, quadruples and proposals in from pinned host memory and the
+    quadruples, the new haplotype rows and the log-likelihoods back."""
+    from glphase_gb300 import synth
+
+    def pinned(shape, dtype):
+        t = torch.empty(shape, dtype=dtype, pin_memory=True)
+        return t.numpy()
+
+    h = pinned((H, wn), torch.int64).view(np.uint64)
+    h[:] = haps
+    hn = pinned((H, wn), torch.int64).view(np.uint64)
+    hn[:] = haps
+    rng = np.random.default_rng(17)
+    qs, ps = [], []
+    total = args.warmup + args.steps
+    for g in range(total):
+        q, p = synth.uniform_proposals(N, H, C, rng)
+        qq = pinned((4, N), torch.int32).view(np.uint32)
+        qq[:] = q
+        pp = pinned((C, N), torch.int32).view(np.uint32)
+        pp[:] = p
+        qs.append(qq)
+        ps.append(pp)
+    qout = pinned((4, N), torch.int32).view(np.uint32)
+    like = pinned((N,), torch.float64)
+    cur, nxt = h, hn
+    for g in range(args.warmup):
+        eng.run_host(cur, qs[g], ps[g], pen_for(g, w.burnin), 99, g, nxt, qout, like)
+        nxt[2 * N:] = cur[2 * N:]
+        cur, nxt = nxt, cur
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        g = args.warmup + i
+        eng.run_host(cur, qs[g], ps[g], pen_for(g, w.burnin), 99, g, nxt, qout, like)
+        cur, nxt = nxt, cur
+    dt = time.perf_counter() - t0
+    h2d = H * wn * 8 + 4 * N * 4 + C * N * 4
+    d2h = 4 * N * 4 + 2 * N * wn * 8 + N * 8
+    return {"value": args.steps * N * (C + 1) * S / dt, "unit": UNIT,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "api": "glp_run_generation_host (pinned host buffers)"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

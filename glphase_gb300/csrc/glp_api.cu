@@ -1,0 +1,692 @@
+// glp_api.cu -- host side of the C ABI declared in include/glphase_gpu.h.
+//
+// Owns the device-resident model inputs of one phasing problem (transition
+// table, mutation matrix, emissions or VQ codes, genotype probabilities) and
+// the per-generation work buffers, and launches the generation kernel of
+// glp_kernels.cuh.  Every entry point returns a status code; nothing exits,
+// throws across the boundary or resets the device (the reference's
+// HMMLikeCUDA calls exit(EXIT_FAILURE) on CUDA errors, src/hmmLike.cu:240-300,
+// and cudaDeviceReset in Cleanup, src/hmmLike.cu:396).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/glphase_gpu.h"
+#include "glp_kernels.cuh"
+
+struct glp_ctx {
+  int device = 0;
+  int sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // model inputs
+  uint32_t S = 0;           // sites of tran
+  float4 *d_tran4 = nullptr;
+  float pc[16] = {0};
+  bool have_pc = false;
+  float codebook[32] = {0};
+  bool have_codebook = false;
+  float4 *d_vq = nullptr;   // [16] emission per VQ code
+  uint32_t *d_packed = nullptr;
+  size_t packed_words = 0;
+  float4 *d_emit = nullptr;
+  float *d_prob = nullptr;
+  uint32_t eN = 0, eS = 0;  // shape of emit/prob
+  // work buffers
+  uint32_t *d_counter = nullptr;
+  unsigned long long *d_stats = nullptr;
+  int *d_error = nullptr;
+  float4 *d_beta = nullptr;
+  size_t beta_cap = 0;
+  // staging for the host-pointer entry points
+  uint64_t *d_haps = nullptr, *d_hnew = nullptr;
+  size_t haps_cap = 0, hnew_cap = 0;
+  uint32_t *d_quad = nullptr, *d_quad_out = nullptr, *d_props = nullptr;
+  size_t quad_cap = 0, quad_out_cap = 0, props_cap = 0;
+  uint8_t *d_tr_slot = nullptr, *d_acc = nullptr;
+  double *d_tr_u = nullptr, *d_like = nullptr, *d_evals = nullptr;
+  float *d_tr_work = nullptr;
+  size_t tr_slot_cap = 0, acc_cap = 0, tr_u_cap = 0, like_cap = 0, evals_cap = 0,
+         tr_work_cap = 0;
+  // tuning and statistics
+  uint32_t lanes = 0;        // 0 = automatic
+  uint32_t lanes_used = 4;
+  double last_accept = -1.0; // acceptance rate of the last generation
+  uint32_t last_N = 0, last_C = 0;
+  unsigned long long last_stats[3] = {0, 0, 0};
+};
+
+namespace {
+
+int fail(glp_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c)
+    c->err = buf;
+  return code;
+}
+
+#define GLP_CUDA(c, call)                                                                   \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail((c), e_ == cudaErrorMemoryAllocation ? GLP_ERR_NOMEM : GLP_ERR_CUDA,     \
+                  "%s failed: %s", #call, cudaGetErrorString(e_));                          \
+  } while (0)
+
+template <class T>
+int ensure(glp_ctx *c, T *&ptr, size_t &cap, size_t count) {
+  if (count <= cap && ptr)
+    return GLP_OK;
+  if (ptr)
+    cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  GLP_CUDA(c, cudaMalloc((void **)&ptr, std::max<size_t>(count, 1) * sizeof(T)));
+  cap = count;
+  return GLP_OK;
+}
+
+template <class T>
+void release(T *&p) {
+  if (p)
+    cudaFree(p);
+  p = nullptr;
+}
+
+// FillEmit of every codebook entry (hmmLike.cu:12-44): G = (cb0, cb1,
+// max(1 - cb0 - cb1, 0)), emit[i] = pc[i][0] G0 + pc[i][1] G1 + pc[i][2] G1
+// + pc[i][3] G2.  Host code is built with -ffp-contract=off, so each term is
+// rounded exactly as in the CPU reference.
+int upload_vq_table(glp_ctx *c) {
+  if (!c->have_pc || !c->have_codebook)
+    return GLP_OK;
+  float4 tab[16];
+  for (int code = 0; code < 16; ++code) {
+    const float g0 = c->codebook[2 * code], g1 = c->codebook[2 * code + 1];
+    const float rest = 1 - g0 - g1;
+    const float g2 = rest > 0.0f ? rest : 0.0f;
+    float em[4];
+    for (int i = 0; i < 4; ++i) {
+      const float a = c->pc[i * 4 + 0] * g0;
+      const float b = c->pc[i * 4 + 1] * g1;
+      const float d = c->pc[i * 4 + 2] * g1;
+      const float f = c->pc[i * 4 + 3] * g2;
+      em[i] = ((a + b) + d) + f;
+    }
+    tab[code] = make_float4(em[0], em[1], em[2], em[3]);
+  }
+  if (!c->d_vq)
+    GLP_CUDA(c, cudaMalloc((void **)&c->d_vq, sizeof(tab)));
+  GLP_CUDA(c, cudaMemcpy(c->d_vq, tab, sizeof(tab), cudaMemcpyHostToDevice));
+  return GLP_OK;
+}
+
+using KernelFn = void (*)(const glp::GenParams);
+
+template <int P>
+KernelFn pick_kernel(bool vq) {
+  return vq ? glp::generation_kernel<P, glp::EmitVQ> : glp::generation_kernel<P, glp::EmitF32>;
+}
+
+KernelFn kernel_for(uint32_t lanes, bool vq) {
+  switch (lanes) {
+    case 1: return pick_kernel<1>(vq);
+    case 2: return pick_kernel<2>(vq);
+    case 4: return pick_kernel<4>(vq);
+    case 8: return pick_kernel<8>(vq);
+    case 16: return pick_kernel<16>(vq);
+    default: return pick_kernel<32>(vq);
+  }
+}
+
+// Speculation width: the expected useful fraction of a round of P
+// evaluations at acceptance rate a is (1 - (1-a)^P) / (a P); lanes are
+// useful only while N*P does not exceed the threads the GPU keeps resident.
+uint32_t choose_lanes(const glp_ctx *c, uint32_t N) {
+  if (c->lanes)
+    return c->lanes;
+  const double a = c->last_accept < 0 ? 0.12 : std::max(c->last_accept, 1e-3);
+  const double resident = (double)c->sms * 1024.0;
+  uint32_t best = 1;
+  double best_score = 0;
+  for (uint32_t P = 1; P <= 32; P <<= 1) {
+    const double eff = (1.0 - std::pow(1.0 - a, (double)P)) / (a * P);
+    const double fill = std::min(1.0, (double)N * P / resident);
+    const double score = eff * fill;
+    if (score > best_score * 1.02) {
+      best_score = score;
+      best = P;
+    }
+  }
+  return best;
+}
+
+int check_ctx(glp_ctx *c) {
+  if (!c)
+    return GLP_ERR_ARG;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess)
+    return fail(c, GLP_ERR_CUDA, "cudaSetDevice(%d): %s", c->device, cudaGetErrorString(e));
+  return GLP_OK;
+}
+
+int launch_generation(glp_ctx *c, const glp_generation_args *a) {
+  const bool vq = (a->flags & GLP_GEN_VQ) != 0;
+  const bool work = (a->flags & GLP_GEN_NO_WORK) == 0;
+  const uint32_t N = a->num_samples, S = a->num_sites, C = a->num_cycles, H = a->num_haps;
+  if (N == 0 || S == 0)
+    return fail(c, GLP_ERR_ARG, "num_samples and num_sites must be positive");
+  if (H < 2 || (uint64_t)2 * N > H)
+    return fail(c, GLP_ERR_ARG, "num_haps=%u must be >= 2*num_samples=%u", H, 2 * N);
+  if (!a->haps || !a->hap_idxs_in || !a->hap_idxs_out || (C && !a->props))
+    return fail(c, GLP_ERR_ARG, "haps, hap_idxs_in/out and props are required");
+  if (work && !a->hnew)
+    return fail(c, GLP_ERR_ARG, "hnew is required unless GLP_GEN_NO_WORK is set");
+  if (!c->d_tran4 || c->S != S)
+    return fail(c, GLP_ERR_STATE, "transition matrix not set for %u sites", S);
+  if (!c->have_pc)
+    return fail(c, GLP_ERR_STATE, "mutation matrix not set");
+  if (vq) {
+    if (!c->d_packed || !c->d_vq)
+      return fail(c, GLP_ERR_STATE, "packed GLs and codebook are required in VQ mode");
+    const size_t want = (size_t)N * ((S + 7) / 8);
+    if (c->packed_words != want)
+      return fail(c, GLP_ERR_ARG, "packed GLs have %zu words, expected %zu", c->packed_words,
+                  want);
+  }
+  if (!vq || work) {
+    if (!c->d_emit || c->eN != N || c->eS != S)
+      return fail(c, GLP_ERR_STATE, "emission not set for N=%u S=%u", N, S);
+  }
+  if (work && !c->d_prob)
+    return fail(c, GLP_ERR_STATE, "genotype probabilities not set (needed by hmm_work)");
+  const bool tr = a->trace_slot || a->trace_accept || a->trace_work;
+  if (tr && !(a->trace_slot && a->trace_accept && a->trace_work))
+    return fail(c, GLP_ERR_ARG, "a replay trace needs slot, accept and work arrays");
+  if (!(a->pen > 0.0f) || !std::isfinite(a->pen))
+    return fail(c, GLP_ERR_ARG, "pen must be positive and finite");
+  if (work) {
+    int rc = ensure(c, c->d_beta, c->beta_cap, (size_t)N * S);
+    if (rc)
+      return rc;
+  }
+
+  glp::GenParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.N = N;
+  p.S = S;
+  p.C = C;
+  p.H = H;
+  p.wn = (S + 63) / 64;
+  p.emit_mode = vq ? GLP_EMIT_VQ : GLP_EMIT_FLOAT;
+  p.haps = a->haps;
+  p.hnew = a->hnew;
+  p.emit = c->d_emit;
+  p.prob = c->d_prob;
+  p.tran4 = c->d_tran4;
+  p.packed = c->d_packed;
+  p.vq_table = vq ? c->d_vq : nullptr;
+  p.quad_in = a->hap_idxs_in;
+  p.quad_out = a->hap_idxs_out;
+  p.props = a->props;
+  p.tr_slot = a->trace_slot;
+  p.tr_u = a->trace_accept;
+  p.tr_work = a->trace_work;
+  p.like_out = a->like_out;
+  p.eval_trace = a->eval_trace;
+  p.accept_trace = a->accept_trace;
+  p.beta = c->d_beta;
+  p.counter = c->d_counter;
+  p.stats = c->d_stats;
+  p.error = c->d_error;
+  std::memcpy(p.pc, c->pc, sizeof(p.pc));
+  p.pen = a->pen;
+  p.seed = a->seed;
+  p.generation = a->generation;
+  p.do_work = work ? 1u : 0u;
+
+  const uint32_t P = choose_lanes(c, N);
+  KernelFn fn = kernel_for(P, vq);
+  int occ = 0;
+  GLP_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, 0));
+  occ = std::max(occ, 1);
+  const uint64_t groups_per_block = (uint64_t)glp::kThreads / P;
+  const uint64_t want_blocks = ((uint64_t)N + groups_per_block - 1) / groups_per_block;
+  const uint64_t max_blocks = (uint64_t)occ * c->sms;
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(want_blocks, max_blocks));
+
+  GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
+  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
+  fn<<<grid, glp::kThreads, 0, c->stream>>>(p);
+  GLP_CUDA(c, cudaGetLastError());
+  c->lanes_used = P;
+  c->last_N = N;
+  c->last_C = C;
+  return GLP_OK;
+}
+
+// 8 independent FMA chains per thread, 4 per loop trip kept live by a
+// dependency through the loop counter; the result is stored so nothing is
+// eliminated.
+__global__ void __launch_bounds__(256) fp32_probe_kernel(float *out, int iters, float a,
+                                                         float b) {
+  float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1e-7f, x2 = x0 + 2e-7f, x3 = x0 + 3e-7f;
+  float x4 = x0 + 4e-7f, x5 = x0 + 5e-7f, x6 = x0 + 6e-7f, x7 = x0 + 7e-7f;
+#pragma unroll 4
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b);
+    x1 = fmaf(x1, a, b);
+    x2 = fmaf(x2, a, b);
+    x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b);
+    x5 = fmaf(x5, a, b);
+    x6 = fmaf(x6, a, b);
+    x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+}
+
+}  // namespace
+
+extern "C" {
+
+int glp_measure_fp32_peak(glp_ctx *c, float ms_target, double *tflops) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!tflops || !(ms_target > 0))
+    return fail(c, GLP_ERR_ARG, "tflops must be non-null and ms_target positive");
+  const int threads = 256, blocks = c->sms * 8;
+  float *out = nullptr;
+  GLP_CUDA(c, cudaMalloc((void **)&out, sizeof(float) * threads * blocks));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int iters = 1 << 14;
+  double best = 0;
+  for (int rep = 0; rep < 6; ++rep) {
+    cudaEventRecord(e0, c->stream);
+    fp32_probe_kernel<<<blocks, threads, 0, c->stream>>>(out, iters, 0.999999f, 1e-7f);
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+    if (rep >= 2)
+      best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    if (ms > 0 && ms < ms_target)
+      iters = (int)std::min<double>(iters * (ms_target / ms), 1 << 26);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  GLP_CUDA(c, cudaGetLastError());
+  *tflops = best;
+  return GLP_OK;
+}
+
+
+int glp_check_device(int device, int *device_count, int *cc_major, int *cc_minor,
+                     int *sm_count) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (device_count)
+    *device_count = (e == cudaSuccess) ? n : 0;
+  if (e != cudaSuccess || n == 0)
+    return GLP_ERR_DEVICE;
+  if (device < 0 || device >= n)
+    return GLP_ERR_ARG;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+    return GLP_ERR_CUDA;
+  if (cc_major)
+    *cc_major = prop.major;
+  if (cc_minor)
+    *cc_minor = prop.minor;
+  if (sm_count)
+    *sm_count = prop.multiProcessorCount;
+  return (prop.major == 10 && prop.minor == 3) ? GLP_OK : GLP_ERR_DEVICE;
+}
+
+int glp_create(int device, glp_ctx **out) {
+  if (!out)
+    return GLP_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+    return GLP_ERR_DEVICE;
+  if (device < 0 || device >= n)
+    return GLP_ERR_ARG;
+  glp_ctx *c = new glp_ctx();
+  c->device = device;
+  int rc = check_ctx(c);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc((void **)&c->d_counter, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc((void **)&c->d_stats, 3 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc((void **)&c->d_error, sizeof(int)) != cudaSuccess ||
+      cudaMemset(c->d_error, 0, sizeof(int)) != cudaSuccess) {
+    glp_destroy(c);
+    return GLP_ERR_CUDA;
+  }
+  c->sms = prop.multiProcessorCount;
+  c->stream = c->own_stream;
+  *out = c;
+  return GLP_OK;
+}
+
+void glp_destroy(glp_ctx *c) {
+  if (!c)
+    return;
+  cudaSetDevice(c->device);
+  if (c->stream)
+    cudaStreamSynchronize(c->stream);
+  release(c->d_tran4);
+  release(c->d_vq);
+  release(c->d_packed);
+  release(c->d_emit);
+  release(c->d_prob);
+  release(c->d_counter);
+  release(c->d_stats);
+  release(c->d_error);
+  release(c->d_beta);
+  release(c->d_haps);
+  release(c->d_hnew);
+  release(c->d_quad);
+  release(c->d_quad_out);
+  release(c->d_props);
+  release(c->d_tr_slot);
+  release(c->d_acc);
+  release(c->d_tr_u);
+  release(c->d_like);
+  release(c->d_evals);
+  release(c->d_tr_work);
+  if (c->own_stream)
+    cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+const char *glp_last_error(const glp_ctx *c) {
+  if (!c)
+    return "null context";
+  return c->err.c_str();
+}
+
+int glp_set_stream(glp_ctx *c, void *stream) {
+  if (!c)
+    return GLP_ERR_ARG;
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return GLP_OK;
+}
+
+int glp_set_tran(glp_ctx *c, const float *tran, uint32_t S) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!tran || S == 0)
+    return fail(c, GLP_ERR_ARG, "tran must be non-null with num_sites > 0");
+  std::vector<float4> t4(S);
+  t4[0] = make_float4(1.f, 0.f, 0.f, 0.f);  // row 0 is unused by the recursion
+  for (uint32_t m = 1; m < S; ++m)
+    t4[m] = make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2], 0.f);
+  if (c->S != S) {
+    release(c->d_tran4);
+    GLP_CUDA(c, cudaMalloc((void **)&c->d_tran4, sizeof(float4) * S));
+    c->S = S;
+  }
+  GLP_CUDA(c, cudaMemcpy(c->d_tran4, t4.data(), sizeof(float4) * S, cudaMemcpyHostToDevice));
+  return GLP_OK;
+}
+
+int glp_set_mutation_mat(glp_ctx *c, const float *pc16) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!pc16)
+    return fail(c, GLP_ERR_ARG, "pc must be non-null");
+  std::memcpy(c->pc, pc16, sizeof(c->pc));
+  c->have_pc = true;
+  return upload_vq_table(c);
+}
+
+int glp_set_codebook(glp_ctx *c, const float *codebook, uint32_t entries) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!codebook || entries != 16)
+    return fail(c, GLP_ERR_ARG, "codebook must hold 16 (RR, Het) entries, got %u", entries);
+  std::memcpy(c->codebook, codebook, sizeof(c->codebook));
+  c->have_codebook = true;
+  return upload_vq_table(c);
+}
+
+int glp_set_packed_gls(glp_ctx *c, const uint32_t *packed, size_t n) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!packed || n == 0)
+    return fail(c, GLP_ERR_ARG, "packed GLs must be non-empty");
+  if (n != c->packed_words) {
+    release(c->d_packed);
+    c->packed_words = 0;
+    GLP_CUDA(c, cudaMalloc((void **)&c->d_packed, sizeof(uint32_t) * n));
+    c->packed_words = n;
+  }
+  GLP_CUDA(c, cudaMemcpy(c->d_packed, packed, sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+  return GLP_OK;
+}
+
+int glp_set_emission(glp_ctx *c, const float *emit, const float *prob, uint32_t N, uint32_t S) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!emit || N == 0 || S == 0)
+    return fail(c, GLP_ERR_ARG, "emit must be non-null with positive N and S");
+  const size_t ns = (size_t)N * S;
+  if (c->eN != N || c->eS != S) {
+    release(c->d_emit);
+    release(c->d_prob);
+    c->eN = c->eS = 0;
+    GLP_CUDA(c, cudaMalloc((void **)&c->d_emit, sizeof(float4) * ns));
+    GLP_CUDA(c, cudaMalloc((void **)&c->d_prob, sizeof(float) * 3 * ns));
+    c->eN = N;
+    c->eS = S;
+  }
+  GLP_CUDA(c, cudaMemcpy(c->d_emit, emit, sizeof(float4) * ns, cudaMemcpyHostToDevice));
+  if (prob)
+    GLP_CUDA(c, cudaMemcpy(c->d_prob, prob, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice));
+  return GLP_OK;
+}
+
+int glp_run_generation(glp_ctx *c, const glp_generation_args *a) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!a)
+    return fail(c, GLP_ERR_ARG, "args must be non-null");
+  return launch_generation(c, a);
+}
+
+int glp_finish(glp_ctx *c) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  GLP_CUDA(c, cudaStreamSynchronize(c->stream));
+  GLP_CUDA(c, cudaGetLastError());
+  int h_err = 0;
+  GLP_CUDA(c, cudaMemcpy(&h_err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost));
+  GLP_CUDA(c, cudaMemcpy(c->last_stats, c->d_stats, sizeof(c->last_stats),
+                         cudaMemcpyDeviceToHost));
+  if (c->last_N && c->last_C)
+    c->last_accept = (double)c->last_stats[2] / ((double)c->last_N * c->last_C);
+  if (h_err) {
+    GLP_CUDA(c, cudaMemset(c->d_error, 0, sizeof(int)));
+    return fail(c, GLP_ERR_INDEX, "a haplotype index >= num_haps reached the device");
+  }
+  return GLP_OK;
+}
+
+int glp_run_generation_host(glp_ctx *c, const glp_generation_args *a) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!a || !a->haps || !a->hap_idxs_in || !a->hap_idxs_out || (a->num_cycles && !a->props))
+    return fail(c, GLP_ERR_ARG, "haps, hap_idxs_in/out and props are required");
+  const uint32_t N = a->num_samples, S = a->num_sites, C = a->num_cycles, H = a->num_haps;
+  const bool work = (a->flags & GLP_GEN_NO_WORK) == 0;
+  if (work && !a->hnew)
+    return fail(c, GLP_ERR_ARG, "hnew is required unless GLP_GEN_NO_WORK is set");
+  const size_t wn = (S + 63) / 64;
+  const size_t hw = (size_t)H * wn;
+  if ((rc = ensure(c, c->d_haps, c->haps_cap, hw)))
+    return rc;
+  if (work && (rc = ensure(c, c->d_hnew, c->hnew_cap, hw)))
+    return rc;
+  if ((rc = ensure(c, c->d_quad, c->quad_cap, (size_t)4 * N)))
+    return rc;
+  if ((rc = ensure(c, c->d_quad_out, c->quad_out_cap, (size_t)4 * N)))
+    return rc;
+  if ((rc = ensure(c, c->d_props, c->props_cap, (size_t)C * N)))
+    return rc;
+  cudaStream_t st = c->stream;
+  // hnew needs no upload: the kernel writes every word of rows 0..2N-1 and
+  // only those rows are copied back.
+  GLP_CUDA(c, cudaMemcpyAsync(c->d_haps, a->haps, hw * 8, cudaMemcpyHostToDevice, st));
+  GLP_CUDA(c, cudaMemcpyAsync(c->d_quad, a->hap_idxs_in, (size_t)16 * N,
+                              cudaMemcpyHostToDevice, st));
+  if (C)
+    GLP_CUDA(c, cudaMemcpyAsync(c->d_props, a->props, (size_t)4 * C * N,
+                                cudaMemcpyHostToDevice, st));
+  glp_generation_args d = *a;
+  d.haps = c->d_haps;
+  d.hnew = work ? c->d_hnew : nullptr;
+  d.hap_idxs_in = c->d_quad;
+  d.hap_idxs_out = c->d_quad_out;
+  d.props = c->d_props;
+  if (a->trace_slot || a->trace_accept || a->trace_work) {
+    if (!(a->trace_slot && a->trace_accept && a->trace_work))
+      return fail(c, GLP_ERR_ARG, "a replay trace needs slot, accept and work arrays");
+    if ((rc = ensure(c, c->d_tr_slot, c->tr_slot_cap, (size_t)N * C)) ||
+        (rc = ensure(c, c->d_tr_u, c->tr_u_cap, (size_t)N * C)) ||
+        (rc = ensure(c, c->d_tr_work, c->tr_work_cap, (size_t)N * S)))
+      return rc;
+    GLP_CUDA(c, cudaMemcpyAsync(c->d_tr_slot, a->trace_slot, (size_t)N * C,
+                                cudaMemcpyHostToDevice, st));
+    GLP_CUDA(c, cudaMemcpyAsync(c->d_tr_u, a->trace_accept, (size_t)8 * N * C,
+                                cudaMemcpyHostToDevice, st));
+    GLP_CUDA(c, cudaMemcpyAsync(c->d_tr_work, a->trace_work, (size_t)4 * N * S,
+                                cudaMemcpyHostToDevice, st));
+    d.trace_slot = c->d_tr_slot;
+    d.trace_accept = c->d_tr_u;
+    d.trace_work = c->d_tr_work;
+  }
+  if (a->like_out) {
+    if ((rc = ensure(c, c->d_like, c->like_cap, N)))
+      return rc;
+    d.like_out = c->d_like;
+  }
+  if (a->eval_trace) {
+    if ((rc = ensure(c, c->d_evals, c->evals_cap, (size_t)N * (C + 1))))
+      return rc;
+    d.eval_trace = c->d_evals;
+  }
+  if (a->accept_trace) {
+    if ((rc = ensure(c, c->d_acc, c->acc_cap, std::max<size_t>((size_t)N * C, 1))))
+      return rc;
+    d.accept_trace = c->d_acc;
+  }
+  if ((rc = launch_generation(c, &d)))
+    return rc;
+  GLP_CUDA(c, cudaMemcpyAsync(a->hap_idxs_out, c->d_quad_out, (size_t)16 * N,
+                              cudaMemcpyDeviceToHost, st));
+  if (work)
+    GLP_CUDA(c, cudaMemcpyAsync(a->hnew, c->d_hnew, (size_t)2 * N * wn * 8,
+                                cudaMemcpyDeviceToHost, st));
+  if (a->like_out)
+    GLP_CUDA(c, cudaMemcpyAsync(a->like_out, c->d_like, (size_t)8 * N, cudaMemcpyDeviceToHost,
+                                st));
+  if (a->eval_trace)
+    GLP_CUDA(c, cudaMemcpyAsync(a->eval_trace, c->d_evals, (size_t)8 * N * (C + 1),
+                                cudaMemcpyDeviceToHost, st));
+  if (a->accept_trace && C)
+    GLP_CUDA(c, cudaMemcpyAsync(a->accept_trace, c->d_acc, (size_t)N * C,
+                                cudaMemcpyDeviceToHost, st));
+  return glp_finish(c);
+}
+
+int glp_run_hmm_on_device(glp_ctx *c, const uint64_t *hap_panel, size_t panel_words,
+                          const uint32_t *extra_prop_haps, uint32_t num_sites,
+                          uint32_t num_samples, uint32_t num_cycles, uint32_t *hap_idxs,
+                          uint64_t seed) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!hap_panel || !hap_idxs || (num_cycles && !extra_prop_haps))
+    return fail(c, GLP_ERR_ARG, "hap_panel, extra_prop_haps and hap_idxs are required");
+  const size_t wn = (num_sites + 63) / 64;
+  if (wn == 0 || panel_words % wn)
+    return fail(c, GLP_ERR_ARG, "panel of %zu words is not a whole number of %zu-word haps",
+                panel_words, wn);
+  const size_t H = panel_words / wn;
+  if (H > 0xffffffffu || H < 2 * (size_t)num_samples)
+    return fail(c, GLP_ERR_ARG, "panel holds %zu haplotypes for %u samples", H, num_samples);
+  std::vector<uint32_t> out(4 * (size_t)num_samples);
+  glp_generation_args a;
+  std::memset(&a, 0, sizeof(a));
+  a.num_samples = num_samples;
+  a.num_sites = num_sites;
+  a.num_cycles = num_cycles;
+  a.num_haps = (uint32_t)H;
+  a.haps = hap_panel;
+  a.hap_idxs_in = hap_idxs;
+  a.hap_idxs_out = out.data();
+  a.props = extra_prop_haps;
+  a.pen = 1.0f;  // findHapSet accepts with S = 1 (hmmLike.cu:159)
+  a.seed = seed;
+  a.flags = GLP_GEN_VQ | GLP_GEN_NO_WORK;
+  rc = glp_run_generation_host(c, &a);
+  if (rc)
+    return rc;
+  std::memcpy(hap_idxs, out.data(), out.size() * sizeof(uint32_t));
+  return GLP_OK;
+}
+
+int glp_set_lanes_per_sample(glp_ctx *c, uint32_t lanes) {
+  if (!c)
+    return GLP_ERR_ARG;
+  if (lanes && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 &&
+      lanes != 32)
+    return fail(c, GLP_ERR_ARG, "lanes per sample must be 0, 1, 2, 4, 8, 16 or 32");
+  c->lanes = lanes;
+  return GLP_OK;
+}
+
+int glp_get_stats(glp_ctx *c, uint64_t *evaluations, uint64_t *rounds, uint32_t *lanes_used) {
+  if (!c)
+    return GLP_ERR_ARG;
+  if (evaluations)
+    *evaluations = c->last_stats[0];
+  if (rounds)
+    *rounds = c->last_stats[1];
+  if (lanes_used)
+    *lanes_used = c->lanes_used;
+  return GLP_OK;
+}
+
+}  // extern "C"

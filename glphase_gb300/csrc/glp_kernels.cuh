@@ -1,0 +1,631 @@
+// glp_kernels.cuh -- sm_103a kernels for one MH generation of GLPhase's
+// haplotype sampler: per-sample Metropolis-Hastings over surrogate-parent
+// quadruples scored by the 4-state HMM forward likelihood, with the final
+// haplotype sampling (hmm_work) fused into the same launch.
+//
+// Reference semantics (paths relative to the reference project root):
+//   likelihood  Impute::hmm_like      src/impute.cpp:327-376 (CPU, float emit)
+//               HMMLikeCUDA::hmmLike  src/hmmLike.cu:53-142  (GPU, VQ GLs)
+//   MH chain    findHapSet            src/hmmLike.cu:145-217
+//               Insti::solve          src/insti.cpp:1478-1551
+//               MHSampler::SampleHap  src/MHSampler.hpp:81-96
+//   sampling    Impute::hmm_work      src/impute.cpp:380-485
+//
+// Work decomposition (one warp = 32/P groups of P lanes, one sample per group):
+//  * A sample's MH chain is inherently sequential, so its parallelism comes
+//    from speculation: the P lanes of a group evaluate the next P evaluations
+//    of the chain (the current quadruple and the next P-1 proposals), each
+//    built on the current state, i.e. assuming all earlier ones are rejected.
+//    The group then replays the accept rule in order; evaluations after the
+//    first accepted proposal are discarded and re-evaluated from the new
+//    state.  Decisions are exactly those of the sequential chain.
+//  * Each lane computes one likelihood as a forward pass over the first half
+//    of the words and a backward pass over the second half, interleaved in
+//    one instruction stream (8 independent FMA chains), joined by a 4-term
+//    dot product: L = alpha_{h-1} . beta_{h-1}.  Same flop count as the
+//    plain forward pass, half the latency.
+//  * Scaling is by exact powers of two with an integer exponent per half;
+//    the log-likelihood is assembled in binary64 (log(dot) + k*ln2).
+//  * hmm_work runs one sample per lane in the reference's exact binary32
+//    operation order (no contraction), on batches of 32 finished samples
+//    collected per warp, so its output bits match the CPU reference.
+//
+// Memory (all resident in HBM across generations):
+//   haps/hnew  uint64 [H][wn] hap-major   (parent words: L2-resident gathers)
+//   emit       float4 [N][S]              (streamed, shared by a group)
+//   packed     uint32 [ceil(S/8)][N]      (VQ codes; 16-entry table in smem)
+//   tran4      float4 [S]                 (t0, t1, t2, 0); tran4[0] = (1,0,0,0)
+//   beta       float4 [N][S]              (hmm_work scratch)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "glp_rng.h"
+
+namespace glp {
+
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr float kTiny = 0x1p-64f;
+constexpr float kHuge = 0x1p64f;
+
+struct GenParams {
+  uint32_t N, S, C, H, wn, emit_mode;
+  const uint64_t *__restrict__ haps;
+  uint64_t *__restrict__ hnew;
+  const float4 *__restrict__ emit;
+  const float *__restrict__ prob;
+  const float4 *__restrict__ tran4;
+  const uint32_t *__restrict__ packed;
+  const float4 *__restrict__ vq_table;
+  const uint32_t *__restrict__ quad_in;
+  uint32_t *__restrict__ quad_out;
+  const uint32_t *__restrict__ props;
+  const uint8_t *__restrict__ tr_slot;
+  const double *__restrict__ tr_u;
+  const float *__restrict__ tr_work;
+  double *__restrict__ like_out;
+  double *__restrict__ eval_trace;
+  uint8_t *__restrict__ accept_trace;
+  float4 *__restrict__ beta;
+  uint32_t *__restrict__ counter;
+  unsigned long long *__restrict__ stats;
+  int *__restrict__ error;
+  float pc[16];
+  float pen;
+  uint64_t seed;
+  uint32_t generation;
+  uint32_t do_work;
+};
+
+// ---------------------------------------------------------------------------
+// Emission sources.  Both hand out the 4 emission values of a site,
+// e[(father_bit << 1) | mother_bit] (impute.cpp:338-342).
+
+struct EmitF32 {
+  const float4 *row;
+  __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *) {
+    row = p.emit + (size_t)s * p.S;
+  }
+  __device__ __forceinline__ void prep(const GenParams &, uint32_t) {}
+  __device__ __forceinline__ float4 get(uint32_t m) const { return __ldg(row + m); }
+};
+
+// 4-bit VQ codes, eight per uint32, most significant nibble first
+// (glPack.cpp:104-109, hmmLike.cu:20-24); table[c] = FillEmit(decode(c)).
+struct EmitVQ {
+  const uint32_t *col;
+  const float4 *table;
+  uint32_t stride, nblk;
+  uint32_t pk[8];
+  __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *tab) {
+    col = p.packed + s;
+    stride = p.N;
+    nblk = (p.S + 7) >> 3;
+    table = tab;
+  }
+  __device__ __forceinline__ void prep(const GenParams &, uint32_t w) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t b = w * 8 + i;
+      pk[i] = b < nblk ? __ldg(col + (size_t)b * stride) : 0u;
+    }
+  }
+  __device__ __forceinline__ float4 get(uint32_t m) const {
+    const uint32_t j = m & 63u;
+    const uint32_t code = (pk[j >> 3] >> (28u - 4u * (j & 7u))) & 15u;
+    return table[code];
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Forward / backward steps of the 4-state recursion (impute.cpp:353-373).
+
+struct FState {
+  float l00, l01, l10, l11, p1, p2;
+  int k;
+};
+struct BState {
+  float b00, b01, b10, b11;
+  int k;
+};
+
+__device__ __forceinline__ void select4(const float4 e, bool a0, bool a1, bool c0,
+                                        bool c1, float &s00, float &s01, float &s10,
+                                        float &s11) {
+  const float lo0 = a0 ? e.z : e.x, hi0 = a0 ? e.w : e.y;
+  const float lo1 = a1 ? e.z : e.x, hi1 = a1 ? e.w : e.y;
+  s00 = c0 ? hi0 : lo0;
+  s01 = c1 ? hi0 : lo0;
+  s10 = c0 ? hi1 : lo1;
+  s11 = c1 ? hi1 : lo1;
+}
+
+__device__ __forceinline__ void fwd_step(FState &f, const float4 t, float s00, float s01,
+                                         float s10, float s11) {
+  const float b00 = fmaf(f.l11, t.z, fmaf(f.p1, t.y, f.l00 * t.x));
+  const float b01 = fmaf(f.l10, t.z, fmaf(f.p2, t.y, f.l01 * t.x));
+  const float b10 = fmaf(f.l01, t.z, fmaf(f.p2, t.y, f.l10 * t.x));
+  const float b11 = fmaf(f.l00, t.z, fmaf(f.p1, t.y, f.l11 * t.x));
+  f.l00 = b00 * s00;
+  f.l01 = b01 * s01;
+  f.l10 = b10 * s10;
+  f.l11 = b11 * s11;
+  f.p1 = f.l01 + f.l10;
+  f.p2 = f.l00 + f.l11;
+  if (f.p1 + f.p2 < kTiny) {
+    f.l00 *= kHuge;
+    f.l01 *= kHuge;
+    f.l10 *= kHuge;
+    f.l11 *= kHuge;
+    f.p1 *= kHuge;
+    f.p2 *= kHuge;
+    f.k -= 64;
+  }
+}
+
+// beta_{m-1} = T_m D_m beta_m (T symmetric, so the forward formulas apply).
+__device__ __forceinline__ void bwd_step(BState &b, const float4 t, float s00, float s01,
+                                         float s10, float s11) {
+  float v00 = b.b00 * s00, v01 = b.b01 * s01, v10 = b.b10 * s10, v11 = b.b11 * s11;
+  float q1 = v01 + v10, q2 = v00 + v11;
+  if (q1 + q2 < kTiny) {
+    v00 *= kHuge;
+    v01 *= kHuge;
+    v10 *= kHuge;
+    v11 *= kHuge;
+    q1 *= kHuge;
+    q2 *= kHuge;
+    b.k -= 64;
+  }
+  b.b00 = fmaf(v11, t.z, fmaf(q1, t.y, v00 * t.x));
+  b.b01 = fmaf(v10, t.z, fmaf(q2, t.y, v01 * t.x));
+  b.b10 = fmaf(v01, t.z, fmaf(q2, t.y, v10 * t.x));
+  b.b11 = fmaf(v00, t.z, fmaf(q1, t.y, v11 * t.x));
+}
+
+__device__ __forceinline__ void fwd_guard(FState &f) {
+  if (f.p1 + f.p2 > kHuge) {
+    f.l00 *= kTiny;
+    f.l01 *= kTiny;
+    f.l10 *= kTiny;
+    f.l11 *= kTiny;
+    f.p1 *= kTiny;
+    f.p2 *= kTiny;
+    f.k += 64;
+  }
+}
+__device__ __forceinline__ void bwd_guard(BState &b) {
+  if ((b.b00 + b.b11) + (b.b01 + b.b10) > kHuge) {
+    b.b00 *= kTiny;
+    b.b01 *= kTiny;
+    b.b10 *= kTiny;
+    b.b11 *= kTiny;
+    b.k += 64;
+  }
+}
+
+struct Parents {
+  uint64_t f0, f1, m0, m1;
+};
+
+__device__ __forceinline__ Parents load_parents(const uint64_t *haps, uint32_t wn, uint4 q,
+                                                uint32_t w) {
+  Parents r;
+  r.f0 = __ldg(haps + (size_t)q.x * wn + w);
+  r.f1 = __ldg(haps + (size_t)q.y * wn + w);
+  r.m0 = __ldg(haps + (size_t)q.z * wn + w);
+  r.m1 = __ldg(haps + (size_t)q.w * wn + w);
+  return r;
+}
+
+template <class E>
+__device__ __forceinline__ void fwd_site(FState &f, const E &em, const float4 *tran4,
+                                         const Parents &pw, uint32_t m, uint32_t j) {
+  float s00, s01, s10, s11;
+  select4(em.get(m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
+          (pw.m1 >> j) & 1, s00, s01, s10, s11);
+  fwd_step(f, __ldg(tran4 + m), s00, s01, s10, s11);
+}
+
+template <class E>
+__device__ __forceinline__ void bwd_site(BState &b, const E &em, const float4 *tran4,
+                                         const Parents &pw, uint32_t m, uint32_t j) {
+  float s00, s01, s10, s11;
+  select4(em.get(m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
+          (pw.m1 >> j) & 1, s00, s01, s10, s11);
+  bwd_step(b, __ldg(tran4 + m), s00, s01, s10, s11);
+}
+
+// Log-likelihood of one quadruple (natural log), binary64.
+template <class E>
+__device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, uint4 q) {
+  const uint32_t S = p.S, wn = p.wn;
+  const float4 *tran4 = p.tran4;
+  FState f;
+  f.l00 = f.l01 = f.l10 = f.l11 = 0.25f;
+  f.p1 = f.p2 = 0.5f;
+  f.k = 0;
+  BState b;
+  b.b00 = b.b01 = b.b10 = b.b11 = 1.0f;
+  b.k = 0;
+  E ef = em0, eb = em0;
+  if (wn == 1) {
+    ef.prep(p, 0);
+    const Parents pw = load_parents(p.haps, wn, q, 0);
+#pragma unroll 1
+    for (uint32_t m = 0; m < S; ++m)
+      fwd_site(f, ef, tran4, pw, m, m);
+  } else {
+    const uint32_t wf = (wn + 1) >> 1;
+    uint32_t wb = wn - 1;
+    if (S & 63u) {
+      eb.prep(p, wb);
+      const Parents pw = load_parents(p.haps, wn, q, wb);
+#pragma unroll 1
+      for (int m = (int)S - 1; m >= (int)(wb * 64); --m)
+        bwd_site(b, eb, tran4, pw, (uint32_t)m, (uint32_t)m & 63u);
+      bwd_guard(b);
+      --wb;
+    }
+    const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
+#pragma unroll 1
+    for (uint32_t i = 0; i < nb; ++i) {
+      const uint32_t wfw = i, wbw = wb - i;
+      ef.prep(p, wfw);
+      eb.prep(p, wbw);
+      const Parents pf = load_parents(p.haps, wn, q, wfw);
+      const Parents pb = load_parents(p.haps, wn, q, wbw);
+      const uint32_t mf = wfw * 64, mb = wbw * 64 + 63;
+#pragma unroll
+      for (uint32_t j = 0; j < 64; ++j) {
+        fwd_site(f, ef, tran4, pf, mf + j, j);
+        bwd_site(b, eb, tran4, pb, mb - j, 63 - j);
+      }
+      fwd_guard(f);
+      bwd_guard(b);
+    }
+#pragma unroll 1
+    for (uint32_t i = nb; i < wf; ++i) {
+      ef.prep(p, i);
+      const Parents pf = load_parents(p.haps, wn, q, i);
+      const uint32_t mf = i * 64;
+#pragma unroll
+      for (uint32_t j = 0; j < 64; ++j)
+        fwd_site(f, ef, tran4, pf, mf + j, j);
+      fwd_guard(f);
+    }
+  }
+  const double dot = (double)f.l00 * (double)b.b00 + (double)f.l01 * (double)b.b01 +
+                     (double)f.l10 * (double)b.b10 + (double)f.l11 * (double)b.b11;
+  return log(dot) + (double)(f.k + b.k) * 0.69314718055994530942;
+}
+
+// ---------------------------------------------------------------------------
+// hmm_work, one sample per lane, binary32 in the reference's operation order
+// (impute.cpp:380-485): explicit _rn intrinsics keep nvcc from contracting
+// products and sums into FMAs, so results are bit-identical to the CPU code.
+
+__device__ __forceinline__ float pick(const float4 e, uint32_t i) {
+  return (i & 2u) ? ((i & 1u) ? e.w : e.z) : ((i & 1u) ? e.y : e.x);
+}
+
+__device__ __forceinline__ uint32_t hbit(const uint64_t *h, uint32_t m) {
+  return (uint32_t)((__ldg(h + (m >> 6)) >> (m & 63u)) & 1u);
+}
+
+__device__ __forceinline__ float fma3_rn(float a0, float b0, float a1, float b1, float a2,
+                                         float b2, float a3, float b3) {
+  // ((a0*b0 + a1*b1) + a2*b2) + a3*b3, every product and sum rounded.
+  return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)),
+                             __fmul_rn(a2, b2)),
+                   __fmul_rn(a3, b3));
+}
+
+__device__ void hmm_work_lane(const GenParams &p, const float *pc, uint32_t s, uint4 q) {
+  const uint32_t S = p.S, wn = p.wn;
+  const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
+                 *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
+  const float4 *e = p.emit + (size_t)s * S;
+  float4 *beta = p.beta + (size_t)s * S;
+  // backward recursion (impute.cpp:389-414)
+  float b0 = 1.f, b1 = 1.f, b2 = 1.f, b3 = 1.f;
+  beta[S - 1] = make_float4(1.f, 1.f, 1.f, 1.f);
+  for (uint32_t m = S - 1; m; --m) {
+    const float4 em = __ldg(e + m);
+    const float4 t = __ldg(p.tran4 + m);
+    const uint32_t a0 = hbit(f0, m), a1 = hbit(f1, m), c0 = hbit(m0, m), c1 = hbit(m1, m);
+    const float b00 = __fmul_rn(b0, pick(em, (a0 << 1) | c0));
+    const float b01 = __fmul_rn(b1, pick(em, (a0 << 1) | c1));
+    const float b10 = __fmul_rn(b2, pick(em, (a1 << 1) | c0));
+    const float b11 = __fmul_rn(b3, pick(em, (a1 << 1) | c1));
+    b0 = __fadd_rn(__fadd_rn(__fmul_rn(b00, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                   __fmul_rn(b11, t.z));
+    b1 = __fadd_rn(__fadd_rn(__fmul_rn(b01, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                   __fmul_rn(b10, t.z));
+    b2 = __fadd_rn(__fadd_rn(__fmul_rn(b10, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                   __fmul_rn(b01, t.z));
+    b3 = __fadd_rn(__fadd_rn(__fmul_rn(b11, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                   __fmul_rn(b00, t.z));
+    const float sum = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(__fadd_rn(b0, b1), b2), b3));
+    b0 = __fmul_rn(b0, sum);
+    b1 = __fmul_rn(b1, sum);
+    b2 = __fmul_rn(b2, sum);
+    b3 = __fmul_rn(b3, sum);
+    beta[m - 1] = make_float4(b0, b1, b2, b3);
+  }
+  // forward sampling (impute.cpp:416-484)
+  const float *pr = p.prob + (size_t)s * S * 3;
+  uint64_t *ha = p.hnew + (size_t)2 * s * wn, *hb = ha + wn;
+  uint64_t wa = 0, wb = 0;
+  float l00 = 0, l01 = 0, l10 = 0, l11 = 0;
+  const bool use_pow = p.pen != 1.0f;
+  glp_u32x4 ux;
+  for (uint32_t m = 0; m < S; ++m) {
+    const float4 em = __ldg(e + m);
+    const float4 t = __ldg(p.tran4 + m);
+    const uint32_t a0 = hbit(f0, m), a1 = hbit(f1, m), c0 = hbit(m0, m), c1 = hbit(m1, m);
+    const uint32_t s00 = (a0 << 1) | c0, s01 = (a0 << 1) | c1, s10 = (a1 << 1) | c0,
+                   s11 = (a1 << 1) | c1;
+    if (m) {
+      const float b00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
+      const float b01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
+      const float b10 = fma3_rn(l00, t.y, l01, t.z, l10, t.x, l11, t.y);
+      const float b11 = fma3_rn(l00, t.z, l01, t.y, l10, t.y, l11, t.x);
+      l00 = __fmul_rn(b00, pick(em, s00));
+      l01 = __fmul_rn(b01, pick(em, s01));
+      l10 = __fmul_rn(b10, pick(em, s10));
+      l11 = __fmul_rn(b11, pick(em, s11));
+    } else {
+      l00 = __fmul_rn(0.25f, pick(em, s00));
+      l01 = __fmul_rn(0.25f, pick(em, s01));
+      l10 = __fmul_rn(0.25f, pick(em, s10));
+      l11 = __fmul_rn(0.25f, pick(em, s11));
+    }
+    const float sum = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(__fadd_rn(l00, l01), l10), l11));
+    l00 = __fmul_rn(l00, sum);
+    l01 = __fmul_rn(l01, sum);
+    l10 = __fmul_rn(l10, sum);
+    l11 = __fmul_rn(l11, sum);
+    const float4 bb = beta[m];
+    const float p00 = __fmul_rn(l00, bb.x), p01 = __fmul_rn(l01, bb.y),
+                p10 = __fmul_rn(l10, bb.z), p11 = __fmul_rn(l11, bb.w);
+    const float g0 = __ldg(pr + 3 * m), g1 = __ldg(pr + 3 * m + 1),
+                g2 = __ldg(pr + 3 * m + 2);
+    float c[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float inner = fma3_rn(p00, pc[s00 * 4 + k], p01, pc[s01 * 4 + k], p10,
+                                  pc[s10 * 4 + k], p11, pc[s11 * 4 + k]);
+      const float g = k == 0 ? g0 : (k == 3 ? g2 : g1);
+      const float x = __fmul_rn(g, inner);
+      c[k] = use_pow ? powf(x, p.pen) : x;
+    }
+    float u;
+    if (p.tr_work) {
+      u = __ldg(p.tr_work + (size_t)s * S + m);
+    } else {
+      if ((m & 3u) == 0 || m == 0)
+        ux = glp_draw(p.seed, p.generation, s, m >> 2, GLP_TAG_WORK);
+      u = glp_u24(ux.v[m & 3u]);
+    }
+    const float c01 = __fadd_rn(c[0], c[1]);
+    const float c012 = __fadd_rn(c01, c[2]);
+    const float r = __fmul_rn(u, __fadd_rn(c012, c[3]));
+    uint32_t bit_a, bit_b;
+    if (r < c[0]) {
+      bit_a = 0;
+      bit_b = 0;
+    } else if (r < c01) {
+      bit_a = 0;
+      bit_b = 1;
+    } else if (r < c012) {
+      bit_a = 1;
+      bit_b = 0;
+    } else {
+      bit_a = 1;
+      bit_b = 1;
+    }
+    wa |= (uint64_t)bit_a << (m & 63u);
+    wb |= (uint64_t)bit_b << (m & 63u);
+    if ((m & 63u) == 63u || m == S - 1) {
+      ha[m >> 6] = wa;
+      hb[m >> 6] = wb;
+      wa = 0;
+      wb = 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The generation kernel.
+
+struct Pending {
+  uint32_t s, q0, q1, q2, q3;
+};
+
+__device__ __forceinline__ uint32_t get_slot(const uint4 &q, uint32_t r) {
+  return r == 0 ? q.x : (r == 1 ? q.y : (r == 2 ? q.z : q.w));
+}
+__device__ __forceinline__ void set_slot(uint4 &q, uint32_t r, uint32_t v) {
+  if (r == 0)
+    q.x = v;
+  else if (r == 1)
+    q.y = v;
+  else if (r == 2)
+    q.z = v;
+  else
+    q.w = v;
+}
+
+template <int P, class E>
+__global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p) {
+  static_assert(P == 1 || P == 2 || P == 4 || P == 8 || P == 16 || P == 32, "P");
+  constexpr unsigned FULL = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t li = lane % P, gbase = lane - li;
+  __shared__ float4 s_vq[16];
+  __shared__ float s_pc[16];
+  __shared__ Pending s_pend[kWarps][64];
+  __shared__ uint32_t s_npend[kWarps];
+  if (threadIdx.x < 16) {
+    s_pc[threadIdx.x] = p.pc[threadIdx.x];
+    if (p.vq_table)
+      s_vq[threadIdx.x] = p.vq_table[threadIdx.x];
+  }
+  if (lane == 0)
+    s_npend[warp] = 0;
+  __syncthreads();
+
+  const uint32_t N = p.N, C = p.C, H = p.H;
+  uint32_t s = kNone, e = 0;
+  uint4 q = make_uint4(0, 0, 0, 0);
+  double curr = 0.0;
+  bool exhausted = false;
+  unsigned long long n_evals = 0, n_rounds = 0, n_acc = 0;
+
+  while (true) {
+    // idle groups take the next sample from the generation's queue
+    const bool need = (s == kNone) && !exhausted;
+    uint32_t ns = 0;
+    if (need && li == 0)
+      ns = atomicAdd(p.counter, 1u);
+    ns = __shfl_sync(FULL, ns, gbase);
+    if (need) {
+      if (ns < N) {
+        s = ns;
+        e = 0;
+        q = make_uint4(__ldg(p.quad_in + s), __ldg(p.quad_in + N + s),
+                       __ldg(p.quad_in + 2 * (size_t)N + s),
+                       __ldg(p.quad_in + 3 * (size_t)N + s));
+        if (q.x >= H || q.y >= H || q.z >= H || q.w >= H) {
+          atomicOr(p.error, 1);
+          q = make_uint4(0, 0, 0, 0);
+        }
+      } else {
+        exhausted = true;
+      }
+    }
+    const bool active = s != kNone;
+    if (!__any_sync(FULL, active))
+      break;
+
+    // one speculative round: lane li scores evaluation e + li
+    const uint32_t k = active ? min((uint32_t)P, C + 1 - e) : 0u;
+    const uint32_t ev = e + li;
+    const bool on = li < k;
+    uint32_t slot = 0, phap = 0;
+    double u = 0.0;
+    uint4 myq = q;
+    if (on && ev > 0) {
+      const uint32_t cyc = ev - 1;
+      if (p.tr_slot) {
+        slot = p.tr_slot[(size_t)s * C + cyc] & 3u;
+        u = p.tr_u[(size_t)s * C + cyc];
+      } else {
+        glp_mh_draw(p.seed, p.generation, s, cyc, &slot, &u);
+      }
+      phap = __ldg(p.props + (size_t)cyc * N + s);
+      if (phap >= H) {
+        atomicOr(p.error, 1);
+        phap = 0;
+      }
+      set_slot(myq, slot, phap);
+    }
+    double L = 0.0;
+    if (on) {
+      E em;
+      em.init(p, s, s_vq);
+      L = eval_like<E>(p, em, myq);
+    }
+    // replay the accept rule in chain order (MHSampler.hpp:86-93)
+    uint32_t first_acc = P;
+#pragma unroll 1
+    for (uint32_t j = 0; j < (uint32_t)P; ++j) {
+      const double Lj = __shfl_sync(FULL, L, gbase + j);
+      const double uj = __shfl_sync(FULL, u, gbase + j);
+      const uint32_t slj = __shfl_sync(FULL, slot, gbase + j);
+      const uint32_t phj = __shfl_sync(FULL, phap, gbase + j);
+      if (active && first_acc == P && j < k) {
+        if (e + j == 0) {
+          curr = Lj;
+        } else if (Lj >= curr || uj < exp((Lj - curr) * (double)p.pen)) {
+          set_slot(q, slj, phj);
+          curr = Lj;
+          first_acc = j;
+        }
+      }
+    }
+    if (on) {
+      const bool valid = li <= first_acc;
+      if (valid && p.eval_trace)
+        p.eval_trace[(size_t)s * (C + 1) + ev] = L;
+      if (valid && ev > 0 && p.accept_trace)
+        p.accept_trace[(size_t)s * C + ev - 1] = (uint8_t)(li == first_acc);
+    }
+    if (active) {
+      e = (first_acc < (uint32_t)P) ? e + first_acc + 1 : e + k;
+      if (li == 0) {
+        n_evals += k;
+        ++n_rounds;
+        n_acc += first_acc < (uint32_t)P ? 1u : 0u;
+      }
+    }
+
+    // finished chains: publish, queue for hmm_work
+    const bool done = active && e > C;
+    if (done && li == 0) {
+      p.quad_out[s] = q.x;
+      p.quad_out[N + s] = q.y;
+      p.quad_out[2 * (size_t)N + s] = q.z;
+      p.quad_out[3 * (size_t)N + s] = q.w;
+      if (p.like_out)
+        p.like_out[s] = curr;
+    }
+    const unsigned dmask = __ballot_sync(FULL, done && li == 0);
+    if (dmask && !p.do_work) {
+      if (done)
+        s = kNone;
+    } else if (dmask) {
+      // at most 31 entries wait between batches and at most 32 groups finish
+      // per round, so the 64-entry list never overflows
+      const uint32_t base = s_npend[warp];
+      if (done && li == 0) {
+        const uint32_t pos = base + __popc(dmask & ((1u << lane) - 1u));
+        s_pend[warp][pos] = Pending{s, q.x, q.y, q.z, q.w};
+      }
+      __syncwarp();
+      uint32_t n = base + __popc(dmask);
+      if (done)
+        s = kNone;
+      if (p.do_work && n >= 32) {
+        const Pending pe = s_pend[warp][lane];
+        hmm_work_lane(p, s_pc, pe.s, make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
+        __syncwarp();
+        if (lane < n - 32)
+          s_pend[warp][lane] = s_pend[warp][lane + 32];
+        n -= 32;
+      }
+      __syncwarp();
+      if (lane == 0)
+        s_npend[warp] = n;
+      __syncwarp();
+    }
+  }
+  if (p.do_work) {
+    const uint32_t n = s_npend[warp];
+    if (lane < n) {
+      const Pending pe = s_pend[warp][lane];
+      hmm_work_lane(p, s_pc, pe.s, make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
+    }
+  }
+  if (p.stats && li == 0 && n_rounds) {
+    atomicAdd(p.stats, n_evals);
+    atomicAdd(p.stats + 1, n_rounds);
+    atomicAdd(p.stats + 2, n_acc);
+  }
+}
+
+}  // namespace glp

@@ -1,0 +1,99 @@
+"""ctypes binding of the C ABI in include/glphase_gpu.h.
+
+Loading fails loudly (``NativeLibraryMissing``) when the in-tree CUDA library
+has not been built: there is no CPU fallback on the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+GLP_OK = 0
+GLP_ERR_ARG = 1
+GLP_ERR_CUDA = 2
+GLP_ERR_NOMEM = 3
+GLP_ERR_STATE = 4
+GLP_ERR_INDEX = 5
+GLP_ERR_DEVICE = 6
+
+GLP_GEN_VQ = 1
+GLP_GEN_NO_WORK = 2
+
+EXPORTED = [
+    "glp_check_device", "glp_create", "glp_destroy", "glp_last_error", "glp_set_stream",
+    "glp_set_tran", "glp_set_mutation_mat", "glp_set_codebook", "glp_set_packed_gls",
+    "glp_set_emission", "glp_run_hmm_on_device", "glp_run_generation",
+    "glp_run_generation_host", "glp_finish", "glp_set_lanes_per_sample", "glp_get_stats",
+    "glp_measure_fp32_peak",
+]
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+class GlpError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"glphase_gpu error {code}: {msg}")
+        self.code = code
+
+
+class GenerationArgs(C.Structure):
+    _fields_ = [
+        ("num_samples", C.c_uint32), ("num_sites", C.c_uint32), ("num_cycles", C.c_uint32),
+        ("num_haps", C.c_uint32),
+        ("haps", C.c_void_p), ("hnew", C.c_void_p),
+        ("hap_idxs_in", C.c_void_p), ("hap_idxs_out", C.c_void_p), ("props", C.c_void_p),
+        ("pen", C.c_float), ("seed", C.c_uint64), ("generation", C.c_uint32),
+        ("flags", C.c_uint32),
+        ("trace_slot", C.c_void_p), ("trace_accept", C.c_void_p), ("trace_work", C.c_void_p),
+        ("like_out", C.c_void_p), ("eval_trace", C.c_void_p), ("accept_trace", C.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the CUDA library (optionally compiling it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise NativeLibraryMissing(
+                f"{_build.LIB} is not built; run glphase_gb300/build.py (nvcc, sm_103a)")
+    L = C.CDLL(_build.LIB)
+    vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+    L.glp_check_device.argtypes = [i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32),
+                                   C.POINTER(i32)]
+    L.glp_create.argtypes = [i32, C.POINTER(vp)]
+    L.glp_destroy.argtypes = [vp]
+    L.glp_destroy.restype = None
+    L.glp_last_error.argtypes = [vp]
+    L.glp_last_error.restype = C.c_char_p
+    L.glp_set_stream.argtypes = [vp, vp]
+    L.glp_set_tran.argtypes = [vp, vp, u32]
+    L.glp_set_mutation_mat.argtypes = [vp, vp]
+    L.glp_set_codebook.argtypes = [vp, vp, u32]
+    L.glp_set_packed_gls.argtypes = [vp, vp, C.c_size_t]
+    L.glp_set_emission.argtypes = [vp, vp, vp, u32, u32]
+    L.glp_run_hmm_on_device.argtypes = [vp, vp, C.c_size_t, vp, u32, u32, u32, vp, u64]
+    L.glp_run_generation.argtypes = [vp, C.POINTER(GenerationArgs)]
+    L.glp_run_generation_host.argtypes = [vp, C.POINTER(GenerationArgs)]
+    L.glp_finish.argtypes = [vp]
+    L.glp_set_lanes_per_sample.argtypes = [vp, u32]
+    L.glp_get_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u32)]
+    L.glp_measure_fp32_peak.argtypes = [vp, C.c_float, C.POINTER(C.c_double)]
+    for name in EXPORTED:
+        getattr(L, name)
+    _lib = L
+    return L

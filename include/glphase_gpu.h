@@ -1,0 +1,169 @@
+/*
+ * glphase_gpu.h -- C ABI of the GB300 (sm_103a) implementation of GLPhase's
+ * per-sample MH/HMM hot path.  Plain pointers and sizes only; every entry
+ * point returns a glp_status code and never exits or throws.
+ *
+ * The entry points replace the reference's device API, namespace HMMLikeCUDA
+ * in src/hmmLike.h:23-38 (implemented in src/hmmLike.cu).  Each declaration
+ * names the reference function it stands in for.  A header-only C++ shim with
+ * the reference's exact signatures lives in include/hmmlike_cuda_shim.hpp,
+ * so src/hmmLike.cpp and Insti::cudaSolve compile against this library
+ * unchanged.
+ *
+ * Array layouts (row-major):
+ *   haps          uint64 [H][wn], wn = ceil(S/64); site m -> word m>>6,
+ *                 bit m&63; haplotypes 2i and 2i+1 belong to sample i,
+ *                 panel haplotypes follow at 2N.. (src/impute.hpp:53-66,
+ *                 src/insti.cpp:1395-1403)
+ *   hap_idxs      uint32 [4][N] (father0, father1, mother0, mother1)
+ *                 (src/hmmLike.cpp:81)
+ *   props         uint32 [C][N] proposal haplotypes (src/hmmLike.cpp:86)
+ *   tran          float  [S][3] (row 0 unused) (src/insti.cpp:1277-1300)
+ *   pc            float  [4][4] row-major mutation matrix pc[i][j]
+ *   emit          float  [N][S][4], prob float [N][S][3] (homRef, het,
+ *                 homAlt) (src/insti.cpp:1345-1382)
+ *   packed GLs    uint32 [ceil(S/8)][N], eight 4-bit codes per word, most
+ *                 significant nibble first (src/glPack.cpp:112-165)
+ *   codebook      float  [16][2] (homRef, het) (src/hmmLike.cu:369-383)
+ */
+#ifndef GLPHASE_GPU_H
+#define GLPHASE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum glp_status {
+  GLP_OK = 0,
+  GLP_ERR_ARG = 1,      /* invalid argument or size mismatch */
+  GLP_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+  GLP_ERR_NOMEM = 3,    /* device allocation failed */
+  GLP_ERR_STATE = 4,    /* a required model input was not set */
+  GLP_ERR_INDEX = 5,    /* a haplotype index >= num_haps reached the device */
+  GLP_ERR_DEVICE = 6    /* no usable device */
+} glp_status;
+
+typedef struct glp_ctx glp_ctx;
+
+/* Emission source of the MH likelihood. */
+#define GLP_EMIT_FLOAT 0u /* float emit [N][S][4]: Impute::hmm_like semantics */
+#define GLP_EMIT_VQ 1u    /* 4-bit VQ GL codes: HMMLikeCUDA::hmmLike semantics */
+
+/* glp_generation_args.flags */
+#define GLP_GEN_VQ 1u      /* score with the VQ codes (else float emit) */
+#define GLP_GEN_NO_WORK 2u /* skip the fused hmm_work (hnew untouched) */
+
+/* One MH generation over all N samples. */
+typedef struct glp_generation_args {
+  uint32_t num_samples; /* N */
+  uint32_t num_sites;   /* S: must equal the S of the model inputs */
+  uint32_t num_cycles;  /* C */
+  uint32_t num_haps;    /* H: rows of haps/hnew, all indices must be < H */
+  const uint64_t *haps; /* [H][wn] current haplotypes (read only) */
+  uint64_t *hnew;       /* [H][wn] rows 2i,2i+1 receive the new haplotypes */
+  const uint32_t *hap_idxs_in; /* [4][N] initial quadruples */
+  uint32_t *hap_idxs_out;      /* [4][N] final quadruples (may alias in) */
+  const uint32_t *props;       /* [C][N] proposals */
+  float pen;                   /* MH and hmm_work penalty (src/insti.cpp:1670) */
+  uint64_t seed;               /* key of the counter-based random streams */
+  uint32_t generation;         /* counter of the random streams */
+  uint32_t flags;              /* GLP_GEN_* */
+  /* optional replay trace (all three or none): */
+  const uint8_t *trace_slot;   /* [N][C] replaced slot (0..3) */
+  const double *trace_accept;  /* [N][C] accept uniforms */
+  const float *trace_work;     /* [N][S] hmm_work uniforms */
+  /* optional outputs: */
+  double *like_out;            /* [N] final log-likelihood of each chain */
+  double *eval_trace;          /* [N][C+1] every evaluated log-likelihood */
+  uint8_t *accept_trace;       /* [N][C] accept decisions */
+} glp_generation_args;
+
+/* Number of visible CUDA devices and whether device `device` is an sm_103
+ * part.  Replaces HMMLikeCUDA::CheckDevice (src/hmmLike.cu:266-320). */
+int glp_check_device(int device, int *device_count, int *cc_major, int *cc_minor,
+                     int *sm_count);
+
+/* Create a context on `device`.  Replaces HMMLikeCUDA::SetDevice and
+ * InitializeConstants (src/hmmLike.cu:228-264). */
+int glp_create(int device, glp_ctx **out);
+
+/* Free every device buffer of the context; the device itself is not reset.
+ * Replaces HMMLikeCUDA::Cleanup (src/hmmLike.cu:385-397). */
+void glp_destroy(glp_ctx *ctx);
+
+/* Message of the last failed call on this context (never NULL). */
+const char *glp_last_error(const glp_ctx *ctx);
+
+/* Bind the context to a CUDA stream (cudaStream_t; NULL = the context's own
+ * stream).  Device-pointer calls are asynchronous on that stream. */
+int glp_set_stream(glp_ctx *ctx, void *stream);
+
+/* Transition matrix tran [S][3].  Replaces HMMLikeCUDA::CopyTranToDevice
+ * (src/hmmLike.cu:322-337); S is no longer capped at NUMSITES=1024. */
+int glp_set_tran(glp_ctx *ctx, const float *tran, uint32_t num_sites);
+
+/* Mutation matrix pc[4][4], row-major.  Replaces
+ * HMMLikeCUDA::CopyMutationMatToDevice (src/hmmLike.cu:339-355). */
+int glp_set_mutation_mat(glp_ctx *ctx, const float *pc16);
+
+/* VQ codebook [entries][2], entries = 16.  Replaces
+ * HMMLikeCUDA::CopyCodeBookToDevice (src/hmmLike.cu:368-383). */
+int glp_set_codebook(glp_ctx *ctx, const float *codebook, uint32_t entries);
+
+/* Packed VQ GLs [ceil(S/8)][N].  Replaces HMMLikeCUDA::CopyPackedGLsToDevice
+ * (src/hmmLike.cu:357-366). */
+int glp_set_packed_gls(glp_ctx *ctx, const uint32_t *packed, size_t num_words);
+
+/* Float emission [N][S][4] and genotype probabilities [N][S][3] from the
+ * host (Insti::initialize's emit and prob, src/insti.cpp:1345-1382): the
+ * inputs of Impute::hmm_like and of the fused hmm_work.  prob may be NULL
+ * when hmm_work is never run. */
+int glp_set_emission(glp_ctx *ctx, const float *emit, const float *prob, uint32_t num_samples,
+                     uint32_t num_sites);
+
+/* The reference's device call, host buffers in and out: MH over numCycles
+ * proposals per sample with VQ-decoded emissions and accept penalty 1,
+ * no hmm_work; hap_idxs [4][N] in/out.  Replaces HMMLikeCUDA::RunHMMOnDevice
+ * (src/hmmLike.cu:399-572).  The panel may hold fewer rows than the context
+ * was sized for; all indices are checked against panel_words / wn. */
+int glp_run_hmm_on_device(glp_ctx *ctx, const uint64_t *hap_panel, size_t panel_words,
+                          const uint32_t *extra_prop_haps, uint32_t num_sites,
+                          uint32_t num_samples, uint32_t num_cycles, uint32_t *hap_idxs,
+                          uint64_t seed);
+
+/* One generation with the fused hmm_work, all array pointers DEVICE
+ * pointers, asynchronous on the context stream.  Call glp_finish() to wait
+ * and collect device-side errors.  Replaces RunHMMOnDevice plus the OpenMP
+ * hmm_work loop of Insti::cudaSolve (src/insti.cpp:1433-1463). */
+int glp_run_generation(glp_ctx *ctx, const glp_generation_args *args);
+
+/* The same generation with HOST pointers: copies inputs in, runs, copies
+ * quadruples, hnew rows of the N samples and the optional outputs back,
+ * synchronously. */
+int glp_run_generation_host(glp_ctx *ctx, const glp_generation_args *args);
+
+/* Wait for the context stream and report device-side errors. */
+int glp_finish(glp_ctx *ctx);
+
+/* Lanes that score one sample's chain speculatively: 1, 2, 4, 8, 16 or 32
+ * (0 = choose from the last generation's acceptance rate). */
+int glp_set_lanes_per_sample(glp_ctx *ctx, uint32_t lanes);
+
+/* Evaluations (scored quadruples, speculative ones included) and speculative
+ * rounds of the most recent generation (after glp_finish). */
+int glp_get_stats(glp_ctx *ctx, uint64_t *evaluations, uint64_t *rounds,
+                  uint32_t *lanes_used);
+
+/* Calibration (no reference counterpart): runs a dependent-free FMA stream on
+ * every SM for about `ms_target` milliseconds and reports the achieved FP32
+ * rate in TFLOP/s (2 flops per FMA): the roofline denominator of the
+ * FP32-bound likelihood recursion. */
+int glp_measure_fp32_peak(glp_ctx *ctx, float ms_target, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GLPHASE_GPU_H */

@@ -1,0 +1,215 @@
+"""The CPU oracle pinned against the reference: golden vectors produced by the
+reference's own impute.cpp (tests/golden/make_golden.py), a live comparison
+with oracle/_ref where that build exists, and the known-answer tests of the
+reference's unit tests (src/testing/*.cpp)."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from glphase_gb300 import model as mdl, synth
+
+
+def _row(a):
+    return np.ascontiguousarray(a)
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 against the published Random123 known-answer vectors."""
+    import subprocess, tempfile, os
+    from conftest import ROOT
+    src = r'''
+#include <stdio.h>
+#include "glp_rng.h"
+int main(){
+  glp_u32x4 c={{0,0,0,0}}; glp_u32x4 o=glp_philox4x32_10(c,0,0);
+  printf("%08x%08x%08x%08x\n",o.v[0],o.v[1],o.v[2],o.v[3]);
+  glp_u32x4 d={{0xffffffffu,0xffffffffu,0xffffffffu,0xffffffffu}};
+  o=glp_philox4x32_10(d,0xffffffffu,0xffffffffu);
+  printf("%08x%08x%08x%08x\n",o.v[0],o.v[1],o.v[2],o.v[3]);
+  glp_u32x4 e={{0x243f6a88u,0x85a308d3u,0x13198a2eu,0x03707344u}};
+  o=glp_philox4x32_10(e,0xa4093822u,0x299f31d0u);
+  printf("%08x%08x%08x%08x\n",o.v[0],o.v[1],o.v[2],o.v[3]);
+  return 0;}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        cfile, exe = os.path.join(d, "k.c"), os.path.join(d, "k")
+        open(cfile, "w").write(src)
+        subprocess.run(["gcc", "-O2", "-I", os.path.join(ROOT, "glphase_gb300", "csrc"), cfile,
+                        "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert out == ["6627e8d5e169c58dbc57ac4c9b00dbd8", "408f276d41c83b0ea20bc7c66d5451fd",
+                   "d16cfe0994fdcceb5001e42024126ea1"]
+
+
+def test_hmm_like_matches_reference_golden(oracle_lib, golden):
+    O, g = oracle_lib, golden
+    for i in range(len(g["like_ref"])):
+        s = int(g["like_sample"][i])
+        v = O.hmm_like_f32(_row(g["emit"][s]), g["tran"], g["haps"], _row(g["like_quad"][i]))
+        assert np.float32(v) == g["like_ref"][i], i
+
+
+def test_hmm_like_f64_yardstick(oracle_lib, golden):
+    O, g = oracle_lib, golden
+    for i in range(16):
+        s = int(g["like_sample"][i])
+        v32 = O.hmm_like_f32(_row(g["emit"][s]), g["tran"], g["haps"], _row(g["like_quad"][i]))
+        v64 = O.hmm_like_f64(_row(g["emit"][s]), g["tran"], g["haps"], _row(g["like_quad"][i]))
+        assert abs(v32 - v64) <= 1e-5 * abs(v64)
+        assert v64 <= 0
+
+
+def test_hmm_work_matches_reference_golden(oracle_lib, golden):
+    O, g = oracle_lib, golden
+    for k, pen in enumerate(g["pens"]):
+        for i in range(len(g["work_sample"])):
+            s = int(g["work_sample"][i])
+            ha, hb = O.hmm_work(_row(g["emit"][s]), _row(g["t"][s]), g["tran"], g["pc"],
+                                g["haps"], _row(g["work_quad"][i]), float(pen),
+                                _row(g["work_u"][i]))
+            assert np.array_equal(ha, g["work_ha"][k, i]), (k, i)
+            assert np.array_equal(hb, g["work_hb"][k, i]), (k, i)
+
+
+def test_model_constants_match_reference_initialize(golden):
+    """mu, pc, tran, t and emit against Impute::initialize (impute.cpp:182-322)."""
+    g = golden
+    gl = g["init_gl"]                    # [S][N][2] (het, homAlt), site-major
+    Si, Ni = gl.shape[0], gl.shape[1]
+    m = mdl.Model(np.ascontiguousarray(gl.transpose(1, 0, 2)), positions=g["init_pos"])
+    assert np.array_equal(m.pc.reshape(16), g["init_pc"])
+    assert np.array_equal(m.t.reshape(-1), g["init_t"])
+    assert np.array_equal(m.emit.reshape(-1), g["init_emit"])
+    # Impute keeps the per-interval distance in binary64 where Insti keeps it
+    # in binary32 (impute.cpp:275-277 vs insti.cpp:1282-1283)
+    np.testing.assert_allclose(m.tran.reshape(-1)[3:], g["init_tran"][3:], rtol=1e-6)
+
+
+def test_replace_matches_reference_golden(oracle_lib, golden):
+    O, g = oracle_lib, golden
+    hs = g["replace_haps"]
+    hsum = np.zeros(2 * 3 * 100, np.uint32)
+    for gen in range(hs.shape[0]):
+        for s in range(3):
+            O.lib().glpo_replace(np.ascontiguousarray(hs[gen].reshape(-1)), 2, 100, s, hsum)
+    assert np.array_equal(hsum, g["replace_hsum"])
+
+
+@pytest.mark.skipif("not __import__('oracle').ref_available()")
+def test_oracle_matches_live_reference_build(oracle_lib):
+    """Random inputs straight through the reference's compiled impute.cpp."""
+    O = oracle_lib
+    R = O.ref()
+    rng = np.random.default_rng(17)
+    for S in (1, 2, 63, 64, 65, 300):
+        H, wn = 12, (S + 63) // 64
+        haps = rng.integers(0, 2**63, size=(H, wn), dtype=np.uint64)
+        emit = rng.random((S, 4)).astype(np.float32)
+        prob = rng.dirichlet([1, 1, 1], S).astype(np.float32)
+        tran = np.zeros((S, 3), np.float32)
+        r = rng.random(S).astype(np.float32) * 0.01
+        tran[:, 0], tran[:, 1], tran[:, 2] = (1 - r) ** 2, r * (1 - r), r * r
+        pc = rng.random(16).astype(np.float32)
+        for _ in range(8):
+            P = rng.integers(0, H, 4).astype(np.uint32)
+            a = O.hmm_like_f32(emit, tran, haps, P)
+            b = R.glpr_hmm_like(emit, tran, haps, H, wn, S, P)
+            assert np.float32(a) == np.float32(b)
+            u = rng.random(S).astype(np.float32)
+            for pen in (1.0, 0.5):
+                ha, hb = O.hmm_work(emit, prob, tran, pc, haps, P, pen, u)
+                ra = np.zeros(wn, np.uint64)
+                rb = np.zeros(wn, np.uint64)
+                R.glpr_hmm_work(emit, prob, tran, pc, haps, H, wn, S, P, pen, u, ra, rb)
+                assert np.array_equal(ha, ra) and np.array_equal(hb, rb)
+
+
+# --- known-answer tests of the reference's unit tests ------------------------
+
+def test_codebook_decode_kat(oracle_lib):
+    """src/testing/cuda_tests.cpp:66-96: codebook (i/10, 2i/100); word 1 slot 7
+    decodes code 1; word 0x01234567 slot i decodes code i."""
+    L = oracle_lib.lib()
+    cb = np.array([[i / 10, i * 2 / 100] for i in range(16)], np.float32).reshape(-1)
+    gl = np.zeros(3, np.float32)
+    L.glpo_unpack_gl_codebook(1, cb, 7, gl)
+    np.testing.assert_array_almost_equal(gl, [0.1, 0.02, 0.88], decimal=6)
+    for i in range(8):
+        L.glpo_unpack_gl_codebook(19088743, cb, i, gl)
+        np.testing.assert_allclose(gl, [i / 10, i * 2 / 100, 1 - i / 10 - i * 2 / 100],
+                                   rtol=1e-6, atol=1e-7)
+
+
+def test_fill_emit_kat(oracle_lib):
+    """src/testing/cuda_tests.cpp:98-116: all-ones mutation matrix gives
+    G0 + 2 G1 + G2 for every state."""
+    L = oracle_lib.lib()
+    rng = np.random.default_rng(1)
+    M = np.ones(16, np.float32)
+    for _ in range(10):
+        gl = rng.random(3).astype(np.float32)
+        em = np.zeros(4, np.float32)
+        L.glpo_fill_emit(gl, M, em)
+        np.testing.assert_allclose(em, gl[0] + 2 * gl[1] + gl[2], rtol=1e-6)
+
+
+def test_mutation_matrix_transpose_kat(oracle_lib):
+    """src/testing/cuda_tests.cpp:46-63: pc[i][j] = i + 4j lands at M[i + 4j]."""
+    L = oracle_lib.lib()
+    pc = np.array([[i + 4 * j for j in range(4)] for i in range(4)], np.float32).reshape(-1)
+    M = np.zeros(16, np.float32)
+    L.glpo_mutation_to_device_layout(pc, M)
+    for i in range(4):
+        for j in range(4):
+            assert M[i + 4 * j] == i + 4 * j
+
+
+def test_mh_accept_semantics(oracle_lib):
+    """src/testing/other_unittests.cpp:256-283 restated on the accept rule:
+    better or equal proposals are always accepted, much worse ones are not."""
+    L = oracle_lib.lib()
+    curr = -100.0
+    for i in range(2, 10):
+        assert L.glpo_mh_accept(curr + i * 0.01, curr, 1.0, 0.999999) == 1
+    assert L.glpo_mh_accept(curr, curr, 1.0, 0.999999) == 1
+    assert L.glpo_mh_accept(2 * curr, curr, 1.0, 1e-12) == 0
+    # u < exp(delta * pen) boundary, binary64
+    d = -0.5
+    assert L.glpo_mh_accept(curr + d, curr, 1.0, math.exp(d) * (1 - 1e-12)) == 1
+    assert L.glpo_mh_accept(curr + d, curr, 1.0, math.exp(d) * (1 + 1e-12)) == 0
+    assert L.glpo_mh_accept(curr + d, curr, 0.25, math.exp(d * 0.25) * 0.999) == 1
+
+
+def test_hap_packing_round_trip():
+    rng = np.random.default_rng(3)
+    for S in (1, 63, 64, 65, 200):
+        bits = rng.integers(0, 2, size=(5, S)).astype(np.uint8)
+        words = mdl.pack_haplotypes(bits)
+        assert words.shape == (5, (S + 63) // 64)
+        assert np.array_equal(mdl.unpack_haplotypes(words, S), bits)
+        # site m -> word m >> 6, bit m & 63 (impute.hpp:53-66)
+        for m in range(S):
+            assert ((int(words[2, m >> 6]) >> (m & 63)) & 1) == bits[2, m]
+
+
+def test_generation_reproducible_and_consistent(oracle_lib):
+    """A generation from the Philox streams equals per-sample solves."""
+    O = oracle_lib
+    w = synth.Workload("t", N=12, S=130, founders=5, depth=3, burnin=1, sampling=1, cycles=9,
+                       seed=4)
+    ds = synth.generate(w)
+    m, haps = synth.initial_state(ds)
+    rng = np.random.default_rng(0)
+    quad, props = synth.uniform_proposals(m.N, haps.shape[0], w.cycles, rng)
+    pb = O.OracleProblem(haps, m.emit, m.t, m.tran, m.pc, w.cycles)
+    tr = pb.trace(seed=5, generation=2)
+    q1, h1, l1 = O.generation(pb, tr, quad, props, 0.5, like=True, nthreads=2)
+    q2, h2, l2 = O.generation(pb, tr, quad, props, 0.5, like=True, nthreads=1)
+    assert np.array_equal(q1, q2) and np.array_equal(h1, h2) and np.array_equal(l1, l2)
+    for s in range(m.N):
+        q, curr, likes, acc, ha, hb = O.solve_sample(pb, tr, s, quad, props, 0.5, do_work=True)
+        assert np.array_equal(q, q1[:, s])
+        assert np.array_equal(ha, h1[2 * s]) and np.array_equal(hb, h1[2 * s + 1])
+        assert curr == l1[s]
