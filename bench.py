@@ -218,6 +218,7 @@ def run_ours(args):
         q, p = synth.uniform_proposals(N, H, C, rng)
         quads.append(torch.from_numpy(q.view(np.int32)).to(dev))
         propss.append(torch.from_numpy(p.view(np.int32)).to(dev))
+    torch.cuda.synchronize()
     peak = C_.c_double()
     eng.dev._c(eng.dev.L.glp_measure_fp32_peak(eng.dev.ctx, 200.0, C_.byref(peak)))
     stream = eng.stream

@@ -19,6 +19,7 @@
 
 #include "../../include/glphase_gpu.h"
 #include "glp_kernels.cuh"
+#include "glp_knn.cuh"
 
 struct glp_ctx {
   int device = 0;
@@ -48,8 +49,10 @@ struct glp_ctx {
   // staging for the host-pointer entry points
   uint64_t *d_haps = nullptr, *d_hnew = nullptr;
   size_t haps_cap = 0, hnew_cap = 0;
-  uint32_t *d_quad = nullptr, *d_quad_out = nullptr, *d_props = nullptr;
-  size_t quad_cap = 0, quad_out_cap = 0, props_cap = 0;
+  uint32_t *d_quad = nullptr, *d_quad_out = nullptr, *d_props = nullptr, *d_nbr = nullptr;
+  size_t quad_cap = 0, quad_out_cap = 0, props_cap = 0, nbr_cap = 0;
+  uint64_t *d_mask = nullptr;  // kNN common-site mask
+  size_t mask_cap = 0;
   uint8_t *d_tr_slot = nullptr, *d_acc = nullptr;
   double *d_tr_u = nullptr, *d_like = nullptr, *d_evals = nullptr;
   float *d_tr_work = nullptr;
@@ -189,8 +192,19 @@ int launch_generation(glp_ctx *c, const glp_generation_args *a) {
     return fail(c, GLP_ERR_ARG, "num_samples and num_sites must be positive");
   if (H < 2 || (uint64_t)2 * N > H)
     return fail(c, GLP_ERR_ARG, "num_haps=%u must be >= 2*num_samples=%u", H, 2 * N);
-  if (!a->haps || !a->hap_idxs_in || !a->hap_idxs_out || (C && !a->props))
-    return fail(c, GLP_ERR_ARG, "haps, hap_idxs_in/out and props are required");
+  if (!a->haps || !a->hap_idxs_out)
+    return fail(c, GLP_ERR_ARG, "haps and hap_idxs_out are required");
+  uint32_t lo = a->sample_lo, hi = a->sample_hi;
+  if (lo == 0 && hi == 0)
+    hi = H;
+  const bool draws = !a->hap_idxs_in || (C && !a->props);
+  if (draws) {
+    if (a->neighbors && a->neighbors_per_sample == 0)
+      return fail(c, GLP_ERR_ARG, "neighbors_per_sample must be positive");
+    if (!a->neighbors && (hi > H || lo >= hi || hi - lo < 3))
+      return fail(c, GLP_ERR_ARG, "surrogate range [%u, %u) must hold 3+ of %u haplotypes",
+                  lo, hi, H);
+  }
   if (work && !a->hnew)
     return fail(c, GLP_ERR_ARG, "hnew is required unless GLP_GEN_NO_WORK is set");
   if (!c->d_tran4 || c->S != S)
@@ -255,6 +269,10 @@ int launch_generation(glp_ctx *c, const glp_generation_args *a) {
   p.seed = a->seed;
   p.generation = a->generation;
   p.do_work = work ? 1u : 0u;
+  p.nbr = a->neighbors;
+  p.klen = a->neighbors_per_sample;
+  p.samp_lo = lo;
+  p.samp_hi = hi;
 
   const uint32_t P = choose_lanes(c, N);
   KernelFn fn = kernel_for(P, vq);
@@ -300,6 +318,37 @@ __global__ void __launch_bounds__(256) fp32_probe_kernel(float *out, int iters, 
 }  // namespace
 
 extern "C" {
+
+int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, uint32_t k,
+                      double lb, double ub, int use_maf, uint32_t *neighbors) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!haps || !neighbors || S == 0 || k == 0)
+    return fail(c, GLP_ERR_ARG, "haps, neighbors, num_sites and k are required");
+  const uint32_t half = (k + 1) / 2;
+  if (H < 4 || (H & 1u) || H > glp::kKnnMaxHaps)
+    return fail(c, GLP_ERR_ARG, "num_haps=%u must be even and in [4, %u]", H,
+                glp::kKnnMaxHaps);
+  if (2 * half > H - 2 || half > glp::kKnnMaxHalf)
+    return fail(c, GLP_ERR_ARG, "k=%u needs 2*ceil(k/2) <= num_haps-2 and <= %u", k,
+                2 * glp::kKnnMaxHalf);
+  if (S >= 0xffffu)
+    return fail(c, GLP_ERR_ARG, "num_sites must be below 65535 for kNN");
+  const uint32_t wn = (S + 63) / 64;
+  if ((rc = ensure(c, c->d_mask, c->mask_cap, wn)))
+    return rc;
+  glp::common_sites_kernel<<<wn, 64, 0, c->stream>>>(haps, H, wn, S, lb, ub, use_maf,
+                                                     c->d_mask);
+  GLP_CUDA(c, cudaGetLastError());
+  const size_t smem = glp::knn_smem_bytes(H);
+  GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  glp::knn_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask, half,
+                                                                 S, neighbors);
+  GLP_CUDA(c, cudaGetLastError());
+  return GLP_OK;
+}
 
 int glp_measure_fp32_peak(glp_ctx *c, float ms_target, double *tflops) {
   int rc = check_ctx(c);
@@ -417,6 +466,8 @@ void glp_destroy(glp_ctx *c) {
   release(c->d_like);
   release(c->d_evals);
   release(c->d_tr_work);
+  release(c->d_nbr);
+  release(c->d_mask);
   if (c->own_stream)
     cudaStreamDestroy(c->own_stream);
   delete c;
@@ -546,8 +597,8 @@ int glp_run_generation_host(glp_ctx *c, const glp_generation_args *a) {
   int rc = check_ctx(c);
   if (rc)
     return rc;
-  if (!a || !a->haps || !a->hap_idxs_in || !a->hap_idxs_out || (a->num_cycles && !a->props))
-    return fail(c, GLP_ERR_ARG, "haps, hap_idxs_in/out and props are required");
+  if (!a || !a->haps || !a->hap_idxs_out)
+    return fail(c, GLP_ERR_ARG, "haps and hap_idxs_out are required");
   const uint32_t N = a->num_samples, S = a->num_sites, C = a->num_cycles, H = a->num_haps;
   const bool work = (a->flags & GLP_GEN_NO_WORK) == 0;
   if (work && !a->hnew)
@@ -568,17 +619,25 @@ int glp_run_generation_host(glp_ctx *c, const glp_generation_args *a) {
   // hnew needs no upload: the kernel writes every word of rows 0..2N-1 and
   // only those rows are copied back.
   GLP_CUDA(c, cudaMemcpyAsync(c->d_haps, a->haps, hw * 8, cudaMemcpyHostToDevice, st));
-  GLP_CUDA(c, cudaMemcpyAsync(c->d_quad, a->hap_idxs_in, (size_t)16 * N,
-                              cudaMemcpyHostToDevice, st));
-  if (C)
+  if (a->hap_idxs_in)
+    GLP_CUDA(c, cudaMemcpyAsync(c->d_quad, a->hap_idxs_in, (size_t)16 * N,
+                                cudaMemcpyHostToDevice, st));
+  if (C && a->props)
     GLP_CUDA(c, cudaMemcpyAsync(c->d_props, a->props, (size_t)4 * C * N,
                                 cudaMemcpyHostToDevice, st));
   glp_generation_args d = *a;
   d.haps = c->d_haps;
   d.hnew = work ? c->d_hnew : nullptr;
-  d.hap_idxs_in = c->d_quad;
+  d.hap_idxs_in = a->hap_idxs_in ? c->d_quad : nullptr;
   d.hap_idxs_out = c->d_quad_out;
-  d.props = c->d_props;
+  d.props = a->props ? c->d_props : nullptr;
+  if (a->neighbors) {
+    const size_t nk = (size_t)N * a->neighbors_per_sample;
+    if ((rc = ensure(c, c->d_nbr, c->nbr_cap, nk)))
+      return rc;
+    GLP_CUDA(c, cudaMemcpyAsync(c->d_nbr, a->neighbors, nk * 4, cudaMemcpyHostToDevice, st));
+    d.neighbors = c->d_nbr;
+  }
   if (a->trace_slot || a->trace_accept || a->trace_work) {
     if (!(a->trace_slot && a->trace_accept && a->trace_work))
       return fail(c, GLP_ERR_ARG, "a replay trace needs slot, accept and work arrays");

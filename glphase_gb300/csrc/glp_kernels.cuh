@@ -73,6 +73,8 @@ struct GenParams {
   uint32_t *__restrict__ counter;
   unsigned long long *__restrict__ stats;
   int *__restrict__ error;
+  const uint32_t *__restrict__ nbr;  // [N][klen] surrogate table, or null
+  uint32_t klen, samp_lo, samp_hi;   // uniform surrogates over [samp_lo, samp_hi)
   float pc[16];
   float pen;
   uint64_t seed;
@@ -497,9 +499,22 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
       if (ns < N) {
         s = ns;
         e = 0;
-        q = make_uint4(__ldg(p.quad_in + s), __ldg(p.quad_in + N + s),
-                       __ldg(p.quad_in + 2 * (size_t)N + s),
-                       __ldg(p.quad_in + 3 * (size_t)N + s));
+        if (p.quad_in) {
+          q = make_uint4(__ldg(p.quad_in + s), __ldg(p.quad_in + N + s),
+                         __ldg(p.quad_in + 2 * (size_t)N + s),
+                         __ldg(p.quad_in + 3 * (size_t)N + s));
+        } else {
+          // fresh quadruple from the sampler, as RunHMMOnSamples draws one
+          // every generation (hmmLike.cpp:90-95)
+          q.x = glp_surrogate(p.seed, p.generation, s, 0, GLP_TAG_INIT, p.samp_lo, p.samp_hi,
+                              p.nbr, p.klen);
+          q.y = glp_surrogate(p.seed, p.generation, s, 1, GLP_TAG_INIT, p.samp_lo, p.samp_hi,
+                              p.nbr, p.klen);
+          q.z = glp_surrogate(p.seed, p.generation, s, 2, GLP_TAG_INIT, p.samp_lo, p.samp_hi,
+                              p.nbr, p.klen);
+          q.w = glp_surrogate(p.seed, p.generation, s, 3, GLP_TAG_INIT, p.samp_lo, p.samp_hi,
+                              p.nbr, p.klen);
+        }
         if (q.x >= H || q.y >= H || q.z >= H || q.w >= H) {
           atomicOr(p.error, 1);
           q = make_uint4(0, 0, 0, 0);
@@ -527,7 +542,9 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
       } else {
         glp_mh_draw(p.seed, p.generation, s, cyc, &slot, &u);
       }
-      phap = __ldg(p.props + (size_t)cyc * N + s);
+      phap = p.props ? __ldg(p.props + (size_t)cyc * N + s)
+                     : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP, p.samp_lo,
+                                     p.samp_hi, p.nbr, p.klen);
       if (phap >= H) {
         atomicOr(p.error, 1);
         phap = 0;
@@ -540,22 +557,28 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
       em.init(p, s, s_vq);
       L = eval_like<E>(p, em, myq);
     }
-    // replay the accept rule in chain order (MHSampler.hpp:86-93)
-    uint32_t first_acc = P;
-#pragma unroll 1
-    for (uint32_t j = 0; j < (uint32_t)P; ++j) {
-      const double Lj = __shfl_sync(FULL, L, gbase + j);
-      const double uj = __shfl_sync(FULL, u, gbase + j);
-      const uint32_t slj = __shfl_sync(FULL, slot, gbase + j);
-      const uint32_t phj = __shfl_sync(FULL, phap, gbase + j);
-      if (active && first_acc == P && j < k) {
-        if (e + j == 0) {
-          curr = Lj;
-        } else if (Lj >= curr || uj < exp((Lj - curr) * (double)p.pen)) {
-          set_slot(q, slj, phj);
-          curr = Lj;
-          first_acc = j;
-        }
+    // The accept rule of MHSampler.hpp:86-93 in chain order.  Every
+    // evaluation of the round was built on the round's starting state, and
+    // until the first acceptance the chain's current likelihood is the
+    // starting one, so each lane tests its own proposal against it in
+    // parallel and the first accepting lane (in chain order) wins: the same
+    // decisions as the sequential loop, one binary64 exp per lane.
+    const double L0 = __shfl_sync(FULL, L, gbase);
+    const double curr0 = (e == 0) ? L0 : curr;
+    const bool acc = on && ev > 0 &&
+                     (L >= curr0 || u < exp((L - curr0) * (double)p.pen));
+    const unsigned gmask = (P == 32) ? FULL : (((1u << P) - 1u) << gbase);
+    const unsigned abal = __ballot_sync(FULL, acc) & gmask;
+    const uint32_t first_acc = abal ? (uint32_t)(__ffs(abal) - 1) - gbase : (uint32_t)P;
+    const uint32_t src = gbase + (abal ? first_acc : 0u);
+    const double La = __shfl_sync(FULL, L, src);
+    const uint32_t sla = __shfl_sync(FULL, slot, src);
+    const uint32_t pha = __shfl_sync(FULL, phap, src);
+    if (active) {
+      curr = curr0;
+      if (abal) {
+        set_slot(q, sla, pha);
+        curr = La;
       }
     }
     if (on) {

@@ -1,0 +1,248 @@
+// glp_knn.cuh -- kNN surrogate restriction on the device: the reference's
+// KNN::ClusterHaps (src/kNN.cpp:123-206) with the Hamming metric
+// (src/haplotype.cpp:35-60) over the common sites of KNN::CutDownHaps
+// (src/kNN.cpp:216-257).
+//
+// For each sample s of the H/2 samples: the ceil(K/2) haplotypes nearest to
+// haplotype 2s, then the ceil(K/2) nearest to haplotype 2s+1 that are not
+// already chosen, interleaved.  The sample's own haplotypes are excluded.
+// Ties are ordered by haplotype index, a total order; the reference sorts
+// with the unstable std::sort (kNN.cpp:172-173), so its tie order is
+// implementation-defined.
+//
+// One CTA per sample.  Distances of both haplotypes to all H haplotypes sit
+// in shared memory as uint16 (H <= kKnnMaxHaps); every warp scores one
+// haplotype at a time with coalesced word loads and a shuffle reduction.  The
+// ceil(K/2) nearest are found by binary search on the distance threshold,
+// ties at the threshold are taken in index order through a block scan, and
+// the chosen list is put in (distance, index) order by a bitonic sort.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace glp {
+
+constexpr int kKnnThreads = 256;
+constexpr uint32_t kKnnMaxHaps = 50000;
+constexpr uint32_t kKnnMaxHalf = 1024;
+constexpr uint16_t kKnnExcluded = 0xffffu;
+
+// Bit m of mask: site m's alt-allele frequency (or MAF) lies in [lb, ub].
+__global__ void common_sites_kernel(const uint64_t *__restrict__ haps, uint32_t H,
+                                    uint32_t wn, uint32_t S, double lb, double ub,
+                                    int use_maf, uint64_t *__restrict__ mask) {
+  const uint32_t w = blockIdx.x;
+  const uint32_t lane = threadIdx.x;  // 64 threads: one site each
+  const uint32_t m = w * 64 + lane;
+  uint32_t alt = 0;
+  if (m < S)
+    for (uint32_t h = 0; h < H; ++h)
+      alt += (uint32_t)((__ldg(haps + (size_t)h * wn + w) >> lane) & 1u);
+  double af = (double)alt / H;
+  if (use_maf)
+    af = fabs(fabs(af - 0.5) - 0.5);
+  const bool keep = m < S && af >= lb && af <= ub;
+  const unsigned lo = __ballot_sync(0xffffffffu, lane < 32 ? keep : false);
+  __shared__ unsigned hi_bits;
+  if (lane == 32)
+    hi_bits = 0;
+  __syncthreads();
+  const unsigned hb = __ballot_sync(0xffffffffu, keep);
+  if (lane == 32)
+    hi_bits = hb;
+  __syncthreads();
+  if (lane == 0)
+    mask[w] = (uint64_t)lo | ((uint64_t)hi_bits << 32);
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *red) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0)
+    red[warp] = v;
+  __syncthreads();
+  uint32_t t = 0;
+#pragma unroll
+  for (int i = 0; i < kKnnThreads / 32; ++i)
+    t += red[i];
+  return t;
+}
+
+// Exclusive prefix over threads (thread order), block total in *total.
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t *red,
+                                                    uint32_t *total) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t n = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o)
+      inc += n;
+  }
+  __syncthreads();
+  if (lane == 31)
+    red[warp] = inc;
+  __syncthreads();
+  uint32_t base = 0, all = 0;
+#pragma unroll
+  for (int i = 0; i < kKnnThreads / 32; ++i) {
+    if ((uint32_t)i < warp)
+      base += red[i];
+    all += red[i];
+  }
+  *total = all;
+  return base + inc - v;
+}
+
+// Choose the `half` smallest (d, index) among entries of d that are not
+// kKnnExcluded, write them sorted to out[0..half).
+__device__ void select_nearest(const uint16_t *d, uint32_t H, uint32_t half, uint32_t dmax,
+                               uint32_t *keys, uint32_t *red, uint32_t *out) {
+  const uint32_t tid = threadIdx.x;
+  // smallest t with #{d <= t} >= half
+  uint32_t lo = 0, hi = dmax;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    uint32_t c = 0;
+    for (uint32_t h = tid; h < H; h += kKnnThreads)
+      c += (d[h] != kKnnExcluded && d[h] <= mid) ? 1u : 0u;
+    if (block_sum(c, red) >= half)
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  const uint32_t t = lo;
+  uint32_t below = 0;
+  for (uint32_t h = tid; h < H; h += kKnnThreads)
+    below += (d[h] != kKnnExcluded && d[h] < t) ? 1u : 0u;
+  below = block_sum(below, red);
+  const uint32_t need = half - below;  // ties at t, taken in index order
+  const uint32_t chunk = (H + kKnnThreads - 1) / kKnnThreads;
+  const uint32_t b0 = min(H, tid * chunk), b1 = min(H, b0 + chunk);
+  uint32_t ties = 0;
+  for (uint32_t h = b0; h < b1; ++h)
+    ties += (d[h] == t) ? 1u : 0u;
+  uint32_t total;
+  uint32_t rank = block_exclusive(ties, red, &total);
+  uint32_t nless = 0;
+  for (uint32_t h = b0; h < b1; ++h)
+    nless += (d[h] != kKnnExcluded && d[h] < t) ? 1u : 0u;
+  uint32_t pos = block_exclusive(nless, red, &total);
+  // entries below the threshold first (positions [0, below)), then ties
+  for (uint32_t h = b0; h < b1; ++h) {
+    const uint16_t v = d[h];
+    if (v == kKnnExcluded)
+      continue;
+    if (v < t) {
+      keys[pos++] = ((uint32_t)v << 16) | 0u;
+      keys[kKnnMaxHalf + pos - 1] = h;
+    } else if (v == t) {
+      if (rank < need) {
+        keys[below + rank] = ((uint32_t)v << 16);
+        keys[kKnnMaxHalf + below + rank] = h;
+      }
+      ++rank;
+    }
+  }
+  __syncthreads();
+  // bitonic sort of (distance, index) over the next power of two
+  uint32_t n2 = 1;
+  while (n2 < half)
+    n2 <<= 1;
+  for (uint32_t i = tid; i < n2; i += kKnnThreads)
+    if (i >= half) {
+      keys[i] = 0xffffffffu;
+      keys[kKnnMaxHalf + i] = 0xffffffffu;
+    }
+  __syncthreads();
+  for (uint32_t k = 2; k <= n2; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = tid; i < n2; i += kKnnThreads) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const uint64_t a = ((uint64_t)keys[i] << 32) | keys[kKnnMaxHalf + i];
+          const uint64_t b = ((uint64_t)keys[l] << 32) | keys[kKnnMaxHalf + l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            keys[i] = (uint32_t)(b >> 32);
+            keys[kKnnMaxHalf + i] = (uint32_t)b;
+            keys[l] = (uint32_t)(a >> 32);
+            keys[kKnnMaxHalf + l] = (uint32_t)a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (uint32_t i = tid; i < half; i += kKnnThreads)
+    out[i] = keys[kKnnMaxHalf + i];
+  __syncthreads();
+}
+
+// Dynamic shared memory: dA, dB [H] uint16, keys [2*kKnnMaxHalf] uint32,
+// chosen [2*kKnnMaxHalf] uint32, taken bits [ceil(H/32)] uint32.
+__global__ void __launch_bounds__(kKnnThreads)
+    knn_kernel(const uint64_t *__restrict__ haps, uint32_t H, uint32_t wn,
+               const uint64_t *__restrict__ mask, uint32_t half, uint32_t dmax,
+               uint32_t *__restrict__ neighbors) {
+  extern __shared__ uint4 knn_smem[];
+  uint16_t *dA = reinterpret_cast<uint16_t *>(knn_smem);
+  uint16_t *dB = dA + H;
+  uint32_t *keys = reinterpret_cast<uint32_t *>(dA + 2 * ((H + 1) & ~1u));
+  uint32_t *chosen = keys + 2 * kKnnMaxHalf;
+  uint32_t *taken = chosen + 2 * kKnnMaxHalf;
+  __shared__ uint32_t red[kKnnThreads / 32];
+  const uint32_t s = blockIdx.x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint64_t *ha = haps + (size_t)2 * s * wn, *hb = ha + wn;
+  for (uint32_t i = tid; i < (H + 31) / 32; i += kKnnThreads)
+    taken[i] = 0;
+  // distances: one haplotype per warp iteration, words across lanes
+  for (uint32_t h = warp; h < H; h += kKnnThreads / 32) {
+    uint32_t a = 0, b = 0;
+    const uint64_t *o = haps + (size_t)h * wn;
+    for (uint32_t w = lane; w < wn; w += 32) {
+      const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
+      a += __popcll((__ldg(ha + w) ^ ow) & mw);
+      b += __popcll((__ldg(hb + w) ^ ow) & mw);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, off);
+      b += __shfl_xor_sync(0xffffffffu, b, off);
+    }
+    if (lane == 0) {
+      const bool own = (h >> 1) == s;
+      dA[h] = own ? kKnnExcluded : (uint16_t)a;
+      dB[h] = own ? kKnnExcluded : (uint16_t)b;
+    }
+  }
+  __syncthreads();
+  select_nearest(dA, H, half, dmax, keys, red, chosen);
+  for (uint32_t i = tid; i < half; i += kKnnThreads) {
+    const uint32_t h = chosen[i];
+    atomicOr(&taken[h >> 5], 1u << (h & 31u));
+  }
+  __syncthreads();
+  for (uint32_t h = tid; h < H; h += kKnnThreads)
+    if ((taken[h >> 5] >> (h & 31u)) & 1u)
+      dB[h] = kKnnExcluded;
+  __syncthreads();
+  select_nearest(dB, H, half, dmax, keys, red, chosen + kKnnMaxHalf);
+  uint32_t *out = neighbors + (size_t)s * 2 * half;
+  for (uint32_t i = tid; i < half; i += kKnnThreads) {
+    out[2 * i] = chosen[i];
+    out[2 * i + 1] = chosen[kKnnMaxHalf + i];
+  }
+}
+
+inline size_t knn_smem_bytes(uint32_t H) {
+  return sizeof(uint16_t) * 2 * ((H + 1) & ~1u) + sizeof(uint32_t) * 4 * kKnnMaxHalf +
+         sizeof(uint32_t) * ((H + 31) / 32);
+}
+
+}  // namespace glp

@@ -99,6 +99,46 @@ GLP_HD void glp_mh_draw(uint64_t seed, uint32_t generation, uint32_t sample,
   *u = glp_u53(x.v[1], x.v[2]);
 }
 
+/* 64-bit draw from two words, reduced modulo n (n <= 2^32; the bias is at
+ * most n / 2^64). */
+GLP_HD uint32_t glp_below(uint32_t hi, uint32_t lo, uint32_t n) {
+  return (uint32_t)((((uint64_t)hi << 32) | (uint64_t)lo) % (uint64_t)n);
+}
+
+/* Surrogate draw for sample s, uniform over haplotypes [lo, hi) except the
+ * sample's own pair 2s, 2s+1 (UnifSampler::SampleHap, sampler.cpp:29-39,
+ * drawn by rejection there; here by skipping the pair).  Returns hi when the
+ * range holds no other haplotype. */
+GLP_HD uint32_t glp_uniform_hap(glp_u32x4 x, uint32_t s, uint32_t lo, uint32_t hi) {
+  const uint32_t a = 2u * s;
+  const int own = (a >= lo && a + 1u < hi);
+  const uint32_t n = hi - lo - (own ? 2u : 0u);
+  if (hi <= lo || n == 0u)
+    return hi;
+  uint32_t h = lo + glp_below(x.v[0], x.v[1], n);
+  if (own && h >= a)
+    h += 2u;
+  return h;
+}
+
+/* Surrogate draw from a neighbour list of length klen (KNN::SampleHap,
+ * kNN.cpp:74-90): the position is uniform over the list. */
+GLP_HD uint32_t glp_table_pos(glp_u32x4 x, uint32_t klen) {
+  return glp_below(x.v[2], x.v[3], klen);
+}
+
+/* One surrogate of sample s: slot `index` of the initial quadruple
+ * (tag GLP_TAG_INIT) or the proposal of cycle `index` (GLP_TAG_PROP), from
+ * the neighbour table nbr [N][klen] when given, else uniform over [lo, hi). */
+GLP_HD uint32_t glp_surrogate(uint64_t seed, uint32_t generation, uint32_t s,
+                              uint32_t index, uint32_t tag, uint32_t lo, uint32_t hi,
+                              const uint32_t *nbr, uint32_t klen) {
+  const glp_u32x4 x = glp_draw(seed, generation, s, index, tag);
+  if (nbr)
+    return nbr[(size_t)s * klen + glp_table_pos(x, klen)];
+  return glp_uniform_hap(x, s, lo, hi);
+}
+
 /* hmm_work uniform for one site. */
 GLP_HD float glp_work_uniform(uint64_t seed, uint32_t generation,
                               uint32_t sample, uint32_t site) {

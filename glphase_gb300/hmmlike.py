@@ -203,7 +203,10 @@ class Engine:
         self.hnew = self.haps.clone()
         self.quad = torch.zeros((4, self.N), dtype=torch.int32, device=self.device)
         self.like = torch.zeros(self.N, dtype=torch.float64, device=self.device)
-        self.stream = torch.cuda.current_stream(self.device)
+        # a dedicated stream: the legacy default stream has handle 0, which the
+        # C ABI reads as "the context's own stream"
+        self.stream = torch.cuda.Stream(self.device)
+        torch.cuda.current_stream(self.device).synchronize()
         self.dev._c(self.dev.L.glp_set_stream(self.dev.ctx, self.stream.cuda_stream))
 
     def args(self, quad_in, props, pen: float, seed: int, generation: int, work: bool = True,

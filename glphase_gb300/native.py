@@ -26,7 +26,7 @@ EXPORTED = [
     "glp_set_tran", "glp_set_mutation_mat", "glp_set_codebook", "glp_set_packed_gls",
     "glp_set_emission", "glp_run_hmm_on_device", "glp_run_generation",
     "glp_run_generation_host", "glp_finish", "glp_set_lanes_per_sample", "glp_get_stats",
-    "glp_measure_fp32_peak",
+    "glp_measure_fp32_peak", "glp_knn_neighbors",
 ]
 
 
@@ -50,6 +50,8 @@ class GenerationArgs(C.Structure):
         ("flags", C.c_uint32),
         ("trace_slot", C.c_void_p), ("trace_accept", C.c_void_p), ("trace_work", C.c_void_p),
         ("like_out", C.c_void_p), ("eval_trace", C.c_void_p), ("accept_trace", C.c_void_p),
+        ("neighbors", C.c_void_p), ("neighbors_per_sample", C.c_uint32),
+        ("sample_lo", C.c_uint32), ("sample_hi", C.c_uint32),
     ]
 
 
@@ -93,6 +95,7 @@ def load(build_if_missing: bool = False):
     L.glp_set_lanes_per_sample.argtypes = [vp, u32]
     L.glp_get_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u32)]
     L.glp_measure_fp32_peak.argtypes = [vp, C.c_float, C.POINTER(C.c_double)]
+    L.glp_knn_neighbors.argtypes = [vp, vp, u32, u32, u32, C.c_double, C.c_double, i32, vp]
     for name in EXPORTED:
         getattr(L, name)
     _lib = L

@@ -79,6 +79,16 @@ typedef struct glp_generation_args {
   double *like_out;            /* [N] final log-likelihood of each chain */
   double *eval_trace;          /* [N][C+1] every evaluated log-likelihood */
   uint8_t *accept_trace;       /* [N][C] accept decisions */
+  /* Device-side surrogate draws, used for whichever of hap_idxs_in / props
+   * is NULL: the 4 initial and C proposal haplotypes of each sample are drawn
+   * in the kernel from the counter-based streams, from the neighbour table
+   * when given (KNN::SampleHap, src/kNN.cpp:74-90), else uniformly over
+   * [sample_lo, sample_hi) minus the sample's own pair
+   * (UnifSampler::SampleHap, src/sampler.cpp:29-39); 0,0 means [0, H).
+   * Replaces the host draws of RunHMMOnSamples (src/hmmLike.cpp:90-102). */
+  const uint32_t *neighbors;     /* [N][neighbors_per_sample] device, or NULL */
+  uint32_t neighbors_per_sample;
+  uint32_t sample_lo, sample_hi;
 } glp_generation_args;
 
 /* Number of visible CUDA devices and whether device `device` is an sm_103
@@ -156,6 +166,18 @@ int glp_set_lanes_per_sample(glp_ctx *ctx, uint32_t lanes);
  * rounds of the most recent generation (after glp_finish). */
 int glp_get_stats(glp_ctx *ctx, uint64_t *evaluations, uint64_t *rounds,
                   uint32_t *lanes_used);
+
+/* kNN surrogate restriction on the device: for each of the H/2 samples,
+ * the ceil(K/2) haplotypes nearest (Hamming distance over the sites whose
+ * alt-allele frequency, or MAF when use_maf, lies in [freq_lb, freq_ub]) to
+ * its first haplotype, then the ceil(K/2) nearest to its second that are not
+ * yet chosen, interleaved; ties in index order.  haps and neighbors
+ * ([H/2][2*ceil(K/2)]) are DEVICE pointers; asynchronous, finish with
+ * glp_finish().  Replaces KNN::KNN / KNN::ClusterHaps (src/kNN.cpp:7-206)
+ * with the Hamming metric.  Needs H <= 50000 and 2*ceil(K/2) <= H - 2. */
+int glp_knn_neighbors(glp_ctx *ctx, const uint64_t *haps, uint32_t num_haps, uint32_t num_sites,
+                      uint32_t k, double freq_lb, double freq_ub, int use_maf,
+                      uint32_t *neighbors);
 
 /* Calibration (no reference counterpart): runs a dependent-free FMA stream on
  * every SM for about `ms_target` milliseconds and reports the achieved FP32

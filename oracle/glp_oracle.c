@@ -445,6 +445,112 @@ void glpo_work_uniforms(uint64_t seed, uint32_t generation, uint32_t sample, uin
     u[m] = glp_work_uniform(seed, generation, sample, m);
 }
 
+void glpo_sample_surrogates(uint64_t seed, uint32_t generation, uint32_t N, uint32_t C,
+                            uint32_t lo, uint32_t hi, const uint32_t *nbr, uint32_t klen,
+                            uint32_t *quad, uint32_t *props) {
+  for (uint32_t s = 0; s < N; ++s) {
+    for (uint32_t j = 0; j < 4; ++j)
+      quad[(size_t)j * N + s] =
+          glp_surrogate(seed, generation, s, j, GLP_TAG_INIT, lo, hi, nbr, klen);
+    for (uint32_t c = 0; c < C; ++c)
+      props[(size_t)c * N + s] =
+          glp_surrogate(seed, generation, s, c, GLP_TAG_PROP, lo, hi, nbr, klen);
+  }
+}
+
+/* kNN.cpp:216-257 */
+void glpo_common_sites(const uint64_t *haps, uint32_t H, uint32_t wn, uint32_t S,
+                       double lb, double ub, int use_maf, uint64_t *mask) {
+  memset(mask, 0, sizeof(uint64_t) * wn);
+  for (uint32_t m = 0; m < S; ++m) {
+    uint32_t alt = 0;
+    for (uint32_t h = 0; h < H; ++h)
+      alt += bit_test(haps + (size_t)h * wn, m);
+    double af = (double)alt / H;
+    if (use_maf)
+      af = fabs(fabs(af - 0.5) - 0.5);
+    if (af >= lb && af <= ub)
+      mask[m >> 6] |= (uint64_t)1 << (m & 63);
+  }
+}
+
+typedef struct {
+  uint32_t d, idx;
+} knn_pair;
+
+static int knn_cmp(const void *a, const void *b) {
+  const knn_pair *x = (const knn_pair *)a, *y = (const knn_pair *)b;
+  if (x->d != y->d)
+    return x->d < y->d ? -1 : 1;
+  return x->idx < y->idx ? -1 : (x->idx > y->idx ? 1 : 0);
+}
+
+static uint32_t hamming_masked(const uint64_t *a, const uint64_t *b,
+                               const uint64_t *mask, uint32_t wn) {
+  uint32_t d = 0;
+  for (uint32_t w = 0; w < wn; ++w)
+    d += (uint32_t)__builtin_popcountll((a[w] ^ b[w]) & mask[w]);
+  return d;
+}
+
+/* kNN.cpp:123-206 */
+int glpo_knn(const uint64_t *haps, uint32_t H, uint32_t wn, const uint64_t *mask,
+             uint32_t K, uint32_t *neighbors) {
+  const uint32_t half = (K + 1) / 2, len = 2 * half, ns = H / 2;
+  if (H < 2 || H - 2 < len)
+    return -1;
+  int failed = 0;
+#ifdef _OPENMP
+#pragma omp parallel reduction(| : failed)
+#endif
+  {
+    knn_pair *da = (knn_pair *)malloc(sizeof(knn_pair) * H);
+    knn_pair *db = (knn_pair *)malloc(sizeof(knn_pair) * H);
+    uint8_t *taken = (uint8_t *)malloc(H);
+    if (!da || !db || !taken) {
+      failed = 1;
+    } else {
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+      for (long s = 0; s < (long)ns; ++s) {
+        const uint64_t *ha = haps + (size_t)2 * s * wn, *hb = ha + wn;
+        uint32_t n = 0;
+        for (uint32_t h = 0; h < H; ++h) {
+          if ((h >> 1) == (uint32_t)s)
+            continue;
+          const uint64_t *o = haps + (size_t)h * wn;
+          da[n].d = hamming_masked(ha, o, mask, wn);
+          da[n].idx = h;
+          db[n].d = hamming_masked(hb, o, mask, wn);
+          db[n].idx = h;
+          ++n;
+        }
+        qsort(da, n, sizeof(knn_pair), knn_cmp);
+        qsort(db, n, sizeof(knn_pair), knn_cmp);
+        memset(taken, 0, H);
+        uint32_t *out = neighbors + (size_t)s * len;
+        for (uint32_t i = 0; i < half; ++i) {
+          out[2 * i] = da[i].idx;
+          taken[da[i].idx] = 1;
+        }
+        uint32_t j = 0;
+        for (uint32_t i = 0; i < half; ++i) {
+          while (taken[db[j].idx])
+            ++j;
+          out[2 * i + 1] = db[j].idx;
+          taken[db[j].idx] = 1;
+          ++j;
+        }
+      }
+    }
+    free(da);
+    free(db);
+    free(taken);
+  }
+  return failed ? -1 : 0;
+}
+
 /* impute.cpp:564-595 */
 void glpo_replace(const uint64_t *haps, uint32_t wn, uint32_t S,
                   uint32_t sample, uint32_t *hsum) {

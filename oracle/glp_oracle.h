@@ -144,6 +144,29 @@ void glpo_mh_draws(uint64_t seed, uint32_t generation, uint32_t sample, uint32_t
 void glpo_work_uniforms(uint64_t seed, uint32_t generation, uint32_t sample, uint32_t S,
                         float *u);
 
+/* The surrogates a generation draws on the device (glp_surrogate of
+ * glp_rng.h), materialised: quad [4][N] and props [C][N]; nbr [N][klen] or
+ * NULL for uniform over [lo, hi) minus the sample's own pair. */
+void glpo_sample_surrogates(uint64_t seed, uint32_t generation, uint32_t N, uint32_t C,
+                            uint32_t lo, uint32_t hi, const uint32_t *nbr, uint32_t klen,
+                            uint32_t *quad, uint32_t *props);
+
+/* KNN::CalculateVarAfs + CutDownHaps (kNN.cpp:216-257): bit m of mask is
+ * set when site m's alt-allele frequency over all H haplotypes (or its minor
+ * allele frequency) lies in [lb, ub].  mask is [wn] uint64. */
+void glpo_common_sites(const uint64_t *haps, uint32_t H, uint32_t wn, uint32_t S,
+                       double lb, double ub, int use_maf, uint64_t *mask);
+
+/* KNN::ClusterHaps (kNN.cpp:123-206), Hamming metric over the masked sites:
+ * for each of the H/2 samples, the ceil(K/2) haplotypes nearest to its first
+ * haplotype, then the ceil(K/2) nearest to its second that are not already
+ * chosen, interleaved (first, second, first, ...).  Ties are ordered by
+ * haplotype index (the reference's std::sort is unstable, kNN.cpp:172-173).
+ * neighbors is [H/2][2*ceil(K/2)].  Returns 0, or -1 when H - 2 < the list
+ * length. */
+int glpo_knn(const uint64_t *haps, uint32_t H, uint32_t wn, const uint64_t *mask,
+             uint32_t K, uint32_t *neighbors);
+
 /* Impute::replace (impute.cpp:564-595): per-site allele tallies, hsum is
  * [2N][S] uint32. */
 void glpo_replace(const uint64_t *haps, uint32_t wn, uint32_t S,

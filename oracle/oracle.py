@@ -88,6 +88,13 @@ def lib():
                                          _u32p]
         L.glpo_mh_draws.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, _u8p, _f64p]
         L.glpo_work_uniforms.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
+        L.glpo_sample_surrogates.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
+                                             C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32,
+                                             _u32p, _u32p]
+        L.glpo_common_sites.argtypes = [_u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double,
+                                        C.c_double, C.c_int, _u64p]
+        L.glpo_knn.restype = C.c_int
+        L.glpo_knn.argtypes = [_u64p, C.c_uint32, C.c_uint32, _u64p, C.c_uint32, _u32p]
         L.glpo_replace.argtypes = [_u64p, C.c_uint32, C.c_uint32, C.c_uint32, _u32p]
         L.glpo_result.argtypes = [_u32p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
         _lib = L
@@ -237,3 +244,37 @@ def work_uniforms(seed, generation, sample, S):
     u = np.zeros(S, np.float32)
     lib().glpo_work_uniforms(seed, generation, sample, S, u)
     return u
+
+
+def sample_surrogates(seed, generation, N, C_cycles, lo, hi, nbr=None):
+    """The surrogates a generation draws on the device, materialised:
+    (quad [4][N], props [C][N])."""
+    quad = np.zeros((4, N), np.uint32)
+    props = np.zeros((max(C_cycles, 1), N), np.uint32)
+    if nbr is not None:
+        nb = _c(nbr, np.uint32)
+        ptr, klen = nb.ctypes.data, nb.shape[1]
+    else:
+        nb, ptr, klen = None, None, 0
+    lib().glpo_sample_surrogates(seed, generation, N, C_cycles, lo, hi, ptr, klen, quad, props)
+    return quad, props[:C_cycles]
+
+
+def common_sites(haps, S, lb=0.0, ub=1.0, use_maf=False):
+    haps = _c(haps, np.uint64)
+    H, wn = haps.shape
+    mask = np.zeros(wn, np.uint64)
+    lib().glpo_common_sites(haps, H, wn, S, lb, ub, int(use_maf), mask)
+    return mask
+
+
+def knn(haps, S, K, lb=0.0, ub=1.0, use_maf=False):
+    """KNN::ClusterHaps restated: [H/2][2*ceil(K/2)] neighbour lists."""
+    haps = _c(haps, np.uint64)
+    H, wn = haps.shape
+    mask = common_sites(haps, S, lb, ub, use_maf)
+    half = (K + 1) // 2
+    out = np.zeros((H // 2, 2 * half), np.uint32)
+    if lib().glpo_knn(haps, H, wn, mask, K, out) != 0:
+        raise ValueError("kNN list longer than the available haplotypes")
+    return out

@@ -41,20 +41,20 @@ def make_problem(N=24, S=300, C=20, panel=0, seed=3, founders=6, depth=3.0):
 def run_gpu(dev, m, haps, quad, props, pen, seed=11, gen=0, flags=0, trace=None):
     N, S = m.N, m.S
     H, wn = haps.shape
-    C = props.shape[0]
+    Cc = props.shape[0]
     dev.copy_tran_to_device(m.tran)
     dev.copy_mutation_mat_to_device(m.pc)
     dev.copy_emission_to_device(m.emit, m.t)
     a = nat.GenerationArgs()
-    a.num_samples, a.num_sites, a.num_cycles, a.num_haps = N, S, C, H
+    a.num_samples, a.num_sites, a.num_cycles, a.num_haps = N, S, Cc, H
     haps = np.ascontiguousarray(haps)
     hnew = haps.copy()
     quad_in = np.ascontiguousarray(quad, dtype=np.uint32)
     quad_out = np.zeros_like(quad_in)
     props_c = np.ascontiguousarray(props, dtype=np.uint32)
     like = np.zeros(N, np.float64)
-    evals = np.full((N, C + 1), np.nan, np.float64)
-    acc = np.zeros((N, max(C, 1)), np.uint8)
+    evals = np.full((N, Cc + 1), np.nan, np.float64)
+    acc = np.zeros((N, max(Cc, 1)), np.uint8)
     a.haps, a.hnew = _p(haps), _p(hnew)
     a.hap_idxs_in, a.hap_idxs_out, a.props = _p(quad_in), _p(quad_out), _p(props_c)
     a.pen, a.seed, a.generation, a.flags = pen, seed, gen, flags
@@ -65,7 +65,7 @@ def run_gpu(dev, m, haps, quad, props, pen, seed=11, gen=0, flags=0, trace=None)
     rc = dev.L.glp_run_generation_host(dev.ctx, C.byref(a))
     if rc != nat.GLP_OK:
         raise nat.GlpError(rc, dev.L.glp_last_error(dev.ctx).decode())
-    return dict(quad=quad_out, hnew=hnew, like=like, evals=evals, acc=acc[:, :C])
+    return dict(quad=quad_out, hnew=hnew, like=like, evals=evals, acc=acc[:, :Cc])
 
 
 @pytest.fixture(scope="module")

@@ -213,3 +213,47 @@ def test_generation_reproducible_and_consistent(oracle_lib):
         assert np.array_equal(q, q1[:, s])
         assert np.array_equal(ha, h1[2 * s]) and np.array_equal(hb, h1[2 * s + 1])
         assert curr == l1[s]
+
+
+def test_knn_reference_kat(oracle_lib):
+    """KNN::ClusterHaps against src/testing/other_unittests.cpp:103-254."""
+    import knn_cases as kc
+    O = oracle_lib
+    for case in (kc.case_nearest, kc.case_threshold):
+        bits, perm, lb, ub, want = case()
+        haps = mdl.pack_haplotypes(bits)
+        nb = O.knn(haps, kc.NUM_SITES, kc.NUM_CLUSTERS, lb, ub)
+        assert [int(perm[i]) for i in nb[0]] == want
+    bits, perm, lb, ub, _ = kc.case_threshold()
+    mask = O.common_sites(mdl.pack_haplotypes(bits), kc.NUM_SITES, lb, ub)
+    _, ncommon = kc.expected_af_threshold()
+    assert bin(int(mask[0])).count("1") == ncommon
+    af = bits.mean(axis=0)
+    assert list(af[:3]) == kc.expected_af_threshold()[0]
+
+
+def test_knn_lists_are_valid(oracle_lib):
+    O = oracle_lib
+    rng = np.random.default_rng(8)
+    haps = rng.integers(0, 2**63, size=(60, 3), dtype=np.uint64)
+    nb = O.knn(haps, 150, 20)
+    assert nb.shape == (30, 20)
+    for s in range(30):
+        assert len(set(nb[s].tolist())) == 20           # unique
+        assert all(h // 2 != s for h in nb[s])           # never the sample's own
+
+
+def test_device_surrogate_streams(oracle_lib):
+    """Uniform draws avoid the sample's own pair and cover [lo, hi)."""
+    O = oracle_lib
+    q, p = O.sample_surrogates(9, 3, 50, 400, 0, 100)
+    for s in range(50):
+        allh = np.r_[q[:, s], p[:, s]]
+        assert not np.any(allh // 2 == s)
+        assert allh.max() < 100
+    q, p = O.sample_surrogates(9, 3, 50, 400, 100, 130)   # panel-only range
+    assert p.min() >= 100 and p.max() < 130
+    nbr = np.tile(np.arange(7, dtype=np.uint32)[None, :] + 60, (50, 1))
+    q, p = O.sample_surrogates(9, 3, 50, 100, 0, 0, nbr=nbr)
+    assert p.min() >= 60 and p.max() < 67
+    assert len(np.unique(p)) == 7
