@@ -1,12 +1,14 @@
 // glp_api.cu -- host side of the C ABI declared in include/glphase_gpu.h.
 //
-// Owns the device-resident model inputs of one phasing problem (transition
-// table, mutation matrix, emissions or VQ codes, genotype probabilities) and
-// the per-generation work buffers, and launches the generation kernel of
-// glp_kernels.cuh.  Every entry point returns a status code; nothing exits,
-// throws across the boundary or resets the device (the reference's
-// HMMLikeCUDA calls exit(EXIT_FAILURE) on CUDA errors, src/hmmLike.cu:240-300,
-// and cudaDeviceReset in Cleanup, src/hmmLike.cu:396).
+// A context owns a device, a stream and the per-generation work buffers.  A
+// problem (one phasing chunk) owns its device-resident model inputs:
+// transition table, mutation matrix, emissions or VQ codes, genotype
+// probabilities and the hmm_work scratch.  The context's own model (the
+// glp_set_* calls that replace HMMLikeCUDA's Copy*ToDevice) is its default
+// problem.  Every entry point returns a status code; nothing exits, throws
+// across the boundary or resets the device (the reference's HMMLikeCUDA calls
+// exit(EXIT_FAILURE) on CUDA errors, src/hmmLike.cu:240-300, and
+// cudaDeviceReset in Cleanup, src/hmmLike.cu:396).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,31 +23,41 @@
 #include "glp_kernels.cuh"
 #include "glp_knn.cuh"
 
+struct glp_problem {
+  glp_ctx *ctx = nullptr;
+  uint32_t S = 0;  // sites of tran
+  float4 *d_tran4 = nullptr;
+  float pc[16] = {0};
+  bool have_pc = false;
+  float codebook[32] = {0};
+  bool have_codebook = false;
+  float4 *d_vq = nullptr;  // [16] emission per VQ code
+  uint32_t *d_packed = nullptr;
+  size_t packed_words = 0;
+  float4 *d_emit = nullptr;
+  float *d_prob = nullptr;
+  uint32_t eN = 0, eS = 0;  // shape of emit/prob
+  float4 *d_beta = nullptr;  // hmm_work scratch [N][S]
+  size_t beta_cap = 0;
+};
+
 struct glp_ctx {
   int device = 0;
   int sms = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   std::string err;
-  // model inputs
-  uint32_t S = 0;           // sites of tran
-  float4 *d_tran4 = nullptr;
-  float pc[16] = {0};
-  bool have_pc = false;
-  float codebook[32] = {0};
-  bool have_codebook = false;
-  float4 *d_vq = nullptr;   // [16] emission per VQ code
-  uint32_t *d_packed = nullptr;
-  size_t packed_words = 0;
-  float4 *d_emit = nullptr;
-  float *d_prob = nullptr;
-  uint32_t eN = 0, eS = 0;  // shape of emit/prob
+  glp_problem def;  // the model set by glp_set_* (HMMLikeCUDA semantics)
   // work buffers
   uint32_t *d_counter = nullptr;
   unsigned long long *d_stats = nullptr;
   int *d_error = nullptr;
-  float4 *d_beta = nullptr;
-  size_t beta_cap = 0;
+  glp::GenParams *d_table = nullptr;  // batch descriptors
+  uint32_t *d_offsets = nullptr;
+  size_t table_cap = 0, offsets_cap = 0;
+  glp::GenParams *h_table = nullptr;  // pinned staging
+  uint32_t *h_offsets = nullptr;
+  size_t h_cap = 0;
   // staging for the host-pointer entry points
   uint64_t *d_haps = nullptr, *d_hnew = nullptr;
   size_t haps_cap = 0, hnew_cap = 0;
@@ -59,10 +71,10 @@ struct glp_ctx {
   size_t tr_slot_cap = 0, acc_cap = 0, tr_u_cap = 0, like_cap = 0, evals_cap = 0,
          tr_work_cap = 0;
   // tuning and statistics
-  uint32_t lanes = 0;        // 0 = automatic
+  uint32_t lanes = 0;  // 0 = automatic
   uint32_t lanes_used = 4;
-  double last_accept = -1.0; // acceptance rate of the last generation
-  uint32_t last_N = 0, last_C = 0;
+  double last_accept = -1.0;  // acceptance rate of the last generation
+  uint64_t last_chain_cycles = 0;
   unsigned long long last_stats[3] = {0, 0, 0};
 };
 
@@ -107,60 +119,167 @@ void release(T *&p) {
   p = nullptr;
 }
 
+void release_problem(glp_problem *pb) {
+  release(pb->d_tran4);
+  release(pb->d_vq);
+  release(pb->d_packed);
+  release(pb->d_emit);
+  release(pb->d_prob);
+  release(pb->d_beta);
+  pb->S = pb->eN = pb->eS = 0;
+  pb->packed_words = pb->beta_cap = 0;
+}
+
+int check_ctx(glp_ctx *c) {
+  if (!c)
+    return GLP_ERR_ARG;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess)
+    return fail(c, GLP_ERR_CUDA, "cudaSetDevice(%d): %s", c->device, cudaGetErrorString(e));
+  return GLP_OK;
+}
+
 // FillEmit of every codebook entry (hmmLike.cu:12-44): G = (cb0, cb1,
 // max(1 - cb0 - cb1, 0)), emit[i] = pc[i][0] G0 + pc[i][1] G1 + pc[i][2] G1
 // + pc[i][3] G2.  Host code is built with -ffp-contract=off, so each term is
 // rounded exactly as in the CPU reference.
-int upload_vq_table(glp_ctx *c) {
-  if (!c->have_pc || !c->have_codebook)
+int upload_vq_table(glp_problem *pb) {
+  glp_ctx *c = pb->ctx;
+  if (!pb->have_pc || !pb->have_codebook)
     return GLP_OK;
   float4 tab[16];
   for (int code = 0; code < 16; ++code) {
-    const float g0 = c->codebook[2 * code], g1 = c->codebook[2 * code + 1];
+    const float g0 = pb->codebook[2 * code], g1 = pb->codebook[2 * code + 1];
     const float rest = 1 - g0 - g1;
     const float g2 = rest > 0.0f ? rest : 0.0f;
     float em[4];
     for (int i = 0; i < 4; ++i) {
-      const float a = c->pc[i * 4 + 0] * g0;
-      const float b = c->pc[i * 4 + 1] * g1;
-      const float d = c->pc[i * 4 + 2] * g1;
-      const float f = c->pc[i * 4 + 3] * g2;
+      const float a = pb->pc[i * 4 + 0] * g0;
+      const float b = pb->pc[i * 4 + 1] * g1;
+      const float d = pb->pc[i * 4 + 2] * g1;
+      const float f = pb->pc[i * 4 + 3] * g2;
       em[i] = ((a + b) + d) + f;
     }
     tab[code] = make_float4(em[0], em[1], em[2], em[3]);
   }
-  if (!c->d_vq)
-    GLP_CUDA(c, cudaMalloc((void **)&c->d_vq, sizeof(tab)));
-  GLP_CUDA(c, cudaMemcpy(c->d_vq, tab, sizeof(tab), cudaMemcpyHostToDevice));
+  if (!pb->d_vq)
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_vq, sizeof(tab)));
+  GLP_CUDA(c, cudaMemcpy(pb->d_vq, tab, sizeof(tab), cudaMemcpyHostToDevice));
   return GLP_OK;
 }
 
-using KernelFn = void (*)(const glp::GenParams);
-
-template <int P>
-KernelFn pick_kernel(bool vq) {
-  return vq ? glp::generation_kernel<P, glp::EmitVQ> : glp::generation_kernel<P, glp::EmitF32>;
+int set_tran(glp_problem *pb, const float *tran, uint32_t S) {
+  glp_ctx *c = pb->ctx;
+  if (!tran || S == 0)
+    return fail(c, GLP_ERR_ARG, "tran must be non-null with num_sites > 0");
+  std::vector<float4> t4(S);
+  t4[0] = make_float4(1.f, 0.f, 0.f, 0.f);  // row 0 is unused by the recursion
+  for (uint32_t m = 1; m < S; ++m)
+    t4[m] = make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2], 0.f);
+  if (pb->S != S) {
+    release(pb->d_tran4);
+    pb->S = 0;
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_tran4, sizeof(float4) * S));
+    pb->S = S;
+  }
+  GLP_CUDA(c, cudaMemcpy(pb->d_tran4, t4.data(), sizeof(float4) * S, cudaMemcpyHostToDevice));
+  return GLP_OK;
 }
 
-KernelFn kernel_for(uint32_t lanes, bool vq) {
+int set_pc(glp_problem *pb, const float *pc16) {
+  if (!pc16)
+    return fail(pb->ctx, GLP_ERR_ARG, "pc must be non-null");
+  std::memcpy(pb->pc, pc16, sizeof(pb->pc));
+  pb->have_pc = true;
+  return upload_vq_table(pb);
+}
+
+int set_codebook(glp_problem *pb, const float *codebook, uint32_t entries) {
+  if (!codebook || entries != 16)
+    return fail(pb->ctx, GLP_ERR_ARG, "codebook must hold 16 (RR, Het) entries, got %u",
+                entries);
+  std::memcpy(pb->codebook, codebook, sizeof(pb->codebook));
+  pb->have_codebook = true;
+  return upload_vq_table(pb);
+}
+
+int set_packed(glp_problem *pb, const uint32_t *packed, size_t n) {
+  glp_ctx *c = pb->ctx;
+  if (!packed || n == 0)
+    return fail(c, GLP_ERR_ARG, "packed GLs must be non-empty");
+  if (n != pb->packed_words) {
+    release(pb->d_packed);
+    pb->packed_words = 0;
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_packed, sizeof(uint32_t) * n));
+    pb->packed_words = n;
+  }
+  GLP_CUDA(c, cudaMemcpy(pb->d_packed, packed, sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+  return GLP_OK;
+}
+
+int set_emission(glp_problem *pb, const float *emit, const float *prob, uint32_t N,
+                 uint32_t S) {
+  glp_ctx *c = pb->ctx;
+  if (!emit || N == 0 || S == 0)
+    return fail(c, GLP_ERR_ARG, "emit must be non-null with positive N and S");
+  const size_t ns = (size_t)N * S;
+  if (pb->eN != N || pb->eS != S) {
+    release(pb->d_emit);
+    release(pb->d_prob);
+    pb->eN = pb->eS = 0;
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_emit, sizeof(float4) * ns));
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_prob, sizeof(float) * 3 * ns));
+    pb->eN = N;
+    pb->eS = S;
+  }
+  GLP_CUDA(c, cudaMemcpy(pb->d_emit, emit, sizeof(float4) * ns, cudaMemcpyHostToDevice));
+  if (prob)
+    GLP_CUDA(c, cudaMemcpy(pb->d_prob, prob, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice));
+  return GLP_OK;
+}
+
+using SingleFn = void (*)(const glp::GenParams);
+using MultiFn = void (*)(const glp::MultiParams);
+
+template <int P>
+SingleFn single_for(bool vq) {
+  return vq ? glp::generation_kernel<P, glp::EmitVQ> : glp::generation_kernel<P, glp::EmitF32>;
+}
+template <int P>
+MultiFn multi_for(bool vq) {
+  return vq ? glp::generation_multi_kernel<P, glp::EmitVQ>
+            : glp::generation_multi_kernel<P, glp::EmitF32>;
+}
+
+SingleFn single_kernel(uint32_t lanes, bool vq) {
   switch (lanes) {
-    case 1: return pick_kernel<1>(vq);
-    case 2: return pick_kernel<2>(vq);
-    case 4: return pick_kernel<4>(vq);
-    case 8: return pick_kernel<8>(vq);
-    case 16: return pick_kernel<16>(vq);
-    default: return pick_kernel<32>(vq);
+    case 1: return single_for<1>(vq);
+    case 2: return single_for<2>(vq);
+    case 4: return single_for<4>(vq);
+    case 8: return single_for<8>(vq);
+    case 16: return single_for<16>(vq);
+    default: return single_for<32>(vq);
+  }
+}
+MultiFn multi_kernel(uint32_t lanes, bool vq) {
+  switch (lanes) {
+    case 1: return multi_for<1>(vq);
+    case 2: return multi_for<2>(vq);
+    case 4: return multi_for<4>(vq);
+    case 8: return multi_for<8>(vq);
+    case 16: return multi_for<16>(vq);
+    default: return multi_for<32>(vq);
   }
 }
 
 // Speculation width: the expected useful fraction of a round of P
 // evaluations at acceptance rate a is (1 - (1-a)^P) / (a P); lanes are
 // useful only while N*P does not exceed the threads the GPU keeps resident.
-uint32_t choose_lanes(const glp_ctx *c, uint32_t N) {
+uint32_t choose_lanes(const glp_ctx *c, uint64_t N) {
   if (c->lanes)
     return c->lanes;
   const double a = c->last_accept < 0 ? 0.12 : std::max(c->last_accept, 1e-3);
-  const double resident = (double)c->sms * 1024.0;
+  const double resident = (double)c->sms * 512.0;
   uint32_t best = 1;
   double best_score = 0;
   for (uint32_t P = 1; P <= 32; P <<= 1) {
@@ -175,16 +294,9 @@ uint32_t choose_lanes(const glp_ctx *c, uint32_t N) {
   return best;
 }
 
-int check_ctx(glp_ctx *c) {
-  if (!c)
-    return GLP_ERR_ARG;
-  cudaError_t e = cudaSetDevice(c->device);
-  if (e != cudaSuccess)
-    return fail(c, GLP_ERR_CUDA, "cudaSetDevice(%d): %s", c->device, cudaGetErrorString(e));
-  return GLP_OK;
-}
-
-int launch_generation(glp_ctx *c, const glp_generation_args *a) {
+// Validate one (problem, generation) pair and fill its kernel descriptor.
+int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
+                glp::GenParams *p) {
   const bool vq = (a->flags & GLP_GEN_VQ) != 0;
   const bool work = (a->flags & GLP_GEN_NO_WORK) == 0;
   const uint32_t N = a->num_samples, S = a->num_sites, C = a->num_cycles, H = a->num_haps;
@@ -207,23 +319,23 @@ int launch_generation(glp_ctx *c, const glp_generation_args *a) {
   }
   if (work && !a->hnew)
     return fail(c, GLP_ERR_ARG, "hnew is required unless GLP_GEN_NO_WORK is set");
-  if (!c->d_tran4 || c->S != S)
+  if (!pb->d_tran4 || pb->S != S)
     return fail(c, GLP_ERR_STATE, "transition matrix not set for %u sites", S);
-  if (!c->have_pc)
+  if (!pb->have_pc)
     return fail(c, GLP_ERR_STATE, "mutation matrix not set");
   if (vq) {
-    if (!c->d_packed || !c->d_vq)
+    if (!pb->d_packed || !pb->d_vq)
       return fail(c, GLP_ERR_STATE, "packed GLs and codebook are required in VQ mode");
     const size_t want = (size_t)N * ((S + 7) / 8);
-    if (c->packed_words != want)
-      return fail(c, GLP_ERR_ARG, "packed GLs have %zu words, expected %zu", c->packed_words,
+    if (pb->packed_words != want)
+      return fail(c, GLP_ERR_ARG, "packed GLs have %zu words, expected %zu", pb->packed_words,
                   want);
   }
   if (!vq || work) {
-    if (!c->d_emit || c->eN != N || c->eS != S)
+    if (!pb->d_emit || pb->eN != N || pb->eS != S)
       return fail(c, GLP_ERR_STATE, "emission not set for N=%u S=%u", N, S);
   }
-  if (work && !c->d_prob)
+  if (work && !pb->d_prob)
     return fail(c, GLP_ERR_STATE, "genotype probabilities not set (needed by hmm_work)");
   const bool tr = a->trace_slot || a->trace_accept || a->trace_work;
   if (tr && !(a->trace_slot && a->trace_accept && a->trace_work))
@@ -231,160 +343,88 @@ int launch_generation(glp_ctx *c, const glp_generation_args *a) {
   if (!(a->pen > 0.0f) || !std::isfinite(a->pen))
     return fail(c, GLP_ERR_ARG, "pen must be positive and finite");
   if (work) {
-    int rc = ensure(c, c->d_beta, c->beta_cap, (size_t)N * S);
+    int rc = ensure(c, pb->d_beta, pb->beta_cap, (size_t)N * S);
     if (rc)
       return rc;
   }
+  std::memset(p, 0, sizeof(*p));
+  p->N = N;
+  p->S = S;
+  p->C = C;
+  p->H = H;
+  p->wn = (S + 63) / 64;
+  p->emit_mode = vq ? GLP_EMIT_VQ : GLP_EMIT_FLOAT;
+  p->haps = a->haps;
+  p->hnew = a->hnew;
+  p->emit = pb->d_emit;
+  p->prob = pb->d_prob;
+  p->tran4 = pb->d_tran4;
+  p->packed = pb->d_packed;
+  p->vq_table = vq ? pb->d_vq : nullptr;
+  p->quad_in = a->hap_idxs_in;
+  p->quad_out = a->hap_idxs_out;
+  p->props = a->props;
+  p->tr_slot = a->trace_slot;
+  p->tr_u = a->trace_accept;
+  p->tr_work = a->trace_work;
+  p->like_out = a->like_out;
+  p->eval_trace = a->eval_trace;
+  p->accept_trace = a->accept_trace;
+  p->beta = pb->d_beta;
+  p->counter = c->d_counter;
+  p->stats = c->d_stats;
+  p->error = c->d_error;
+  p->nbr = a->neighbors;
+  p->klen = a->neighbors_per_sample;
+  p->samp_lo = lo;
+  p->samp_hi = hi;
+  std::memcpy(p->pc, pb->pc, sizeof(p->pc));
+  p->pen = a->pen;
+  p->seed = a->seed;
+  p->generation = a->generation;
+  p->do_work = work ? 1u : 0u;
+  return GLP_OK;
+}
 
-  glp::GenParams p;
-  std::memset(&p, 0, sizeof(p));
-  p.N = N;
-  p.S = S;
-  p.C = C;
-  p.H = H;
-  p.wn = (S + 63) / 64;
-  p.emit_mode = vq ? GLP_EMIT_VQ : GLP_EMIT_FLOAT;
-  p.haps = a->haps;
-  p.hnew = a->hnew;
-  p.emit = c->d_emit;
-  p.prob = c->d_prob;
-  p.tran4 = c->d_tran4;
-  p.packed = c->d_packed;
-  p.vq_table = vq ? c->d_vq : nullptr;
-  p.quad_in = a->hap_idxs_in;
-  p.quad_out = a->hap_idxs_out;
-  p.props = a->props;
-  p.tr_slot = a->trace_slot;
-  p.tr_u = a->trace_accept;
-  p.tr_work = a->trace_work;
-  p.like_out = a->like_out;
-  p.eval_trace = a->eval_trace;
-  p.accept_trace = a->accept_trace;
-  p.beta = c->d_beta;
-  p.counter = c->d_counter;
-  p.stats = c->d_stats;
-  p.error = c->d_error;
-  std::memcpy(p.pc, c->pc, sizeof(p.pc));
-  p.pen = a->pen;
-  p.seed = a->seed;
-  p.generation = a->generation;
-  p.do_work = work ? 1u : 0u;
-  p.nbr = a->neighbors;
-  p.klen = a->neighbors_per_sample;
-  p.samp_lo = lo;
-  p.samp_hi = hi;
-
-  const uint32_t P = choose_lanes(c, N);
-  KernelFn fn = kernel_for(P, vq);
+template <class Fn>
+unsigned grid_for(glp_ctx *c, Fn fn, uint64_t samples, uint32_t P, int *rc) {
   int occ = 0;
-  GLP_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, 0));
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, 0);
+  if (e != cudaSuccess) {
+    *rc = fail(c, GLP_ERR_CUDA, "occupancy query failed: %s", cudaGetErrorString(e));
+    return 0;
+  }
   occ = std::max(occ, 1);
   const uint64_t groups_per_block = (uint64_t)glp::kThreads / P;
-  const uint64_t want_blocks = ((uint64_t)N + groups_per_block - 1) / groups_per_block;
-  const uint64_t max_blocks = (uint64_t)occ * c->sms;
-  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(want_blocks, max_blocks));
+  const uint64_t want = (samples + groups_per_block - 1) / groups_per_block;
+  const uint64_t cap = (uint64_t)occ * c->sms;
+  *rc = GLP_OK;
+  return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
+}
 
+int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
+  glp::GenParams p;
+  int rc = make_params(c, pb, a, &p);
+  if (rc)
+    return rc;
+  const bool vq = (a->flags & GLP_GEN_VQ) != 0;
+  const uint32_t P = choose_lanes(c, a->num_samples);
+  SingleFn fn = single_kernel(P, vq);
+  const unsigned grid = grid_for(c, fn, a->num_samples, P, &rc);
+  if (rc)
+    return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
   fn<<<grid, glp::kThreads, 0, c->stream>>>(p);
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
-  c->last_N = N;
-  c->last_C = C;
+  c->last_chain_cycles = (uint64_t)a->num_samples * a->num_cycles;
   return GLP_OK;
-}
-
-// 8 independent FMA chains per thread, 4 per loop trip kept live by a
-// dependency through the loop counter; the result is stored so nothing is
-// eliminated.
-__global__ void __launch_bounds__(256) fp32_probe_kernel(float *out, int iters, float a,
-                                                         float b) {
-  float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1e-7f, x2 = x0 + 2e-7f, x3 = x0 + 3e-7f;
-  float x4 = x0 + 4e-7f, x5 = x0 + 5e-7f, x6 = x0 + 6e-7f, x7 = x0 + 7e-7f;
-#pragma unroll 4
-  for (int i = 0; i < iters; ++i) {
-    x0 = fmaf(x0, a, b);
-    x1 = fmaf(x1, a, b);
-    x2 = fmaf(x2, a, b);
-    x3 = fmaf(x3, a, b);
-    x4 = fmaf(x4, a, b);
-    x5 = fmaf(x5, a, b);
-    x6 = fmaf(x6, a, b);
-    x7 = fmaf(x7, a, b);
-  }
-  out[blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
 }
 
 }  // namespace
 
 extern "C" {
-
-int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, uint32_t k,
-                      double lb, double ub, int use_maf, uint32_t *neighbors) {
-  int rc = check_ctx(c);
-  if (rc)
-    return rc;
-  if (!haps || !neighbors || S == 0 || k == 0)
-    return fail(c, GLP_ERR_ARG, "haps, neighbors, num_sites and k are required");
-  const uint32_t half = (k + 1) / 2;
-  if (H < 4 || (H & 1u) || H > glp::kKnnMaxHaps)
-    return fail(c, GLP_ERR_ARG, "num_haps=%u must be even and in [4, %u]", H,
-                glp::kKnnMaxHaps);
-  if (2 * half > H - 2 || half > glp::kKnnMaxHalf)
-    return fail(c, GLP_ERR_ARG, "k=%u needs 2*ceil(k/2) <= num_haps-2 and <= %u", k,
-                2 * glp::kKnnMaxHalf);
-  if (S >= 0xffffu)
-    return fail(c, GLP_ERR_ARG, "num_sites must be below 65535 for kNN");
-  const uint32_t wn = (S + 63) / 64;
-  if ((rc = ensure(c, c->d_mask, c->mask_cap, wn)))
-    return rc;
-  glp::common_sites_kernel<<<wn, 64, 0, c->stream>>>(haps, H, wn, S, lb, ub, use_maf,
-                                                     c->d_mask);
-  GLP_CUDA(c, cudaGetLastError());
-  const size_t smem = glp::knn_smem_bytes(H);
-  GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-  glp::knn_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask, half,
-                                                                 S, neighbors);
-  GLP_CUDA(c, cudaGetLastError());
-  return GLP_OK;
-}
-
-int glp_measure_fp32_peak(glp_ctx *c, float ms_target, double *tflops) {
-  int rc = check_ctx(c);
-  if (rc)
-    return rc;
-  if (!tflops || !(ms_target > 0))
-    return fail(c, GLP_ERR_ARG, "tflops must be non-null and ms_target positive");
-  const int threads = 256, blocks = c->sms * 8;
-  float *out = nullptr;
-  GLP_CUDA(c, cudaMalloc((void **)&out, sizeof(float) * threads * blocks));
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  int iters = 1 << 14;
-  double best = 0;
-  for (int rep = 0; rep < 6; ++rep) {
-    cudaEventRecord(e0, c->stream);
-    fp32_probe_kernel<<<blocks, threads, 0, c->stream>>>(out, iters, 0.999999f, 1e-7f);
-    cudaEventRecord(e1, c->stream);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
-    if (rep >= 2)
-      best = std::max(best, flops / (ms * 1e-3) / 1e12);
-    if (ms > 0 && ms < ms_target)
-      iters = (int)std::min<double>(iters * (ms_target / ms), 1 << 26);
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaFree(out);
-  GLP_CUDA(c, cudaGetLastError());
-  *tflops = best;
-  return GLP_OK;
-}
-
 
 int glp_check_device(int device, int *device_count, int *cc_major, int *cc_minor,
                      int *sm_count) {
@@ -419,6 +459,7 @@ int glp_create(int device, glp_ctx **out) {
     return GLP_ERR_ARG;
   glp_ctx *c = new glp_ctx();
   c->device = device;
+  c->def.ctx = c;
   int rc = check_ctx(c);
   if (rc) {
     delete c;
@@ -446,28 +487,29 @@ void glp_destroy(glp_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream)
     cudaStreamSynchronize(c->stream);
-  release(c->d_tran4);
-  release(c->d_vq);
-  release(c->d_packed);
-  release(c->d_emit);
-  release(c->d_prob);
+  release_problem(&c->def);
   release(c->d_counter);
   release(c->d_stats);
   release(c->d_error);
-  release(c->d_beta);
+  release(c->d_table);
+  release(c->d_offsets);
+  if (c->h_table)
+    cudaFreeHost(c->h_table);
+  if (c->h_offsets)
+    cudaFreeHost(c->h_offsets);
   release(c->d_haps);
   release(c->d_hnew);
   release(c->d_quad);
   release(c->d_quad_out);
   release(c->d_props);
+  release(c->d_nbr);
+  release(c->d_mask);
   release(c->d_tr_slot);
   release(c->d_acc);
   release(c->d_tr_u);
   release(c->d_like);
   release(c->d_evals);
   release(c->d_tr_work);
-  release(c->d_nbr);
-  release(c->d_mask);
   if (c->own_stream)
     cudaStreamDestroy(c->own_stream);
   delete c;
@@ -488,80 +530,72 @@ int glp_set_stream(glp_ctx *c, void *stream) {
 
 int glp_set_tran(glp_ctx *c, const float *tran, uint32_t S) {
   int rc = check_ctx(c);
-  if (rc)
-    return rc;
-  if (!tran || S == 0)
-    return fail(c, GLP_ERR_ARG, "tran must be non-null with num_sites > 0");
-  std::vector<float4> t4(S);
-  t4[0] = make_float4(1.f, 0.f, 0.f, 0.f);  // row 0 is unused by the recursion
-  for (uint32_t m = 1; m < S; ++m)
-    t4[m] = make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2], 0.f);
-  if (c->S != S) {
-    release(c->d_tran4);
-    GLP_CUDA(c, cudaMalloc((void **)&c->d_tran4, sizeof(float4) * S));
-    c->S = S;
-  }
-  GLP_CUDA(c, cudaMemcpy(c->d_tran4, t4.data(), sizeof(float4) * S, cudaMemcpyHostToDevice));
-  return GLP_OK;
+  return rc ? rc : set_tran(&c->def, tran, S);
 }
 
 int glp_set_mutation_mat(glp_ctx *c, const float *pc16) {
   int rc = check_ctx(c);
-  if (rc)
-    return rc;
-  if (!pc16)
-    return fail(c, GLP_ERR_ARG, "pc must be non-null");
-  std::memcpy(c->pc, pc16, sizeof(c->pc));
-  c->have_pc = true;
-  return upload_vq_table(c);
+  return rc ? rc : set_pc(&c->def, pc16);
 }
 
 int glp_set_codebook(glp_ctx *c, const float *codebook, uint32_t entries) {
   int rc = check_ctx(c);
-  if (rc)
-    return rc;
-  if (!codebook || entries != 16)
-    return fail(c, GLP_ERR_ARG, "codebook must hold 16 (RR, Het) entries, got %u", entries);
-  std::memcpy(c->codebook, codebook, sizeof(c->codebook));
-  c->have_codebook = true;
-  return upload_vq_table(c);
+  return rc ? rc : set_codebook(&c->def, codebook, entries);
 }
 
 int glp_set_packed_gls(glp_ctx *c, const uint32_t *packed, size_t n) {
   int rc = check_ctx(c);
-  if (rc)
-    return rc;
-  if (!packed || n == 0)
-    return fail(c, GLP_ERR_ARG, "packed GLs must be non-empty");
-  if (n != c->packed_words) {
-    release(c->d_packed);
-    c->packed_words = 0;
-    GLP_CUDA(c, cudaMalloc((void **)&c->d_packed, sizeof(uint32_t) * n));
-    c->packed_words = n;
-  }
-  GLP_CUDA(c, cudaMemcpy(c->d_packed, packed, sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
-  return GLP_OK;
+  return rc ? rc : set_packed(&c->def, packed, n);
 }
 
 int glp_set_emission(glp_ctx *c, const float *emit, const float *prob, uint32_t N, uint32_t S) {
   int rc = check_ctx(c);
+  return rc ? rc : set_emission(&c->def, emit, prob, N, S);
+}
+
+int glp_problem_create(glp_ctx *c, glp_problem **out) {
+  int rc = check_ctx(c);
   if (rc)
     return rc;
-  if (!emit || N == 0 || S == 0)
-    return fail(c, GLP_ERR_ARG, "emit must be non-null with positive N and S");
-  const size_t ns = (size_t)N * S;
-  if (c->eN != N || c->eS != S) {
-    release(c->d_emit);
-    release(c->d_prob);
-    c->eN = c->eS = 0;
-    GLP_CUDA(c, cudaMalloc((void **)&c->d_emit, sizeof(float4) * ns));
-    GLP_CUDA(c, cudaMalloc((void **)&c->d_prob, sizeof(float) * 3 * ns));
-    c->eN = N;
-    c->eS = S;
+  if (!out)
+    return fail(c, GLP_ERR_ARG, "out must be non-null");
+  glp_problem *pb = new glp_problem();
+  pb->ctx = c;
+  *out = pb;
+  return GLP_OK;
+}
+
+void glp_problem_destroy(glp_problem *pb) {
+  if (!pb)
+    return;
+  if (pb->ctx) {
+    cudaSetDevice(pb->ctx->device);
+    if (pb->ctx->stream)
+      cudaStreamSynchronize(pb->ctx->stream);
   }
-  GLP_CUDA(c, cudaMemcpy(c->d_emit, emit, sizeof(float4) * ns, cudaMemcpyHostToDevice));
-  if (prob)
-    GLP_CUDA(c, cudaMemcpy(c->d_prob, prob, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice));
+  release_problem(pb);
+  delete pb;
+}
+
+int glp_problem_set_model(glp_problem *pb, const float *tran, const float *pc16,
+                          const float *emit, const float *prob, uint32_t num_samples,
+                          uint32_t num_sites) {
+  if (!pb || !pb->ctx)
+    return GLP_ERR_ARG;
+  int rc = check_ctx(pb->ctx);
+  if (rc || (rc = set_tran(pb, tran, num_sites)) || (rc = set_pc(pb, pc16)) ||
+      (rc = set_emission(pb, emit, prob, num_samples, num_sites)))
+    return rc;
+  return GLP_OK;
+}
+
+int glp_problem_set_vq(glp_problem *pb, const uint32_t *packed, size_t num_words,
+                       const float *codebook) {
+  if (!pb || !pb->ctx)
+    return GLP_ERR_ARG;
+  int rc = check_ctx(pb->ctx);
+  if (rc || (rc = set_codebook(pb, codebook, 16)) || (rc = set_packed(pb, packed, num_words)))
+    return rc;
   return GLP_OK;
 }
 
@@ -571,7 +605,73 @@ int glp_run_generation(glp_ctx *c, const glp_generation_args *a) {
     return rc;
   if (!a)
     return fail(c, GLP_ERR_ARG, "args must be non-null");
-  return launch_generation(c, a);
+  return launch_single(c, &c->def, a);
+}
+
+int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
+                  const glp_generation_args *args) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (count == 0 || !problems || !args)
+    return fail(c, GLP_ERR_ARG, "a batch needs count > 0, problems and args");
+  const bool vq = (args[0].flags & GLP_GEN_VQ) != 0;
+  if (count > c->h_cap) {
+    if (c->h_table)
+      cudaFreeHost(c->h_table);
+    if (c->h_offsets)
+      cudaFreeHost(c->h_offsets);
+    c->h_table = nullptr;
+    c->h_offsets = nullptr;
+    c->h_cap = 0;
+    GLP_CUDA(c, cudaMallocHost((void **)&c->h_table, sizeof(glp::GenParams) * count));
+    GLP_CUDA(c, cudaMallocHost((void **)&c->h_offsets, sizeof(uint32_t) * (count + 1)));
+    c->h_cap = count;
+  }
+  // the staging buffers are reused: wait for the previous batch's upload
+  GLP_CUDA(c, cudaStreamSynchronize(c->stream));
+  uint64_t total = 0, chain_cycles = 0;
+  c->h_offsets[0] = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    glp_problem *pb = problems[i];
+    if (!pb || pb->ctx != c)
+      return fail(c, GLP_ERR_ARG, "problem %u does not belong to this context", i);
+    if (((args[i].flags & GLP_GEN_VQ) != 0) != vq)
+      return fail(c, GLP_ERR_ARG, "all chunks of a batch must use the same emission source");
+    if ((rc = make_params(c, pb, &args[i], &c->h_table[i])))
+      return rc;
+    total += args[i].num_samples;
+    chain_cycles += (uint64_t)args[i].num_samples * args[i].num_cycles;
+    if (total > 0xffffffffull)
+      return fail(c, GLP_ERR_ARG, "a batch holds at most 2^32-1 samples");
+    c->h_offsets[i + 1] = (uint32_t)total;
+  }
+  if ((rc = ensure(c, c->d_table, c->table_cap, count)) ||
+      (rc = ensure(c, c->d_offsets, c->offsets_cap, (size_t)count + 1)))
+    return rc;
+  GLP_CUDA(c, cudaMemcpyAsync(c->d_table, c->h_table, sizeof(glp::GenParams) * count,
+                              cudaMemcpyHostToDevice, c->stream));
+  GLP_CUDA(c, cudaMemcpyAsync(c->d_offsets, c->h_offsets, sizeof(uint32_t) * (count + 1),
+                              cudaMemcpyHostToDevice, c->stream));
+  glp::MultiParams mp;
+  mp.chunks = c->d_table;
+  mp.offsets = c->d_offsets;
+  mp.nchunks = count;
+  mp.counter = c->d_counter;
+  mp.stats = c->d_stats;
+  mp.error = c->d_error;
+  const uint32_t P = choose_lanes(c, total);
+  MultiFn fn = multi_kernel(P, vq);
+  const unsigned grid = grid_for(c, fn, total, P, &rc);
+  if (rc)
+    return rc;
+  GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
+  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
+  fn<<<grid, glp::kThreads, 0, c->stream>>>(mp);
+  GLP_CUDA(c, cudaGetLastError());
+  c->lanes_used = P;
+  c->last_chain_cycles = chain_cycles;
+  return GLP_OK;
 }
 
 int glp_finish(glp_ctx *c) {
@@ -584,8 +684,8 @@ int glp_finish(glp_ctx *c) {
   GLP_CUDA(c, cudaMemcpy(&h_err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost));
   GLP_CUDA(c, cudaMemcpy(c->last_stats, c->d_stats, sizeof(c->last_stats),
                          cudaMemcpyDeviceToHost));
-  if (c->last_N && c->last_C)
-    c->last_accept = (double)c->last_stats[2] / ((double)c->last_N * c->last_C);
+  if (c->last_chain_cycles)
+    c->last_accept = (double)c->last_stats[2] / (double)c->last_chain_cycles;
   if (h_err) {
     GLP_CUDA(c, cudaMemset(c->d_error, 0, sizeof(int)));
     return fail(c, GLP_ERR_INDEX, "a haplotype index >= num_haps reached the device");
@@ -670,7 +770,7 @@ int glp_run_generation_host(glp_ctx *c, const glp_generation_args *a) {
       return rc;
     d.accept_trace = c->d_acc;
   }
-  if ((rc = launch_generation(c, &d)))
+  if ((rc = launch_single(c, &c->def, &d)))
     return rc;
   GLP_CUDA(c, cudaMemcpyAsync(a->hap_idxs_out, c->d_quad_out, (size_t)16 * N,
                               cudaMemcpyDeviceToHost, st));
@@ -698,7 +798,7 @@ int glp_run_hmm_on_device(glp_ctx *c, const uint64_t *hap_panel, size_t panel_wo
     return rc;
   if (!hap_panel || !hap_idxs || (num_cycles && !extra_prop_haps))
     return fail(c, GLP_ERR_ARG, "hap_panel, extra_prop_haps and hap_idxs are required");
-  const size_t wn = (num_sites + 63) / 64;
+  const size_t wn = ((size_t)num_sites + 63) / 64;
   if (wn == 0 || panel_words % wn)
     return fail(c, GLP_ERR_ARG, "panel of %zu words is not a whole number of %zu-word haps",
                 panel_words, wn);
@@ -748,4 +848,94 @@ int glp_get_stats(glp_ctx *c, uint64_t *evaluations, uint64_t *rounds, uint32_t 
   return GLP_OK;
 }
 
+int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, uint32_t k,
+                      double lb, double ub, int use_maf, uint32_t *neighbors) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!haps || !neighbors || S == 0 || k == 0)
+    return fail(c, GLP_ERR_ARG, "haps, neighbors, num_sites and k are required");
+  const uint32_t half = (k + 1) / 2;
+  if (H < 4 || (H & 1u) || H > glp::kKnnMaxHaps)
+    return fail(c, GLP_ERR_ARG, "num_haps=%u must be even and in [4, %u]", H,
+                glp::kKnnMaxHaps);
+  if (2 * half > H - 2 || half > glp::kKnnMaxHalf)
+    return fail(c, GLP_ERR_ARG, "k=%u needs 2*ceil(k/2) <= num_haps-2 and <= %u", k,
+                2 * glp::kKnnMaxHalf);
+  if (S >= 0xffffu)
+    return fail(c, GLP_ERR_ARG, "num_sites must be below 65535 for kNN");
+  const uint32_t wn = (S + 63) / 64;
+  if ((rc = ensure(c, c->d_mask, c->mask_cap, wn)))
+    return rc;
+  glp::common_sites_kernel<<<wn, 64, 0, c->stream>>>(haps, H, wn, S, lb, ub, use_maf,
+                                                     c->d_mask);
+  GLP_CUDA(c, cudaGetLastError());
+  const size_t smem = glp::knn_smem_bytes(H);
+  GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  glp::knn_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask, half,
+                                                                 S, neighbors);
+  GLP_CUDA(c, cudaGetLastError());
+  return GLP_OK;
+}
+
 }  // extern "C"
+
+namespace {
+
+// 8 independent FMA chains per thread; the result is stored so nothing is
+// eliminated.
+__global__ void __launch_bounds__(256) fp32_probe_kernel(float *out, int iters, float a,
+                                                         float b) {
+  float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1e-7f, x2 = x0 + 2e-7f, x3 = x0 + 3e-7f;
+  float x4 = x0 + 4e-7f, x5 = x0 + 5e-7f, x6 = x0 + 6e-7f, x7 = x0 + 7e-7f;
+#pragma unroll 4
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b);
+    x1 = fmaf(x1, a, b);
+    x2 = fmaf(x2, a, b);
+    x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b);
+    x5 = fmaf(x5, a, b);
+    x6 = fmaf(x6, a, b);
+    x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+}
+
+}  // namespace
+
+extern "C" int glp_measure_fp32_peak(glp_ctx *c, float ms_target, double *tflops) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!tflops || !(ms_target > 0))
+    return fail(c, GLP_ERR_ARG, "tflops must be non-null and ms_target positive");
+  const int threads = 256, blocks = c->sms * 8;
+  float *out = nullptr;
+  GLP_CUDA(c, cudaMalloc((void **)&out, sizeof(float) * threads * blocks));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int iters = 1 << 14;
+  double best = 0;
+  for (int rep = 0; rep < 6; ++rep) {
+    cudaEventRecord(e0, c->stream);
+    fp32_probe_kernel<<<blocks, threads, 0, c->stream>>>(out, iters, 0.999999f, 1e-7f);
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+    if (rep >= 2)
+      best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    if (ms > 0 && ms < ms_target)
+      iters = (int)std::min<double>(iters * (ms_target / ms), 1 << 26);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  GLP_CUDA(c, cudaGetLastError());
+  *tflops = best;
+  return GLP_OK;
+}

@@ -86,39 +86,43 @@ struct GenParams {
 // Emission sources.  Both hand out the 4 emission values of a site,
 // e[(father_bit << 1) | mother_bit] (impute.cpp:338-342).
 
+// Sites are consumed in blocks of 8 (m0 a multiple of 8): prep8(m0) readies
+// a block, get8(m0, j) returns site m0 + j for a compile-time j; get1(m) is
+// the unblocked form used on ragged tails.
 struct EmitF32 {
   const float4 *row;
   __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *) {
     row = p.emit + (size_t)s * p.S;
   }
-  __device__ __forceinline__ void prep(const GenParams &, uint32_t) {}
-  __device__ __forceinline__ float4 get(uint32_t m) const { return __ldg(row + m); }
+  __device__ __forceinline__ void prep8(uint32_t) {}
+  __device__ __forceinline__ float4 get8(uint32_t m0, uint32_t j) const {
+    return __ldg(row + m0 + j);
+  }
+  __device__ __forceinline__ float4 get1(uint32_t m) const { return __ldg(row + m); }
 };
 
 // 4-bit VQ codes, eight per uint32, most significant nibble first
-// (glPack.cpp:104-109, hmmLike.cu:20-24); table[c] = FillEmit(decode(c)).
+// (glPack.cpp:104-109, hmmLike.cu:20-24), so one block of 8 sites is one
+// word; table[c] = FillEmit(decode(c)) computed once on the host.
 struct EmitVQ {
   const uint32_t *col;
   const float4 *table;
-  uint32_t stride, nblk;
-  uint32_t pk[8];
+  uint32_t stride;
+  uint32_t pk;
   __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *tab) {
     col = p.packed + s;
     stride = p.N;
-    nblk = (p.S + 7) >> 3;
     table = tab;
   }
-  __device__ __forceinline__ void prep(const GenParams &, uint32_t w) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const uint32_t b = w * 8 + i;
-      pk[i] = b < nblk ? __ldg(col + (size_t)b * stride) : 0u;
-    }
+  __device__ __forceinline__ void prep8(uint32_t m0) {
+    pk = __ldg(col + (size_t)(m0 >> 3) * stride);
   }
-  __device__ __forceinline__ float4 get(uint32_t m) const {
-    const uint32_t j = m & 63u;
-    const uint32_t code = (pk[j >> 3] >> (28u - 4u * (j & 7u))) & 15u;
-    return table[code];
+  __device__ __forceinline__ float4 get8(uint32_t, uint32_t j) const {
+    return table[(pk >> (28u - 4u * j)) & 15u];
+  }
+  __device__ __forceinline__ float4 get1(uint32_t m) const {
+    const uint32_t w = __ldg(col + (size_t)(m >> 3) * stride);
+    return table[(w >> (28u - 4u * (m & 7u))) & 15u];
   }
 };
 
@@ -223,25 +227,61 @@ __device__ __forceinline__ Parents load_parents(const uint64_t *haps, uint32_t w
   return r;
 }
 
+// 8-bit windows of the four parent words for one block of 8 sites.
+struct Bits8 {
+  uint32_t f0, f1, m0, m1;
+};
+
+__device__ __forceinline__ Bits8 window8(const Parents &pw, uint32_t shift) {
+  Bits8 r;
+  r.f0 = (uint32_t)(pw.f0 >> shift);
+  r.f1 = (uint32_t)(pw.f1 >> shift);
+  r.m0 = (uint32_t)(pw.m0 >> shift);
+  r.m1 = (uint32_t)(pw.m1 >> shift);
+  return r;
+}
+
+__device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, uint32_t j,
+                                              float &s00, float &s01, float &s10,
+                                              float &s11) {
+  select4(e, (bw.f0 >> j) & 1u, (bw.f1 >> j) & 1u, (bw.m0 >> j) & 1u, (bw.m1 >> j) & 1u,
+          s00, s01, s10, s11);
+}
+
+// Forward over the 8 sites m0..m0+7 and backward over n0+7..n0 (both blocks
+// full), interleaved: 8 independent FMA chains per lane.
 template <class E>
-__device__ __forceinline__ void fwd_site(FState &f, const E &em, const float4 *tran4,
-                                         const Parents &pw, uint32_t m, uint32_t j) {
-  float s00, s01, s10, s11;
-  select4(em.get(m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
-          (pw.m1 >> j) & 1, s00, s01, s10, s11);
-  fwd_step(f, __ldg(tran4 + m), s00, s01, s10, s11);
+__device__ __forceinline__ void both_block8(FState &f, BState &b, const E &ef, const E &eb,
+                                            const float4 *tran4, const Bits8 &wf,
+                                            const Bits8 &wb, uint32_t m0, uint32_t n0) {
+#pragma unroll
+  for (uint32_t j = 0; j < 8; ++j) {
+    float s00, s01, s10, s11, r00, r01, r10, r11;
+    site_emission(ef.get8(m0, j), wf, j, s00, s01, s10, s11);
+    site_emission(eb.get8(n0, 7 - j), wb, 7 - j, r00, r01, r10, r11);
+    const float4 tf = __ldg(tran4 + m0 + j), tb = __ldg(tran4 + n0 + 7 - j);
+    fwd_step(f, tf, s00, s01, s10, s11);
+    bwd_step(b, tb, r00, r01, r10, r11);
+  }
 }
 
 template <class E>
-__device__ __forceinline__ void bwd_site(BState &b, const E &em, const float4 *tran4,
-                                         const Parents &pw, uint32_t m, uint32_t j) {
-  float s00, s01, s10, s11;
-  select4(em.get(m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
-          (pw.m1 >> j) & 1, s00, s01, s10, s11);
-  bwd_step(b, __ldg(tran4 + m), s00, s01, s10, s11);
+__device__ __forceinline__ void fwd_block8(FState &f, const E &ef, const float4 *tran4,
+                                           const Bits8 &wf, uint32_t m0) {
+#pragma unroll
+  for (uint32_t j = 0; j < 8; ++j) {
+    float s00, s01, s10, s11;
+    site_emission(ef.get8(m0, j), wf, j, s00, s01, s10, s11);
+    fwd_step(f, __ldg(tran4 + m0 + j), s00, s01, s10, s11);
+  }
 }
 
 // Log-likelihood of one quadruple (natural log), binary64.
+//
+// Words [0, wf) run forward and words [wf, wn) backward, two at a time in
+// one instruction stream; a ragged last word (S % 64 != 0) runs backward
+// alone, site by site, before the rest.  With wn == 1 the single word runs
+// forward, site by site.
 template <class E>
 __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, uint4 q) {
   const uint32_t S = p.S, wn = p.wn;
@@ -255,20 +295,27 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
   b.k = 0;
   E ef = em0, eb = em0;
   if (wn == 1) {
-    ef.prep(p, 0);
     const Parents pw = load_parents(p.haps, wn, q, 0);
 #pragma unroll 1
-    for (uint32_t m = 0; m < S; ++m)
-      fwd_site(f, ef, tran4, pw, m, m);
+    for (uint32_t m = 0; m < S; ++m) {
+      float s00, s01, s10, s11;
+      select4(ef.get1(m), (pw.f0 >> m) & 1, (pw.f1 >> m) & 1, (pw.m0 >> m) & 1,
+              (pw.m1 >> m) & 1, s00, s01, s10, s11);
+      fwd_step(f, __ldg(tran4 + m), s00, s01, s10, s11);
+    }
   } else {
     const uint32_t wf = (wn + 1) >> 1;
     uint32_t wb = wn - 1;
     if (S & 63u) {
-      eb.prep(p, wb);
       const Parents pw = load_parents(p.haps, wn, q, wb);
 #pragma unroll 1
-      for (int m = (int)S - 1; m >= (int)(wb * 64); --m)
-        bwd_site(b, eb, tran4, pw, (uint32_t)m, (uint32_t)m & 63u);
+      for (int m = (int)S - 1; m >= (int)(wb * 64); --m) {
+        const uint32_t j = (uint32_t)m & 63u;
+        float s00, s01, s10, s11;
+        select4(eb.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
+                (pw.m1 >> j) & 1, s00, s01, s10, s11);
+        bwd_step(b, __ldg(tran4 + m), s00, s01, s10, s11);
+      }
       bwd_guard(b);
       --wb;
     }
@@ -276,27 +323,28 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
 #pragma unroll 1
     for (uint32_t i = 0; i < nb; ++i) {
       const uint32_t wfw = i, wbw = wb - i;
-      ef.prep(p, wfw);
-      eb.prep(p, wbw);
       const Parents pf = load_parents(p.haps, wn, q, wfw);
       const Parents pb = load_parents(p.haps, wn, q, wbw);
-      const uint32_t mf = wfw * 64, mb = wbw * 64 + 63;
-#pragma unroll
-      for (uint32_t j = 0; j < 64; ++j) {
-        fwd_site(f, ef, tran4, pf, mf + j, j);
-        bwd_site(b, eb, tran4, pb, mb - j, 63 - j);
+#pragma unroll 1
+      for (uint32_t blk = 0; blk < 8; ++blk) {
+        const uint32_t m0 = wfw * 64 + blk * 8, n0 = wbw * 64 + (7 - blk) * 8;
+        ef.prep8(m0);
+        eb.prep8(n0);
+        both_block8(f, b, ef, eb, tran4, window8(pf, blk * 8), window8(pb, (7 - blk) * 8), m0,
+                    n0);
       }
       fwd_guard(f);
       bwd_guard(b);
     }
 #pragma unroll 1
     for (uint32_t i = nb; i < wf; ++i) {
-      ef.prep(p, i);
       const Parents pf = load_parents(p.haps, wn, q, i);
-      const uint32_t mf = i * 64;
-#pragma unroll
-      for (uint32_t j = 0; j < 64; ++j)
-        fwd_site(f, ef, tran4, pf, mf + j, j);
+#pragma unroll 1
+      for (uint32_t blk = 0; blk < 8; ++blk) {
+        const uint32_t m0 = i * 64 + blk * 8;
+        ef.prep8(m0);
+        fwd_block8(f, ef, tran4, window8(pf, blk * 8), m0);
+      }
       fwd_guard(f);
     }
   }
@@ -442,15 +490,12 @@ __device__ void hmm_work_lane(const GenParams &p, const float *pc, uint32_t s, u
 }
 
 // ---------------------------------------------------------------------------
-// The generation kernel.
+// The generation kernels.
 
 struct Pending {
-  uint32_t s, q0, q1, q2, q3;
+  uint32_t c, s, q0, q1, q2, q3;
 };
 
-__device__ __forceinline__ uint32_t get_slot(const uint4 &q, uint32_t r) {
-  return r == 0 ? q.x : (r == 1 ? q.y : (r == 2 ? q.z : q.w));
-}
 __device__ __forceinline__ void set_slot(uint4 &q, uint32_t r, uint32_t v) {
   if (r == 0)
     q.x = v;
@@ -462,27 +507,64 @@ __device__ __forceinline__ void set_slot(uint4 &q, uint32_t r, uint32_t v) {
     q.w = v;
 }
 
-template <int P, class E>
-__global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p) {
+// Work sources.  One chunk: the kernel parameter.  Many chunks: a descriptor
+// table in global memory; the samples of all chunks form one queue, chunk by
+// chunk, so a group's neighbours in the queue usually share its chunk.
+struct OneChunk {
+  static constexpr bool kMulti = false;
+  const GenParams &p;
+  __device__ __forceinline__ uint32_t total() const { return p.N; }
+  __device__ __forceinline__ const GenParams &chunk(uint32_t) const { return p; }
+  __device__ __forceinline__ void locate(uint32_t g, uint32_t &c, uint32_t &s) const {
+    c = 0;
+    s = g;
+  }
+};
+
+struct MultiParams {
+  const GenParams *chunks;   // [nchunks]
+  const uint32_t *offsets;   // [nchunks + 1] prefix sums of the chunks' N
+  uint32_t nchunks;
+  uint32_t *counter;
+  unsigned long long *stats;
+  int *error;
+};
+
+struct ManyChunks {
+  static constexpr bool kMulti = true;
+  const MultiParams &mp;
+  __device__ __forceinline__ uint32_t total() const { return __ldg(mp.offsets + mp.nchunks); }
+  __device__ __forceinline__ const GenParams &chunk(uint32_t c) const { return mp.chunks[c]; }
+  __device__ __forceinline__ void locate(uint32_t g, uint32_t &c, uint32_t &s) const {
+    uint32_t lo = 0, hi = mp.nchunks;  // largest c with offsets[c] <= g
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(mp.offsets + mid) <= g)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    c = lo;
+    s = g - __ldg(mp.offsets + lo);
+  }
+};
+
+template <int P, class E, class Src>
+__device__ __forceinline__ void generation_body(const Src &src, uint32_t *counter,
+                                                unsigned long long *stats, int *error,
+                                                const float4 *vq_smem, const float *pc_smem) {
   static_assert(P == 1 || P == 2 || P == 4 || P == 8 || P == 16 || P == 32, "P");
   constexpr unsigned FULL = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t li = lane % P, gbase = lane - li;
-  __shared__ float4 s_vq[16];
-  __shared__ float s_pc[16];
   __shared__ Pending s_pend[kWarps][64];
   __shared__ uint32_t s_npend[kWarps];
-  if (threadIdx.x < 16) {
-    s_pc[threadIdx.x] = p.pc[threadIdx.x];
-    if (p.vq_table)
-      s_vq[threadIdx.x] = p.vq_table[threadIdx.x];
-  }
   if (lane == 0)
     s_npend[warp] = 0;
-  __syncthreads();
+  __syncwarp();
 
-  const uint32_t N = p.N, C = p.C, H = p.H;
-  uint32_t s = kNone, e = 0;
+  const uint32_t total = src.total();
+  uint32_t c = 0, s = kNone, e = 0;
   uint4 q = make_uint4(0, 0, 0, 0);
   double curr = 0.0;
   bool exhausted = false;
@@ -493,12 +575,14 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
     const bool need = (s == kNone) && !exhausted;
     uint32_t ns = 0;
     if (need && li == 0)
-      ns = atomicAdd(p.counter, 1u);
+      ns = atomicAdd(counter, 1u);
     ns = __shfl_sync(FULL, ns, gbase);
     if (need) {
-      if (ns < N) {
-        s = ns;
+      if (ns < total) {
+        src.locate(ns, c, s);
         e = 0;
+        const GenParams &p = src.chunk(c);
+        const uint32_t N = p.N;
         if (p.quad_in) {
           q = make_uint4(__ldg(p.quad_in + s), __ldg(p.quad_in + N + s),
                          __ldg(p.quad_in + 2 * (size_t)N + s),
@@ -515,8 +599,9 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
           q.w = glp_surrogate(p.seed, p.generation, s, 3, GLP_TAG_INIT, p.samp_lo, p.samp_hi,
                               p.nbr, p.klen);
         }
+        const uint32_t H = p.H;
         if (q.x >= H || q.y >= H || q.z >= H || q.w >= H) {
-          atomicOr(p.error, 1);
+          atomicOr(error, 1);
           q = make_uint4(0, 0, 0, 0);
         }
       } else {
@@ -527,6 +612,8 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
     if (!__any_sync(FULL, active))
       break;
 
+    const GenParams &p = src.chunk(c);
+    const uint32_t N = p.N, C = p.C, H = p.H;
     // one speculative round: lane li scores evaluation e + li
     const uint32_t k = active ? min((uint32_t)P, C + 1 - e) : 0u;
     const uint32_t ev = e + li;
@@ -546,7 +633,7 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
                      : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP, p.samp_lo,
                                      p.samp_hi, p.nbr, p.klen);
       if (phap >= H) {
-        atomicOr(p.error, 1);
+        atomicOr(error, 1);
         phap = 0;
       }
       set_slot(myq, slot, phap);
@@ -554,7 +641,7 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
     double L = 0.0;
     if (on) {
       E em;
-      em.init(p, s, s_vq);
+      em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
       L = eval_like<E>(p, em, myq);
     }
     // The accept rule of MHSampler.hpp:86-93 in chain order.  Every
@@ -570,10 +657,10 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
     const unsigned gmask = (P == 32) ? FULL : (((1u << P) - 1u) << gbase);
     const unsigned abal = __ballot_sync(FULL, acc) & gmask;
     const uint32_t first_acc = abal ? (uint32_t)(__ffs(abal) - 1) - gbase : (uint32_t)P;
-    const uint32_t src = gbase + (abal ? first_acc : 0u);
-    const double La = __shfl_sync(FULL, L, src);
-    const uint32_t sla = __shfl_sync(FULL, slot, src);
-    const uint32_t pha = __shfl_sync(FULL, phap, src);
+    const uint32_t srcl = gbase + (abal ? first_acc : 0u);
+    const double La = __shfl_sync(FULL, L, srcl);
+    const uint32_t sla = __shfl_sync(FULL, slot, srcl);
+    const uint32_t pha = __shfl_sync(FULL, phap, srcl);
     if (active) {
       curr = curr0;
       if (abal) {
@@ -607,25 +694,26 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
       if (p.like_out)
         p.like_out[s] = curr;
     }
-    const unsigned dmask = __ballot_sync(FULL, done && li == 0);
-    if (dmask && !p.do_work) {
-      if (done)
-        s = kNone;
-    } else if (dmask) {
+    const bool queue = done && li == 0 && p.do_work;
+    const unsigned dmask = __ballot_sync(FULL, queue);
+    const uint32_t s_done = s;
+    if (done)
+      s = kNone;
+    if (dmask) {
       // at most 31 entries wait between batches and at most 32 groups finish
       // per round, so the 64-entry list never overflows
       const uint32_t base = s_npend[warp];
-      if (done && li == 0) {
+      if (queue) {
         const uint32_t pos = base + __popc(dmask & ((1u << lane) - 1u));
-        s_pend[warp][pos] = Pending{s, q.x, q.y, q.z, q.w};
+        s_pend[warp][pos] = Pending{c, s_done, q.x, q.y, q.z, q.w};
       }
       __syncwarp();
       uint32_t n = base + __popc(dmask);
-      if (done)
-        s = kNone;
-      if (p.do_work && n >= 32) {
+      if (n >= 32) {
         const Pending pe = s_pend[warp][lane];
-        hmm_work_lane(p, s_pc, pe.s, make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
+        const GenParams &pw = src.chunk(pe.c);
+        hmm_work_lane(pw, Src::kMulti ? pw.pc : pc_smem, pe.s,
+                      make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
         __syncwarp();
         if (lane < n - 32)
           s_pend[warp][lane] = s_pend[warp][lane + 32];
@@ -637,18 +725,41 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
       __syncwarp();
     }
   }
-  if (p.do_work) {
-    const uint32_t n = s_npend[warp];
-    if (lane < n) {
-      const Pending pe = s_pend[warp][lane];
-      hmm_work_lane(p, s_pc, pe.s, make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
-    }
+  const uint32_t n = s_npend[warp];
+  if (lane < n) {
+    const Pending pe = s_pend[warp][lane];
+    const GenParams &pw = src.chunk(pe.c);
+    hmm_work_lane(pw, Src::kMulti ? pw.pc : pc_smem, pe.s,
+                  make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
   }
-  if (p.stats && li == 0 && n_rounds) {
-    atomicAdd(p.stats, n_evals);
-    atomicAdd(p.stats + 1, n_rounds);
-    atomicAdd(p.stats + 2, n_acc);
+  if (stats && li == 0 && n_rounds) {
+    atomicAdd(stats, n_evals);
+    atomicAdd(stats + 1, n_rounds);
+    atomicAdd(stats + 2, n_acc);
   }
+}
+
+// One chunk per launch (the reference's RunHMMOnDevice granularity).
+template <int P, class E>
+__global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p) {
+  __shared__ float4 s_vq[16];
+  __shared__ float s_pc[16];
+  if (threadIdx.x < 16) {
+    s_pc[threadIdx.x] = p.pc[threadIdx.x];
+    if (p.vq_table)
+      s_vq[threadIdx.x] = p.vq_table[threadIdx.x];
+  }
+  __syncthreads();
+  const OneChunk src{p};
+  generation_body<P, E>(src, p.counter, p.stats, p.error, s_vq, s_pc);
+}
+
+// Many chunks of uneven size in one persistent launch: one queue over all
+// samples of all chunks.
+template <int P, class E>
+__global__ void __launch_bounds__(kThreads) generation_multi_kernel(const MultiParams mp) {
+  const ManyChunks src{mp};
+  generation_body<P, E>(src, mp.counter, mp.stats, mp.error, nullptr, nullptr);
 }
 
 }  // namespace glp

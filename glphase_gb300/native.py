@@ -26,7 +26,8 @@ EXPORTED = [
     "glp_set_tran", "glp_set_mutation_mat", "glp_set_codebook", "glp_set_packed_gls",
     "glp_set_emission", "glp_run_hmm_on_device", "glp_run_generation",
     "glp_run_generation_host", "glp_finish", "glp_set_lanes_per_sample", "glp_get_stats",
-    "glp_measure_fp32_peak", "glp_knn_neighbors",
+    "glp_measure_fp32_peak", "glp_knn_neighbors", "glp_problem_create",
+    "glp_problem_destroy", "glp_problem_set_model", "glp_problem_set_vq", "glp_run_batch",
 ]
 
 
@@ -96,6 +97,12 @@ def load(build_if_missing: bool = False):
     L.glp_get_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u32)]
     L.glp_measure_fp32_peak.argtypes = [vp, C.c_float, C.POINTER(C.c_double)]
     L.glp_knn_neighbors.argtypes = [vp, vp, u32, u32, u32, C.c_double, C.c_double, i32, vp]
+    L.glp_problem_create.argtypes = [vp, C.POINTER(vp)]
+    L.glp_problem_destroy.argtypes = [vp]
+    L.glp_problem_destroy.restype = None
+    L.glp_problem_set_model.argtypes = [vp, vp, vp, vp, vp, u32, u32]
+    L.glp_problem_set_vq.argtypes = [vp, vp, C.c_size_t, vp]
+    L.glp_run_batch.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs)]
     for name in EXPORTED:
         getattr(L, name)
     _lib = L

@@ -167,6 +167,35 @@ int glp_set_lanes_per_sample(glp_ctx *ctx, uint32_t lanes);
 int glp_get_stats(glp_ctx *ctx, uint64_t *evaluations, uint64_t *rounds,
                   uint32_t *lanes_used);
 
+/* ---- Many phasing chunks per launch (no reference counterpart: the
+ * reference runs one chunk per RunHMMOnDevice call, src/hmmLike.cu:399). ----
+ * A problem holds one chunk's device-resident model inputs, the same ones
+ * glp_set_tran / glp_set_mutation_mat / glp_set_emission / glp_set_codebook /
+ * glp_set_packed_gls give the context's own chunk. */
+typedef struct glp_problem glp_problem;
+
+int glp_problem_create(glp_ctx *ctx, glp_problem **out);
+void glp_problem_destroy(glp_problem *pb);
+
+/* tran [S][3], pc [4][4], emit [N][S][4], prob [N][S][3] (prob may be NULL
+ * when hmm_work is never run); host arrays, copied to the device. */
+int glp_problem_set_model(glp_problem *pb, const float *tran, const float *pc16,
+                          const float *emit, const float *prob, uint32_t num_samples,
+                          uint32_t num_sites);
+
+/* VQ codes [ceil(S/8)][N] and codebook [16][2] (host arrays). */
+int glp_problem_set_vq(glp_problem *pb, const uint32_t *packed, size_t num_words,
+                       const float *codebook);
+
+/* One generation of `count` chunks of any sizes in ONE persistent launch:
+ * args[i] (device pointers, as for glp_run_generation) runs on problems[i].
+ * The samples of all chunks share one work queue.  Asynchronous; finish with
+ * glp_finish().  All chunks use the same emission source (GLP_GEN_VQ or
+ * not).  Each chunk's results equal those of the same generation run alone
+ * (glp_run_generation): every draw is keyed by the chunk's own seed. */
+int glp_run_batch(glp_ctx *ctx, uint32_t count, glp_problem *const *problems,
+                  const glp_generation_args *args);
+
 /* kNN surrogate restriction on the device: for each of the H/2 samples,
  * the ceil(K/2) haplotypes nearest (Hamming distance over the sites whose
  * alt-allele frequency, or MAF when use_maf, lies in [freq_lb, freq_ub]) to
