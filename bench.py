@@ -48,6 +48,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--chunks", type=int, default=64, help="uneven workload: chunk count")
+    ap.add_argument("--scale", type=float, default=1.0, help="uneven workload: shrink shapes")
+    ap.add_argument("--requests", type=int, default=24, help="serving: request count")
+    ap.add_argument("--generations", type=int, default=32, help="serving: generations/request")
+    ap.add_argument("--budget-gb", type=float, default=180.0, help="serving: HBM budget")
+    ap.add_argument("--serve-limit", type=float, default=600.0)
     return ap.parse_args()
 
 
@@ -347,10 +353,170 @@ def run_e2e(eng, haps, N, S, C, H, wn, w, args, torch):
             "api": "glp_run_generation_host (pinned host buffers)"}
 
 
+def uneven_shapes(n_chunks, seed=4, scale=1.0):
+    """Chunk shapes of the uneven workload: sites ~ U{512..16384} in steps of
+    64, samples ~ U{100..5000} (scale < 1 shrinks both for tests)."""
+    rng = np.random.default_rng(seed)
+    S = 64 * rng.integers(8, 257, n_chunks)
+    N = rng.integers(100, 5001, n_chunks)
+    if scale != 1.0:
+        S = np.maximum(64, (S * scale).astype(int) // 64 * 64)
+        N = np.maximum(4, (N * scale).astype(int))
+    return [(int(n), int(s)) for n, s in zip(N, S)]
+
+
+def run_uneven(args):
+    """Batched (one persistent launch per generation, replayed CUDA graph)
+    vs plain (one launch per chunk) on the uneven-chunk workload."""
+    import torch
+    from glphase_gb300 import synth, synth_device as sd
+    from glphase_gb300.batch import DeviceProblem, PreparedBatch
+    from glphase_gb300.hmmlike import HMMLikeCUDA
+    C = args.cycles
+    shapes = uneven_shapes(args.chunks, scale=args.scale)
+    dev = HMMLikeCUDA(0)
+    dev.set_lanes_per_sample(args.lanes)
+    stream = torch.cuda.Stream()
+    dev._c(dev.L.glp_set_stream(dev.ctx, stream.cuda_stream))
+    probs = []
+    t0 = time.perf_counter()
+    for i, (N, S) in enumerate(shapes):
+        w = synth.Workload(f"chunk{i}", N=N, S=S, founders=40, depth=4.0, burnin=8,
+                           sampling=24, seed=100 + i)
+        probs.append(DeviceProblem(dev, sd.generate(w, N, S, seed=100 + i), C,
+                                   seed=5000 + i, burnin=8))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    upd = sum(N * (C + 1) * S for N, S in shapes)
+
+    def timed(fn, steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        dev._c(dev.L.glp_finish(dev.ctx))
+        return e0.elapsed_time(e1) / 1e3
+
+    batch = PreparedBatch(dev, probs, generation=0)
+    for _ in range(args.warmup):
+        batch.run()
+    dev._c(dev.L.glp_finish(dev.ctx))
+    clocks = ClockSampler(0)
+    clocks.start()
+    t_batched = timed(batch.run, args.steps)
+    ck = clocks.stop()
+    gen = batch.generation
+    batch.close()
+    singles = [PreparedBatch(dev, [p], generation=gen) for p in probs]
+
+    def plain():
+        for s in singles:
+            s.run(graph=False)
+    plain()
+    dev._c(dev.L.glp_finish(dev.ctx))
+    t_plain = timed(plain, args.steps)
+    for s in singles:
+        s.close()
+    ev, rounds, lanes = dev.stats()
+    v_b = args.steps * upd / t_batched
+    v_p = args.steps * upd / t_plain
+    line = {
+        "metric": METRIC, "value": v_b, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_batched / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"uneven: {len(shapes)} chunks, sites U{{512..16384}}/64, "
+                               f"samples U{{100..5000}}, C={C}, own seed/founders/map each",
+                   "chunks": len(shapes), "samples_total": int(sum(n for n, _ in shapes)),
+                   "updates_per_step": upd, "setup_s": round(setup_s, 1),
+                   "lanes_per_sample": lanes,
+                   "plain_value": v_p, "plain_ms_per_step": t_plain / args.steps * 1e3,
+                   "batched_over_plain": v_b / v_p,
+                   "form": "batched = one persistent launch per generation replayed from a "
+                           "captured CUDA graph; plain = one launch per chunk"},
+        "clocks": ck, "gpu_launches": 2 * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    for p in probs:
+        p.close()
+
+
+def run_serve(args):
+    """Poisson-arriving phasing requests (uneven-chunk shapes, 32 generations
+    each) served with continuous batching at 0.5x, 1x and 2x the measured
+    capacity; the plain form (one launch per resident request per tick) at
+    1x beside it."""
+    import torch
+    from glphase_gb300 import synth, synth_device as sd
+    from glphase_gb300.hmmlike import HMMLikeCUDA
+    from glphase_gb300.serve import Request, Server
+    C, G = args.cycles, args.generations
+    shapes = uneven_shapes(args.requests, seed=9, scale=args.scale)
+    dev = HMMLikeCUDA(0)
+    dev.set_lanes_per_sample(args.lanes)
+    stream = torch.cuda.Stream()
+    dev._c(dev.L.glp_set_stream(dev.ctx, stream.cuda_stream))
+    budget = int(args.budget_gb * 1e9)
+
+    def make(i, N, S):
+        w = synth.Workload(f"req{i}", N=N, S=S, founders=40, depth=4.0, burnin=8,
+                           sampling=24, seed=300 + i)
+        return Request(rid=i, chunk=sd.generate(w, N, S, seed=300 + i), generations=G,
+                       cycles=C, seed=9000 + i, burnin=8)
+
+    # capacity: saturated throughput of all requests resident at once
+    reqs = [make(i, N, S) for i, (N, S) in enumerate(shapes)]
+    mean_updates = float(np.mean([r.updates for r in reqs]))
+    cal = Server(dev, budget)
+    for r in reqs[:8]:
+        r.generations = 2
+        cal.submit(r)
+    cal.tick(0.0)
+    t0 = time.perf_counter()
+    cal.tick(0.0)
+    per_gen = sum(r.chunk.N * (C + 1) * r.chunk.S for r in reqs[:8])
+    capacity_ups = per_gen / (time.perf_counter() - t0)
+    capacity_rps = capacity_ups / mean_updates
+    results = {}
+    for load, plain in ((0.5, False), (1.0, False), (2.0, False), (1.0, True)):
+        rng = np.random.default_rng(int(load * 100) + plain)
+        gaps = rng.exponential(1.0 / (load * capacity_rps), size=len(shapes))
+        reqs = [make(i, N, S) for i, (N, S) in enumerate(shapes)]
+        for r, a in zip(reqs, np.cumsum(gaps)):
+            r.arrival = float(a)
+        torch.cuda.synchronize()
+        srv = Server(dev, budget, plain=plain)
+        st = srv.serve(reqs, time_limit=args.serve_limit)
+        key = ("plain" if plain else "batched") + f"@{load}x"
+        results[key] = st.summary()
+        del reqs, srv
+        torch.cuda.empty_cache()
+    b1, p1 = results["batched@1.0x"], results["plain@1.0x"]
+    line = {
+        "metric": "serving: p50/p99 request latency and site-updates/s", "value":
+            b1["updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": len(shapes),
+        "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"serving: {len(shapes)} Poisson-arriving requests, uneven-chunk "
+                               f"shapes, {G} generations each, C={C}, panel off",
+                   "hbm_budget_gb": args.budget_gb, "capacity_updates_per_s": capacity_ups,
+                   "capacity_requests_per_s": capacity_rps, "results": results,
+                   "batched_over_plain_at_1x": b1["updates_per_s"] / p1["updates_per_s"]},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "uneven":
+        run_uneven(args)
+    elif args.config == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

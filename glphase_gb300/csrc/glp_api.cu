@@ -37,6 +37,7 @@ struct glp_problem {
   float4 *d_emit = nullptr;
   float *d_prob = nullptr;
   uint32_t eN = 0, eS = 0;  // shape of emit/prob
+  bool borrowed = false;     // emit/prob belong to the caller
   float4 *d_beta = nullptr;  // hmm_work scratch [N][S]
   size_t beta_cap = 0;
 };
@@ -119,12 +120,23 @@ void release(T *&p) {
   p = nullptr;
 }
 
+void drop_emission(glp_problem *pb) {
+  if (pb->borrowed) {
+    pb->d_emit = nullptr;
+    pb->d_prob = nullptr;
+  } else {
+    release(pb->d_emit);
+    release(pb->d_prob);
+  }
+  pb->borrowed = false;
+  pb->eN = pb->eS = 0;
+}
+
 void release_problem(glp_problem *pb) {
   release(pb->d_tran4);
   release(pb->d_vq);
   release(pb->d_packed);
-  release(pb->d_emit);
-  release(pb->d_prob);
+  drop_emission(pb);
   release(pb->d_beta);
   pb->S = pb->eN = pb->eS = 0;
   pb->packed_words = pb->beta_cap = 0;
@@ -223,10 +235,8 @@ int set_emission(glp_problem *pb, const float *emit, const float *prob, uint32_t
   if (!emit || N == 0 || S == 0)
     return fail(c, GLP_ERR_ARG, "emit must be non-null with positive N and S");
   const size_t ns = (size_t)N * S;
-  if (pb->eN != N || pb->eS != S) {
-    release(pb->d_emit);
-    release(pb->d_prob);
-    pb->eN = pb->eS = 0;
+  if (pb->eN != N || pb->eS != S || pb->borrowed) {
+    drop_emission(pb);
     GLP_CUDA(c, cudaMalloc((void **)&pb->d_emit, sizeof(float4) * ns));
     GLP_CUDA(c, cudaMalloc((void **)&pb->d_prob, sizeof(float) * 3 * ns));
     pb->eN = N;
@@ -383,6 +393,8 @@ int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
   p->seed = a->seed;
   p->generation = a->generation;
   p->do_work = work ? 1u : 0u;
+  p->burnin = a->burnin;
+  p->kick = a->kick_start ? 1u : 0u;
   return GLP_OK;
 }
 
@@ -589,6 +601,28 @@ int glp_problem_set_model(glp_problem *pb, const float *tran, const float *pc16,
   return GLP_OK;
 }
 
+int glp_problem_set_model_device(glp_problem *pb, const float *tran, const float *pc16,
+                                 const float *emit_dev, const float *prob_dev,
+                                 uint32_t num_samples, uint32_t num_sites) {
+  if (!pb || !pb->ctx)
+    return GLP_ERR_ARG;
+  glp_ctx *c = pb->ctx;
+  int rc = check_ctx(c);
+  if (rc || (rc = set_tran(pb, tran, num_sites)) || (rc = set_pc(pb, pc16)))
+    return rc;
+  if (!emit_dev || num_samples == 0 || num_sites == 0)
+    return fail(c, GLP_ERR_ARG, "emit must be non-null with positive N and S");
+  if (((uintptr_t)emit_dev & 15u) || ((uintptr_t)prob_dev & 3u))
+    return fail(c, GLP_ERR_ARG, "emit must be 16-byte and prob 4-byte aligned");
+  drop_emission(pb);
+  pb->d_emit = (float4 *)emit_dev;
+  pb->d_prob = (float *)prob_dev;
+  pb->borrowed = true;
+  pb->eN = num_samples;
+  pb->eS = num_sites;
+  return GLP_OK;
+}
+
 int glp_problem_set_vq(glp_problem *pb, const uint32_t *packed, size_t num_words,
                        const float *codebook) {
   if (!pb || !pb->ctx)
@@ -671,6 +705,160 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = chain_cycles;
+  return GLP_OK;
+}
+
+}  // extern "C"
+
+struct glp_batch {
+  glp_ctx *c = nullptr;
+  uint32_t count = 0;
+  uint64_t total = 0, chain_cycles = 0;
+  uint32_t P = 4;
+  unsigned grid = 1;
+  glp::GenParams *d_table = nullptr;
+  uint32_t *d_offsets = nullptr;
+  glp::MultiParams mp;
+  MultiFn fn = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int batch_enqueue(glp_batch *b, cudaStream_t st) {
+  glp_ctx *c = b->c;
+  GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), st));
+  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), st));
+  b->fn<<<b->grid, glp::kThreads, 0, st>>>(b->mp);
+  GLP_CUDA(c, cudaGetLastError());
+  glp::advance_kernel<<<(b->count + 127) / 128, 128, 0, st>>>(b->d_table, b->count);
+  GLP_CUDA(c, cudaGetLastError());
+  return GLP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void glp_batch_destroy(glp_batch *b) {
+  if (!b)
+    return;
+  if (b->c) {
+    cudaSetDevice(b->c->device);
+    cudaStreamSynchronize(b->c->stream);
+  }
+  if (b->exec)
+    cudaGraphExecDestroy(b->exec);
+  if (b->graph)
+    cudaGraphDestroy(b->graph);
+  release(b->d_table);
+  release(b->d_offsets);
+  delete b;
+}
+
+int glp_batch_prepare(glp_ctx *c, uint32_t count, glp_problem *const *problems,
+                      const glp_generation_args *args, glp_batch **out) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!out || count == 0 || !problems || !args)
+    return fail(c, GLP_ERR_ARG, "a batch needs count > 0, problems, args and out");
+  *out = nullptr;
+  const bool vq = (args[0].flags & GLP_GEN_VQ) != 0;
+  std::vector<glp::GenParams> table(count);
+  std::vector<uint32_t> offsets(count + 1, 0);
+  uint64_t total = 0, chain_cycles = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    glp_problem *pb = problems[i];
+    if (!pb || pb->ctx != c)
+      return fail(c, GLP_ERR_ARG, "problem %u does not belong to this context", i);
+    if (((args[i].flags & GLP_GEN_VQ) != 0) != vq)
+      return fail(c, GLP_ERR_ARG, "all chunks of a batch must use the same emission source");
+    if (args[i].hap_idxs_in || (args[i].num_cycles && args[i].props))
+      return fail(c, GLP_ERR_ARG, "prepared batches draw their surrogates on the device");
+    if (args[i].trace_slot || args[i].trace_accept || args[i].trace_work)
+      return fail(c, GLP_ERR_ARG, "prepared batches do not replay traces");
+    if ((rc = make_params(c, pb, &args[i], &table[i])))
+      return rc;
+    total += args[i].num_samples;
+    chain_cycles += (uint64_t)args[i].num_samples * args[i].num_cycles;
+    if (total > 0xffffffffull)
+      return fail(c, GLP_ERR_ARG, "a batch holds at most 2^32-1 samples");
+    offsets[i + 1] = (uint32_t)total;
+  }
+  glp_batch *b = new glp_batch();
+  b->c = c;
+  b->count = count;
+  b->total = total;
+  b->chain_cycles = chain_cycles;
+  cudaStream_t cs = nullptr;
+  auto bail = [&](int code) {
+    if (cs)
+      cudaStreamDestroy(cs);
+    glp_batch_destroy(b);
+    return code;
+  };
+  if (cudaMalloc((void **)&b->d_table, sizeof(glp::GenParams) * count) != cudaSuccess ||
+      cudaMalloc((void **)&b->d_offsets, sizeof(uint32_t) * (count + 1)) != cudaSuccess)
+    return bail(fail(c, GLP_ERR_NOMEM, "batch descriptor allocation failed"));
+  if (cudaMemcpy(b->d_table, table.data(), sizeof(glp::GenParams) * count,
+                 cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_offsets, offsets.data(), sizeof(uint32_t) * (count + 1),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(c, GLP_ERR_CUDA, "batch descriptor upload failed"));
+  b->mp.chunks = b->d_table;
+  b->mp.offsets = b->d_offsets;
+  b->mp.nchunks = count;
+  b->mp.counter = c->d_counter;
+  b->mp.stats = c->d_stats;
+  b->mp.error = c->d_error;
+  b->P = choose_lanes(c, total);
+  b->fn = multi_kernel(b->P, vq);
+  b->grid = grid_for(c, b->fn, total, b->P, &rc);
+  if (rc)
+    return bail(rc);
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(c, GLP_ERR_CUDA, "capture stream creation failed"));
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess)
+    return bail(fail(c, GLP_ERR_CUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e)));
+  rc = batch_enqueue(b, cs);
+  e = cudaStreamEndCapture(cs, &b->graph);
+  if (rc)
+    return bail(rc);
+  if (e != cudaSuccess)
+    return bail(fail(c, GLP_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e)));
+  e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  if (e != cudaSuccess)
+    return bail(fail(c, GLP_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e)));
+  cudaStreamDestroy(cs);
+  *out = b;
+  return GLP_OK;
+}
+
+int glp_batch_run(glp_batch *b) {
+  if (!b || !b->c)
+    return GLP_ERR_ARG;
+  glp_ctx *c = b->c;
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  GLP_CUDA(c, cudaGraphLaunch(b->exec, c->stream));
+  c->lanes_used = b->P;
+  c->last_chain_cycles = b->chain_cycles;
+  return GLP_OK;
+}
+
+int glp_batch_launch(glp_batch *b) {
+  if (!b || !b->c)
+    return GLP_ERR_ARG;
+  glp_ctx *c = b->c;
+  int rc = check_ctx(c);
+  if (rc || (rc = batch_enqueue(b, c->stream)))
+    return rc;
+  c->lanes_used = b->P;
+  c->last_chain_cycles = b->chain_cycles;
   return GLP_OK;
 }
 

@@ -75,6 +75,8 @@ struct GenParams {
   int *__restrict__ error;
   const uint32_t *__restrict__ nbr;  // [N][klen] surrogate table, or null
   uint32_t klen, samp_lo, samp_hi;   // uniform surrogates over [samp_lo, samp_hi)
+  uint32_t burnin;                   // >0: advance_kernel sets pen = min((g+1)/burnin,1)^2
+  uint32_t kick;                     // 1: surrogates from [samp_lo, H) in generation 0 only
   float pc[16];
   float pen;
   uint64_t seed;
@@ -86,14 +88,22 @@ struct GenParams {
 // Emission sources.  Both hand out the 4 emission values of a site,
 // e[(father_bit << 1) | mother_bit] (impute.cpp:338-342).
 
+// L1 prefetch of the line holding `ptr` (no register is held; the later
+// load of the same line then hits L1).
+__device__ __forceinline__ void prefetch_l1(const void *ptr) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+}
+
 // Sites are consumed in blocks of 8 (m0 a multiple of 8): prep8(m0) readies
 // a block, get8(m0, j) returns site m0 + j for a compile-time j; get1(m) is
-// the unblocked form used on ragged tails.
+// the unblocked form used on ragged tails; ahead(m) prefetches the block
+// holding site m (m must be a valid site).
 struct EmitF32 {
   const float4 *row;
   __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *) {
     row = p.emit + (size_t)s * p.S;
   }
+  __device__ __forceinline__ void ahead(uint32_t m) const { prefetch_l1(row + m); }
   __device__ __forceinline__ void prep8(uint32_t) {}
   __device__ __forceinline__ float4 get8(uint32_t m0, uint32_t j) const {
     return __ldg(row + m0 + j);
@@ -113,6 +123,9 @@ struct EmitVQ {
     col = p.packed + s;
     stride = p.N;
     table = tab;
+  }
+  __device__ __forceinline__ void ahead(uint32_t m) const {
+    prefetch_l1(col + (size_t)(m >> 3) * stride);
   }
   __device__ __forceinline__ void prep8(uint32_t m0) {
     pk = __ldg(col + (size_t)(m0 >> 3) * stride);
@@ -320,14 +333,35 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
       --wb;
     }
     const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
+    // the forward stream only ever reads sites below wf*64 and the backward
+    // stream sites at or above it, so prefetches stay inside the row
+    const uint32_t fwd_end = wf * 64 - 1, bwd_lo = wf * 64;
+    if (nb) {
+      ef.ahead(0);
+      ef.ahead(8);
+      eb.ahead(wb * 64 + 56);
+      eb.ahead(wb * 64 + 48);
+    }
 #pragma unroll 1
     for (uint32_t i = 0; i < nb; ++i) {
       const uint32_t wfw = i, wbw = wb - i;
       const Parents pf = load_parents(p.haps, wn, q, wfw);
       const Parents pb = load_parents(p.haps, wn, q, wbw);
+      if (i + 1 < nb) {  // next words' parents
+        prefetch_l1(p.haps + (size_t)q.x * wn + wfw + 1);
+        prefetch_l1(p.haps + (size_t)q.y * wn + wfw + 1);
+        prefetch_l1(p.haps + (size_t)q.z * wn + wfw + 1);
+        prefetch_l1(p.haps + (size_t)q.w * wn + wfw + 1);
+        prefetch_l1(p.haps + (size_t)q.x * wn + wbw - 1);
+        prefetch_l1(p.haps + (size_t)q.y * wn + wbw - 1);
+        prefetch_l1(p.haps + (size_t)q.z * wn + wbw - 1);
+        prefetch_l1(p.haps + (size_t)q.w * wn + wbw - 1);
+      }
 #pragma unroll 1
       for (uint32_t blk = 0; blk < 8; ++blk) {
         const uint32_t m0 = wfw * 64 + blk * 8, n0 = wbw * 64 + (7 - blk) * 8;
+        ef.ahead(min(m0 + 16, fwd_end));
+        eb.ahead(n0 >= bwd_lo + 16 ? n0 - 16 : bwd_lo);
         ef.prep8(m0);
         eb.prep8(n0);
         both_block8(f, b, ef, eb, tran4, window8(pf, blk * 8), window8(pb, (7 - blk) * 8), m0,
@@ -342,6 +376,7 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
 #pragma unroll 1
       for (uint32_t blk = 0; blk < 8; ++blk) {
         const uint32_t m0 = i * 64 + blk * 8;
+        ef.ahead(min(m0 + 16, fwd_end));
         ef.prep8(m0);
         fwd_block8(f, ef, tran4, window8(pf, blk * 8), m0);
       }
@@ -752,6 +787,33 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
   __syncthreads();
   const OneChunk src{p};
   generation_body<P, E>(src, p.counter, p.stats, p.error, s_vq, s_pc);
+}
+
+// Moves every chunk of a prepared batch to its next generation in place, so
+// a captured CUDA graph can replay generation after generation: the new
+// haplotypes become the current ones (Insti::cudaSolve's swap,
+// insti.cpp:1455), the generation counter advances, the annealing penalty
+// follows Insti::estimate (insti.cpp:1670-1671, binary32), and the
+// kick-start restriction of the surrogates ends after generation 0.
+__global__ void advance_kernel(GenParams *__restrict__ table, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  GenParams &p = table[i];
+  if (p.do_work) {
+    uint64_t *cur = const_cast<uint64_t *>(p.haps);
+    p.haps = p.hnew;
+    p.hnew = cur;
+  }
+  p.generation += 1;
+  if (p.burnin) {
+    const float x = fminf(__fdiv_rn((float)p.generation + 1.0f, (float)p.burnin), 1.0f);
+    p.pen = x * x;
+  }
+  if (p.kick) {
+    p.samp_lo = 0;
+    p.kick = 0;
+  }
 }
 
 // Many chunks of uneven size in one persistent launch: one queue over all

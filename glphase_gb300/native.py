@@ -28,6 +28,8 @@ EXPORTED = [
     "glp_run_generation_host", "glp_finish", "glp_set_lanes_per_sample", "glp_get_stats",
     "glp_measure_fp32_peak", "glp_knn_neighbors", "glp_problem_create",
     "glp_problem_destroy", "glp_problem_set_model", "glp_problem_set_vq", "glp_run_batch",
+    "glp_problem_set_model_device", "glp_batch_prepare", "glp_batch_run", "glp_batch_launch",
+    "glp_batch_destroy",
 ]
 
 
@@ -53,6 +55,7 @@ class GenerationArgs(C.Structure):
         ("like_out", C.c_void_p), ("eval_trace", C.c_void_p), ("accept_trace", C.c_void_p),
         ("neighbors", C.c_void_p), ("neighbors_per_sample", C.c_uint32),
         ("sample_lo", C.c_uint32), ("sample_hi", C.c_uint32),
+        ("burnin", C.c_uint32), ("kick_start", C.c_uint32),
     ]
 
 
@@ -102,6 +105,13 @@ def load(build_if_missing: bool = False):
     L.glp_problem_destroy.restype = None
     L.glp_problem_set_model.argtypes = [vp, vp, vp, vp, vp, u32, u32]
     L.glp_problem_set_vq.argtypes = [vp, vp, C.c_size_t, vp]
+    L.glp_problem_set_model_device.argtypes = [vp, vp, vp, vp, vp, u32, u32]
+    L.glp_batch_prepare.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs),
+                                    C.POINTER(vp)]
+    L.glp_batch_run.argtypes = [vp]
+    L.glp_batch_launch.argtypes = [vp]
+    L.glp_batch_destroy.argtypes = [vp]
+    L.glp_batch_destroy.restype = None
     L.glp_run_batch.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs)]
     for name in EXPORTED:
         getattr(L, name)

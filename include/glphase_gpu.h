@@ -89,6 +89,13 @@ typedef struct glp_generation_args {
   const uint32_t *neighbors;     /* [N][neighbors_per_sample] device, or NULL */
   uint32_t neighbors_per_sample;
   uint32_t sample_lo, sample_hi;
+  /* Used by prepared batches advancing on the device (glp_batch_run):
+   * burnin > 0 recomputes pen = min((generation+1)/burnin, 1)^2 each
+   * generation (src/insti.cpp:1670-1671); kick_start = 1 limits the
+   * surrogates to [sample_lo, sample_hi) in the first generation only, then
+   * [0, sample_hi) (README "kickstart" semantics). */
+  uint32_t burnin;
+  uint32_t kick_start;
 } glp_generation_args;
 
 /* Number of visible CUDA devices and whether device `device` is an sm_103
@@ -183,6 +190,13 @@ int glp_problem_set_model(glp_problem *pb, const float *tran, const float *pc16,
                           const float *emit, const float *prob, uint32_t num_samples,
                           uint32_t num_sites);
 
+/* The same with emit and prob already in device memory: the problem borrows
+ * the two DEVICE arrays (no copy); the caller keeps them alive until the
+ * problem is destroyed or given new ones.  tran and pc are host arrays. */
+int glp_problem_set_model_device(glp_problem *pb, const float *tran, const float *pc16,
+                                 const float *emit_dev, const float *prob_dev,
+                                 uint32_t num_samples, uint32_t num_sites);
+
 /* VQ codes [ceil(S/8)][N] and codebook [16][2] (host arrays). */
 int glp_problem_set_vq(glp_problem *pb, const uint32_t *packed, size_t num_words,
                        const float *codebook);
@@ -195,6 +209,23 @@ int glp_problem_set_vq(glp_problem *pb, const uint32_t *packed, size_t num_words
  * (glp_run_generation): every draw is keyed by the chunk's own seed. */
 int glp_run_batch(glp_ctx *ctx, uint32_t count, glp_problem *const *problems,
                   const glp_generation_args *args);
+
+/* A prepared batch: the chunk descriptors live on the device and each run
+ * performs one generation of every chunk and then advances all chunks to
+ * their next generation on the device (haps <-> hnew swap, generation + 1,
+ * penalty schedule, kick-start end).  glp_batch_run replays a CUDA graph
+ * captured at preparation (reset counters, the persistent generation kernel,
+ * the advance kernel): no host work per generation.  glp_batch_launch issues
+ * the same work as plain launches.  Both are asynchronous on the context
+ * stream; glp_finish() waits and reports device errors.  The lanes per
+ * sample are fixed at preparation. */
+typedef struct glp_batch glp_batch;
+
+int glp_batch_prepare(glp_ctx *ctx, uint32_t count, glp_problem *const *problems,
+                      const glp_generation_args *args, glp_batch **out);
+int glp_batch_run(glp_batch *batch);
+int glp_batch_launch(glp_batch *batch);
+void glp_batch_destroy(glp_batch *batch);
 
 /* kNN surrogate restriction on the device: for each of the H/2 samples,
  * the ceil(K/2) haplotypes nearest (Hamming distance over the sites whose

@@ -105,6 +105,45 @@ def test_batch_equals_alone_and_oracle(dev, oracle_lib):
         dev.L.glp_problem_destroy(ch.pb)
 
 
+def _device_problems(dev, sizes, cycles, burnin, kick=False):
+    from glphase_gb300 import synth_device as sd
+    from glphase_gb300.batch import DeviceProblem
+    w = synth.Workload("dev", N=1, S=1, founders=9, depth=3.0, burnin=burnin, sampling=2,
+                       panel_haps=12 if kick else 0)
+    out = []
+    for i, (N, S) in enumerate(sizes):
+        ch = sd.generate(w, N, S, seed=50 + i)
+        out.append(DeviceProblem(dev, ch, cycles, seed=700 + i, burnin=burnin, kick_start=kick))
+    return out
+
+
+@pytest.mark.parametrize("kick", [False, True])
+def test_prepared_batch_graph_replay(dev, kick):
+    """G generations replayed from one captured CUDA graph (device-side
+    advance) equal G generations driven from the host with glp_run_batch."""
+    import torch
+    from glphase_gb300.batch import PreparedBatch, run_batch
+    sizes = [(33, 200), (7, 640), (90, 129), (20, 1024)]
+    G = 5
+    a = _device_problems(dev, sizes, 9, burnin=3, kick=kick)
+    b = _device_problems(dev, sizes, 9, burnin=3, kick=kick)
+    torch.cuda.synchronize()
+    pb = PreparedBatch(dev, a, generation=0)
+    for g in range(G):
+        pb.run(graph=(g % 2 == 0))
+    dev._c(dev.L.glp_finish(dev.ctx))
+    for g in range(G):
+        run_batch(dev, b, g)
+        dev._c(dev.L.glp_finish(dev.ctx))
+    for x, y in zip(a, b):
+        assert torch.equal(x.haps, y.haps)
+        assert torch.equal(x.quad, y.quad)
+        assert torch.equal(x.like, y.like)
+    pb.close()
+    for p in a + b:
+        p.close()
+
+
 def test_batch_argument_errors(dev):
     ch = Chunk(dev, 6, 100, 4, seed=9)
     a = ch.args(1.0, 0)

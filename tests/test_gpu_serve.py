@@ -1,0 +1,61 @@
+"""Serving loop with continuous batching: a request's result is the same
+alone and in a mix of requests that arrive while it is on the GPU; the HBM
+budget bounds what is resident."""
+import pytest
+
+from glphase_gb300 import synth, synth_device as sd
+from glphase_gb300.hmmlike import HMMLikeCUDA
+from glphase_gb300.serve import Request, Server
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dev():
+    import torch
+    torch.cuda.init()
+    d = HMMLikeCUDA(0)
+    yield d
+    d.cleanup()
+
+
+def make(i, N, S, generations=6, arrival=0.0):
+    w = synth.Workload(f"r{i}", N=N, S=S, founders=8, depth=3.0, burnin=3, sampling=3,
+                       seed=40 + i)
+    return Request(rid=i, chunk=sd.generate(w, N, S, seed=40 + i), generations=generations,
+                   cycles=12, seed=900 + i, burnin=3, arrival=arrival)
+
+
+def test_request_same_alone_and_in_mix(dev):
+    import torch
+    alone = Server(dev, budget_bytes=1 << 34)
+    r = make(0, 60, 700)
+    alone.serve([r])
+    ref_haps = r.result_haps.clone()
+    ref_like = r.result_like.clone()
+    # the same request, arriving while three others are being served
+    others = [make(1, 25, 130, 9, 0.0), make(2, 80, 1024, 4, 0.0), make(3, 7, 64, 7, 0.0)]
+    r2 = make(0, 60, 700, arrival=0.01)
+    mix = Server(dev, budget_bytes=1 << 34)
+    st = mix.serve(others + [r2])
+    assert st.peak_resident >= 2
+    assert torch.equal(r2.result_haps, ref_haps)
+    assert torch.equal(r2.result_like, ref_like)
+    assert len(st.latencies) == 4
+
+
+def test_budget_limits_residency(dev):
+    reqs = [make(i, 30, 300, 3) for i in range(4)]
+    one = reqs[0].footprint()
+    srv = Server(dev, budget_bytes=int(one * 2.5))
+    st = srv.serve(reqs)
+    assert st.peak_resident == 2
+    assert st.peak_bytes <= int(one * 2.5)
+    assert len(st.latencies) == 4
+
+
+def test_oversized_request_is_rejected(dev):
+    r = make(0, 30, 300, 2)
+    srv = Server(dev, budget_bytes=r.footprint() - 1)
+    with pytest.raises(ValueError):
+        srv.serve([r])
