@@ -16,13 +16,13 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/glphase_gpu.h"
 #include "glp_kernels.cuh"
 #include "glp_knn.cuh"
-
 struct glp_problem {
   glp_ctx *ctx = nullptr;
   uint32_t S = 0;  // sites of tran
@@ -1126,4 +1126,162 @@ extern "C" int glp_measure_fp32_peak(glp_ctx *c, float ms_target, double *tflops
   GLP_CUDA(c, cudaGetLastError());
   *tflops = best;
   return GLP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free generation (glp_run_generation_noalloc).
+//
+// The scratch of one generation lives in a file-scope device array instead
+// of memory from cudaMalloc.  Layout, in bytes from the start:
+//   [0, 4)     work-queue counter          (cleared by every call)
+//   [8, 32)    statistics, 3 x uint64      (cleared by every call)
+//   [32, 36)   device error flag           (cleared by every call)
+//   [256, 256 + round_up(16 S, 256))        transition table, float4 [S]
+//   then       hmm_work rows, float4 [N][S] (written before they are read)
+// Host code never dereferences g_noalloc_scratch: its name there is a host
+// stand-in, so the device address is looked up with cudaGetSymbolAddress once
+// per device (with that device current) and passed to the kernels.
+
+namespace {
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[GLP_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[kNoallocMaxDevices];
+
+// Kernel layout of the reference's tran [S][3] (row 0 unused,
+// hmmLike.cu:325): row 0 becomes the identity so that the first forward step
+// reproduces l = e / 4.
+__global__ void tran4_kernel(const float *__restrict__ tran, uint32_t S,
+                             float4 *__restrict__ out) {
+  const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < S)
+    out[m] = m ? make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2], 0.f)
+               : make_float4(1.f, 0.f, 0.f, 0.f);
+}
+
+size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const float *tran,
+                                          const float *pc16, const float *emit,
+                                          const float *prob, void *stream) {
+  if (!a || !tran || !pc16 || !emit || !a->haps || !a->hap_idxs_out)
+    return GLP_ERR_ARG;
+  const uint32_t N = a->num_samples, S = a->num_sites, C = a->num_cycles, H = a->num_haps;
+  const bool work = (a->flags & GLP_GEN_NO_WORK) == 0;
+  if (N == 0 || S == 0 || H < 2 || (uint64_t)2 * N > H || (a->flags & GLP_GEN_VQ))
+    return GLP_ERR_ARG;
+  if ((work && (!a->hnew || !prob)) || ((uintptr_t)emit & 15u))
+    return GLP_ERR_ARG;
+  if (!(a->pen > 0.0f) || !std::isfinite(a->pen))
+    return GLP_ERR_ARG;
+  const bool tr = a->trace_slot || a->trace_accept || a->trace_work;
+  if (tr && !(a->trace_slot && a->trace_accept && a->trace_work))
+    return GLP_ERR_ARG;
+  uint32_t lo = a->sample_lo, hi = a->sample_hi;
+  if (lo == 0 && hi == 0)
+    hi = H;
+  if ((!a->hap_idxs_in || (C && !a->props)) && !a->neighbors &&
+      (hi > H || lo >= hi || hi - lo < 3))
+    return GLP_ERR_ARG;
+  if (a->neighbors && a->neighbors_per_sample == 0)
+    return GLP_ERR_ARG;
+  const size_t tran_off = 256, beta_off = tran_off + round256((size_t)16 * S);
+  const size_t need = beta_off + (work ? (size_t)16 * N * S : 0);
+  if (need > GLP_NOALLOC_SCRATCH_BYTES)
+    return GLP_ERR_TOO_LARGE;
+
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess)
+    return GLP_ERR_CUDA;
+  if (dev < 0 || dev >= kNoallocMaxDevices)
+    return GLP_ERR_DEVICE;
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+        return GLP_ERR_CUDA;
+      g_noalloc_addr[dev] = p;
+    }
+    base = static_cast<unsigned char *>(g_noalloc_addr[dev]);
+  }
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return GLP_ERR_CUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+
+  glp::GenParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.N = N;
+  p.S = S;
+  p.C = C;
+  p.H = H;
+  p.wn = (S + 63) / 64;
+  p.emit_mode = GLP_EMIT_FLOAT;
+  p.haps = a->haps;
+  p.hnew = a->hnew;
+  p.emit = reinterpret_cast<const float4 *>(emit);
+  p.prob = prob;
+  p.tran4 = reinterpret_cast<const float4 *>(base + tran_off);
+  p.quad_in = a->hap_idxs_in;
+  p.quad_out = a->hap_idxs_out;
+  p.props = a->props;
+  p.tr_slot = a->trace_slot;
+  p.tr_u = a->trace_accept;
+  p.tr_work = a->trace_work;
+  p.like_out = a->like_out;
+  p.eval_trace = a->eval_trace;
+  p.accept_trace = a->accept_trace;
+  p.beta = reinterpret_cast<float4 *>(base + beta_off);
+  p.counter = reinterpret_cast<uint32_t *>(base);
+  p.stats = reinterpret_cast<unsigned long long *>(base + 8);
+  p.error = reinterpret_cast<int *>(base + 32);
+  p.nbr = a->neighbors;
+  p.klen = a->neighbors_per_sample;
+  p.samp_lo = lo;
+  p.samp_hi = hi;
+  std::memcpy(p.pc, pc16, sizeof(p.pc));
+  p.pen = a->pen;
+  p.seed = a->seed;
+  p.generation = a->generation;
+  p.do_work = work ? 1u : 0u;
+
+  // speculation width for an acceptance rate of about 0.12 (the rule of
+  // choose_lanes without a context's history)
+  uint32_t P = 1;
+  double best = 0;
+  for (uint32_t w = 1; w <= 32; w <<= 1) {
+    const double eff = (1.0 - std::pow(0.88, (double)w)) / (0.12 * w);
+    const double score = eff * std::min(1.0, (double)N * w / ((double)sms * 512.0));
+    if (score > best * 1.02) {
+      best = score;
+      P = w;
+    }
+  }
+  SingleFn fn = single_kernel(P, false);
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, 0) != cudaSuccess)
+    return GLP_ERR_CUDA;
+  const uint64_t groups = (uint64_t)glp::kThreads / P;
+  const uint64_t want = ((uint64_t)N + groups - 1) / groups;
+  const unsigned grid =
+      (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)std::max(occ, 1) * sms));
+
+  if (cudaMemsetAsync(base, 0, 256, st) != cudaSuccess)
+    return GLP_ERR_CUDA;
+  tran4_kernel<<<(S + 255) / 256, 256, 0, st>>>(tran, S, (float4 *)(base + tran_off));
+  fn<<<grid, glp::kThreads, 0, st>>>(p);
+  if (cudaGetLastError() != cudaSuccess)
+    return GLP_ERR_CUDA;
+  int h_err = 0;
+  if (cudaMemcpyAsync(&h_err, base + 32, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return GLP_ERR_CUDA;
+  return h_err ? GLP_ERR_INDEX : GLP_OK;
 }

@@ -43,7 +43,8 @@ typedef enum glp_status {
   GLP_ERR_NOMEM = 3,    /* device allocation failed */
   GLP_ERR_STATE = 4,    /* a required model input was not set */
   GLP_ERR_INDEX = 5,    /* a haplotype index >= num_haps reached the device */
-  GLP_ERR_DEVICE = 6    /* no usable device */
+  GLP_ERR_DEVICE = 6,   /* no usable device */
+  GLP_ERR_TOO_LARGE = 7 /* problem exceeds the fixed scratch of glp_run_generation_noalloc */
 } glp_status;
 
 typedef struct glp_ctx glp_ctx;
@@ -238,6 +239,40 @@ void glp_batch_destroy(glp_batch *batch);
 int glp_knn_neighbors(glp_ctx *ctx, const uint64_t *haps, uint32_t num_haps, uint32_t num_sites,
                       uint32_t k, double freq_lb, double freq_ub, int use_maf,
                       uint32_t *neighbors);
+
+/* Allocation-free generation (no counterpart in the reference).
+ *
+ * For callers that must not allocate device memory: code whose device memory
+ * is owned by another allocator (a framework's caching allocator or an arena
+ * reserved at start-up) and code that must not stall other streams, since
+ * cudaMalloc/cudaFree can synchronize the whole device.  Every other entry
+ * point of this library allocates its buffers (context, staging, scratch) on
+ * first use; this one allocates nothing.
+ *
+ * It runs one generation like glp_run_generation (fused hmm_work, float
+ * emission, surrogates from args or drawn on the device) with all of its
+ * scratch -- work counter, statistics, error flag, the transition table in
+ * kernel layout and the hmm_work rows -- in one fixed array of
+ * GLP_NOALLOC_SCRATCH_BYTES (32 MiB) of device memory that every GPU loading
+ * this library holds until the process exits.  It needs
+ * 256 + 16*ceil(S/16)*16 + 16*N*S bytes of it and returns GLP_ERR_TOO_LARGE
+ * beyond that (about N*S <= 2.0e6 site-samples).
+ *
+ * All array arguments are DEVICE pointers except pc16 (host, row-major
+ * pc[4][4]): tran [S][3], emit [N][S][4] (16-byte aligned), prob [N][S][3],
+ * and those of args (GLP_GEN_VQ is not accepted).  Work is issued on
+ * `stream` (cudaStream_t, NULL = legacy default stream) and the call returns
+ * when it has finished, reporting GLP_ERR_INDEX for an out-of-range
+ * haplotype index.
+ *
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  Calls share the one array: calls that overlap on the GPU (other
+ * host threads, other streams) race and must be serialized by the caller. */
+#define GLP_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+int glp_run_generation_noalloc(const glp_generation_args *args, const float *tran,
+                               const float *pc16, const float *emit, const float *prob,
+                               void *stream);
 
 /* Calibration (no reference counterpart): runs a dependent-free FMA stream on
  * every SM for about `ms_target` milliseconds and reports the achieved FP32
