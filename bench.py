@@ -65,11 +65,13 @@ def dist_env():
 
 
 def workload(args, rank):
-    from glphase_gb300 import synth
+    """This rank's chunk: replicas phase independent chunks (weak scaling)."""
+    from glphase_gb300 import replicas, synth
     w = synth.CONFIGS[args.config]
     N = args.samples or w.N
     S = args.sites or w.S
-    ds = synth.generate(w, N=N, S=S, seed=w.seed + 1000 * rank)
+    rp = replicas.plan(w.seed, rank=rank, world=max(rank + 1, dist_env()[0]))
+    ds = synth.generate(w, N=N, S=S, seed=rp.data_seed)
     m, haps = synth.initial_state(ds, seed=7 + rank)
     return w, m, haps
 
@@ -256,10 +258,8 @@ def run_ours(args):
     per = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     elapsed = evs[0].elapsed_time(evs[-1]) / 1e3
     ev, rounds, lanes = eng.dev.stats()
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
+    from glphase_gb300 import replicas
+    elapsed = replicas.max_elapsed(elapsed, device=dev)
     updates_step = N * (C + 1) * S
     value = world * args.steps * updates_step / elapsed
     kernel_ms = float(np.mean(per))

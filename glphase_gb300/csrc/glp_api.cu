@@ -23,6 +23,8 @@
 #include "../../include/glphase_gpu.h"
 #include "glp_kernels.cuh"
 #include "glp_knn.cuh"
+#include "glp_tally.cuh"
+
 struct glp_problem {
   glp_ctx *ctx = nullptr;
   uint32_t S = 0;  // sites of tran
@@ -1033,6 +1035,32 @@ int glp_get_stats(glp_ctx *c, uint64_t *evaluations, uint64_t *rounds, uint32_t 
     *rounds = c->last_stats[1];
   if (lanes_used)
     *lanes_used = c->lanes_used;
+  return GLP_OK;
+}
+
+int glp_tally(glp_ctx *c, const uint64_t *haps, uint32_t N, uint32_t S, uint32_t *hsum) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!haps || !hsum || N == 0 || S == 0)
+    return fail(c, GLP_ERR_ARG, "haps, hsum, num_samples and num_sites are required");
+  glp::replace_kernel<<<N, glp::kTallyThreads, 0, c->stream>>>(haps, N, S, (S + 63) / 64, hsum);
+  GLP_CUDA(c, cudaGetLastError());
+  return GLP_OK;
+}
+
+int glp_result(glp_ctx *c, const uint32_t *hsum, uint32_t N, uint32_t S, uint32_t sn,
+               float *prob_out) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!hsum || !prob_out || N == 0 || S == 0 || sn == 0)
+    return fail(c, GLP_ERR_ARG, "hsum, prob_out, sizes and sampling_generations are required");
+  const uint64_t total = (uint64_t)2 * N * S;
+  const float norm = (float)(1.0 / sn);
+  glp::result_kernel<<<(unsigned)((total + 255) / 256), 256, 0, c->stream>>>(hsum, N, S, norm,
+                                                                          prob_out);
+  GLP_CUDA(c, cudaGetLastError());
   return GLP_OK;
 }
 

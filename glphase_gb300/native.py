@@ -30,7 +30,7 @@ EXPORTED = [
     "glp_measure_fp32_peak", "glp_knn_neighbors", "glp_problem_create",
     "glp_problem_destroy", "glp_problem_set_model", "glp_problem_set_vq", "glp_run_batch",
     "glp_problem_set_model_device", "glp_batch_prepare", "glp_batch_run", "glp_batch_launch",
-    "glp_batch_destroy", "glp_run_generation_noalloc",
+    "glp_batch_destroy", "glp_run_generation_noalloc", "glp_tally", "glp_result",
 ]
 
 
@@ -114,6 +114,8 @@ def load(build_if_missing: bool = False):
     L.glp_batch_destroy.argtypes = [vp]
     L.glp_batch_destroy.restype = None
     L.glp_run_generation_noalloc.argtypes = [C.POINTER(GenerationArgs), vp, vp, vp, vp, vp]
+    L.glp_tally.argtypes = [vp, vp, u32, u32, vp]
+    L.glp_result.argtypes = [vp, vp, u32, u32, u32, vp]
     L.glp_run_batch.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs)]
     for name in EXPORTED:
         getattr(L, name)

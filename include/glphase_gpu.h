@@ -240,6 +240,21 @@ int glp_knn_neighbors(glp_ctx *ctx, const uint64_t *haps, uint32_t num_haps, uin
                       uint32_t k, double freq_lb, double freq_ub, int use_maf,
                       uint32_t *neighbors);
 
+/* Allele tallies of a sampling generation for all N samples: for each
+ * sample, hsum rows 2i and 2i+1 ([2N][S] uint32) gain the sample's two
+ * current haplotypes, in the orientation that agrees best with the tallies
+ * so far.  Replaces the Impute::replace loop of Insti::estimate
+ * (src/impute.cpp:564-595, src/insti.cpp:1710-1712).  DEVICE pointers,
+ * asynchronous. */
+int glp_tally(glp_ctx *ctx, const uint64_t *haps, uint32_t num_samples, uint32_t num_sites,
+              uint32_t *hsum);
+
+/* Allele probabilities from the tallies: prob_out [S][2N] = hsum / sn in
+ * binary32.  Replaces Impute::result (src/impute.cpp:599-613).  DEVICE
+ * pointers, asynchronous. */
+int glp_result(glp_ctx *ctx, const uint32_t *hsum, uint32_t num_samples, uint32_t num_sites,
+               uint32_t sampling_generations, float *prob_out);
+
 /* Allocation-free generation (no counterpart in the reference).
  *
  * For callers that must not allocate device memory: code whose device memory
