@@ -402,8 +402,11 @@ int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
 
 template <class Fn>
 unsigned grid_for(glp_ctx *c, Fn fn, uint64_t samples, uint32_t P, int *rc) {
+  const size_t smem = glp::stage_bytes((int)P);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, smem);
   if (e != cudaSuccess) {
     *rc = fail(c, GLP_ERR_CUDA, "occupancy query failed: %s", cudaGetErrorString(e));
     return 0;
@@ -429,7 +432,7 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
-  fn<<<grid, glp::kThreads, 0, c->stream>>>(p);
+  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P), c->stream>>>(p);
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = (uint64_t)a->num_samples * a->num_cycles;
@@ -703,7 +706,7 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
-  fn<<<grid, glp::kThreads, 0, c->stream>>>(mp);
+  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P), c->stream>>>(mp);
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = chain_cycles;
@@ -732,7 +735,7 @@ int batch_enqueue(glp_batch *b, cudaStream_t st) {
   glp_ctx *c = b->c;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), st));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), st));
-  b->fn<<<b->grid, glp::kThreads, 0, st>>>(b->mp);
+  b->fn<<<b->grid, glp::kThreads, glp::stage_bytes((int)b->P), st>>>(b->mp);
   GLP_CUDA(c, cudaGetLastError());
   glp::advance_kernel<<<(b->count + 127) / 128, 128, 0, st>>>(b->d_table, b->count);
   GLP_CUDA(c, cudaGetLastError());
@@ -1293,7 +1296,10 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   }
   SingleFn fn = single_kernel(P, false);
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, 0) != cudaSuccess)
+  const size_t smem = glp::stage_bytes((int)P);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, smem) != cudaSuccess)
     return GLP_ERR_CUDA;
   const uint64_t groups = (uint64_t)glp::kThreads / P;
   const uint64_t want = ((uint64_t)N + groups - 1) / groups;
@@ -1303,7 +1309,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   if (cudaMemsetAsync(base, 0, 256, st) != cudaSuccess)
     return GLP_ERR_CUDA;
   tran4_kernel<<<(S + 255) / 256, 256, 0, st>>>(tran, S, (float4 *)(base + tran_off));
-  fn<<<grid, glp::kThreads, 0, st>>>(p);
+  fn<<<grid, glp::kThreads, smem, st>>>(p);
   if (cudaGetLastError() != cudaSuccess)
     return GLP_ERR_CUDA;
   int h_err = 0;

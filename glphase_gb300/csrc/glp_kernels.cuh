@@ -94,6 +94,29 @@ __device__ __forceinline__ void prefetch_l1(const void *ptr) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
 }
 
+// Asynchronous global -> shared copies (cp.async): the data lands in shared
+// memory without occupying registers; cp_async_wait<n> returns once at most n
+// of this thread's committed copy groups are still in flight.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int n>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(n));
+}
+
+// Staging of 8-site blocks: one slot = 8 transition rows followed by the 8
+// sites' emission data (8 float4, or the block's VQ word in the first 4 bytes).
+constexpr int kSlotF4 = 16;
+constexpr int kRing = 3;                   // slots per stream: two blocks in flight
+constexpr int kGroupF4 = 2 * kRing * kSlotF4;  // forward + backward rings
+
 // Sites are consumed in blocks of 8 (m0 a multiple of 8): prep8(m0) readies
 // a block, get8(m0, j) returns site m0 + j for a compile-time j; get1(m) is
 // the unblocked form used on ragged tails; ahead(m) prefetches the block
@@ -109,6 +132,15 @@ struct EmitF32 {
     return __ldg(row + m0 + j);
   }
   __device__ __forceinline__ float4 get1(uint32_t m) const { return __ldg(row + m); }
+  // copy the emission of sites m0..m0+7 into dst (lane li of P)
+  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, uint32_t li,
+                                        uint32_t P) const {
+    for (uint32_t k = li; k < 8; k += P)
+      cp_async16(dst + k, row + m0 + k);
+  }
+  __device__ __forceinline__ float4 staged(const float4 *src, uint32_t j) const {
+    return src[j];
+  }
 };
 
 // 4-bit VQ codes, eight per uint32, most significant nibble first
@@ -136,6 +168,15 @@ struct EmitVQ {
   __device__ __forceinline__ float4 get1(uint32_t m) const {
     const uint32_t w = __ldg(col + (size_t)(m >> 3) * stride);
     return table[(w >> (28u - 4u * (m & 7u))) & 15u];
+  }
+  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, uint32_t li,
+                                        uint32_t) const {
+    if (li == 0)
+      cp_async4(dst, col + (size_t)(m0 >> 3) * stride);
+  }
+  __device__ __forceinline__ float4 staged(const float4 *src, uint32_t j) const {
+    const uint32_t w = *reinterpret_cast<const uint32_t *>(src);
+    return table[(w >> (28u - 4u * j)) & 15u];
   }
 };
 
@@ -289,6 +330,33 @@ __device__ __forceinline__ void fwd_block8(FState &f, const E &ef, const float4 
   }
 }
 
+// The same blocks read from a staging slot (8 transition rows, then the
+// 8 sites' emission data).
+template <class E>
+__device__ __forceinline__ void both_staged8(FState &f, BState &b, const E &ef, const E &eb,
+                                             const float4 *sf, const float4 *sb,
+                                             const Bits8 &wf, const Bits8 &wb) {
+#pragma unroll
+  for (uint32_t j = 0; j < 8; ++j) {
+    float s00, s01, s10, s11, r00, r01, r10, r11;
+    site_emission(ef.staged(sf + 8, j), wf, j, s00, s01, s10, s11);
+    site_emission(eb.staged(sb + 8, 7 - j), wb, 7 - j, r00, r01, r10, r11);
+    fwd_step(f, sf[j], s00, s01, s10, s11);
+    bwd_step(b, sb[7 - j], r00, r01, r10, r11);
+  }
+}
+
+template <class E>
+__device__ __forceinline__ void fwd_staged8(FState &f, const E &ef, const float4 *sf,
+                                            const Bits8 &wf) {
+#pragma unroll
+  for (uint32_t j = 0; j < 8; ++j) {
+    float s00, s01, s10, s11;
+    site_emission(ef.staged(sf + 8, j), wf, j, s00, s01, s10, s11);
+    fwd_step(f, sf[j], s00, s01, s10, s11);
+  }
+}
+
 // Log-likelihood of one quadruple (natural log), binary64.
 //
 // Words [0, wf) run forward and words [wf, wn) backward, two at a time in
@@ -296,7 +364,9 @@ __device__ __forceinline__ void fwd_block8(FState &f, const E &ef, const float4 
 // alone, site by site, before the rest.  With wn == 1 the single word runs
 // forward, site by site.
 template <class E>
-__device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, uint4 q) {
+__device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, uint4 q,
+                                            float4 *stage, uint32_t li, uint32_t P,
+                                            unsigned gmask) {
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tran4 = p.tran4;
   FState f;
@@ -333,54 +403,89 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
       --wb;
     }
     const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
-    // the forward stream only ever reads sites below wf*64 and the backward
-    // stream sites at or above it, so prefetches stay inside the row
-    const uint32_t fwd_end = wf * 64 - 1, bwd_lo = wf * 64;
-    if (nb) {
-      ef.ahead(0);
-      ef.ahead(8);
-      eb.ahead(wb * 64 + 56);
-      eb.ahead(wb * 64 + 48);
+    float4 *stF = stage, *stB = stage + kRing * kSlotF4;
+    // Block pairs t = 8 i + blk: forward sites i*64 + 8*blk .. +7 and
+    // backward sites (wb - i)*64 + 8*(7 - blk) .. +7, each staged into the
+    // group's shared-memory ring two pairs ahead of use.
+    const uint32_t T = nb * 8;
+    auto issue_pair = [&](uint32_t t) {
+      const uint32_t i = t >> 3, blk = t & 7u;
+      const uint32_t m0 = i * 64 + blk * 8, n0 = (wb - i) * 64 + (7 - blk) * 8;
+      float4 *sf = stF + (t % kRing) * kSlotF4, *sb = stB + (t % kRing) * kSlotF4;
+      for (uint32_t k = li; k < 8; k += P) {
+        cp_async16(sf + k, tran4 + m0 + k);
+        cp_async16(sb + k, tran4 + n0 + k);
+      }
+      ef.stage(sf + 8, m0, li, P);
+      eb.stage(sb + 8, n0, li, P);
+    };
+    if (T > 0)
+      issue_pair(0);
+    cp_async_commit();
+    if (T > 1)
+      issue_pair(1);
+    cp_async_commit();
+    Parents pf, pb;
+#pragma unroll 1
+    for (uint32_t t = 0; t < T; ++t) {
+      if (t + 2 < T)
+        issue_pair(t + 2);
+      cp_async_commit();
+      const uint32_t i = t >> 3, blk = t & 7u;
+      if (blk == 0) {
+        pf = load_parents(p.haps, wn, q, i);
+        pb = load_parents(p.haps, wn, q, wb - i);
+        if (i + 1 < nb) {  // next words' parents
+          prefetch_l1(p.haps + (size_t)q.x * wn + i + 1);
+          prefetch_l1(p.haps + (size_t)q.y * wn + i + 1);
+          prefetch_l1(p.haps + (size_t)q.z * wn + i + 1);
+          prefetch_l1(p.haps + (size_t)q.w * wn + i + 1);
+          prefetch_l1(p.haps + (size_t)q.x * wn + wb - i - 1);
+          prefetch_l1(p.haps + (size_t)q.y * wn + wb - i - 1);
+          prefetch_l1(p.haps + (size_t)q.z * wn + wb - i - 1);
+          prefetch_l1(p.haps + (size_t)q.w * wn + wb - i - 1);
+        }
+      }
+      cp_async_wait<2>();
+      __syncwarp(gmask);
+      const uint32_t slot = (t % kRing) * kSlotF4;
+      both_staged8(f, b, ef, eb, stF + slot, stB + slot, window8(pf, blk * 8),
+                   window8(pb, (7 - blk) * 8));
+      if (blk == 7) {
+        fwd_guard(f);
+        bwd_guard(b);
+      }
+      __syncwarp(gmask);
     }
+    // forward-only words [nb, wf) (wn odd, or a ragged last word)
+    const uint32_t T2 = (wf - nb) * 8;
+    auto issue_fwd = [&](uint32_t t) {
+      const uint32_t m0 = (nb + (t >> 3)) * 64 + (t & 7u) * 8;
+      float4 *sf = stF + (t % kRing) * kSlotF4;
+      for (uint32_t k = li; k < 8; k += P)
+        cp_async16(sf + k, tran4 + m0 + k);
+      ef.stage(sf + 8, m0, li, P);
+    };
+    if (T2 > 0)
+      issue_fwd(0);
+    cp_async_commit();
+    if (T2 > 1)
+      issue_fwd(1);
+    cp_async_commit();
 #pragma unroll 1
-    for (uint32_t i = 0; i < nb; ++i) {
-      const uint32_t wfw = i, wbw = wb - i;
-      const Parents pf = load_parents(p.haps, wn, q, wfw);
-      const Parents pb = load_parents(p.haps, wn, q, wbw);
-      if (i + 1 < nb) {  // next words' parents
-        prefetch_l1(p.haps + (size_t)q.x * wn + wfw + 1);
-        prefetch_l1(p.haps + (size_t)q.y * wn + wfw + 1);
-        prefetch_l1(p.haps + (size_t)q.z * wn + wfw + 1);
-        prefetch_l1(p.haps + (size_t)q.w * wn + wfw + 1);
-        prefetch_l1(p.haps + (size_t)q.x * wn + wbw - 1);
-        prefetch_l1(p.haps + (size_t)q.y * wn + wbw - 1);
-        prefetch_l1(p.haps + (size_t)q.z * wn + wbw - 1);
-        prefetch_l1(p.haps + (size_t)q.w * wn + wbw - 1);
-      }
-#pragma unroll 1
-      for (uint32_t blk = 0; blk < 8; ++blk) {
-        const uint32_t m0 = wfw * 64 + blk * 8, n0 = wbw * 64 + (7 - blk) * 8;
-        ef.ahead(min(m0 + 16, fwd_end));
-        eb.ahead(n0 >= bwd_lo + 16 ? n0 - 16 : bwd_lo);
-        ef.prep8(m0);
-        eb.prep8(n0);
-        both_block8(f, b, ef, eb, tran4, window8(pf, blk * 8), window8(pb, (7 - blk) * 8), m0,
-                    n0);
-      }
-      fwd_guard(f);
-      bwd_guard(b);
-    }
-#pragma unroll 1
-    for (uint32_t i = nb; i < wf; ++i) {
-      const Parents pf = load_parents(p.haps, wn, q, i);
-#pragma unroll 1
-      for (uint32_t blk = 0; blk < 8; ++blk) {
-        const uint32_t m0 = i * 64 + blk * 8;
-        ef.ahead(min(m0 + 16, fwd_end));
-        ef.prep8(m0);
-        fwd_block8(f, ef, tran4, window8(pf, blk * 8), m0);
-      }
-      fwd_guard(f);
+    for (uint32_t t = 0; t < T2; ++t) {
+      if (t + 2 < T2)
+        issue_fwd(t + 2);
+      cp_async_commit();
+      const uint32_t blk = t & 7u;
+      if (blk == 0)
+        pf = load_parents(p.haps, wn, q, nb + (t >> 3));
+      cp_async_wait<2>();
+      __syncwarp(gmask);
+      fwd_staged8(f, ef, stF + (t % kRing) * kSlotF4, window8(pf, blk * 8));
+      if (blk == 7)
+        fwd_guard(f);
+      __syncwarp(gmask);
     }
   }
   const double dot = (double)f.l00 * (double)b.b00 + (double)f.l01 * (double)b.b01 +
@@ -594,6 +699,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
   const uint32_t li = lane % P, gbase = lane - li;
   __shared__ Pending s_pend[kWarps][64];
   __shared__ uint32_t s_npend[kWarps];
+  extern __shared__ float4 glp_stage[];  // kWarps * (32/P) * kGroupF4 float4
   if (lane == 0)
     s_npend[warp] = 0;
   __syncwarp();
@@ -674,10 +780,16 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       set_slot(myq, slot, phap);
     }
     double L = 0.0;
-    if (on) {
+    if (active) {
+      // every lane of an active group evaluates (lanes past k score the base
+      // quadruple and drop the result) so the group shares its staging ring
       E em;
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
-      L = eval_like<E>(p, em, myq);
+      const unsigned gm = (P == 32) ? FULL : (((1u << P) - 1u) << gbase);
+      float4 *ring = glp_stage + ((size_t)warp * (32 / P) + lane / P) * kGroupF4;
+      L = eval_like<E>(p, em, myq, ring, li, (uint32_t)P, gm);
+      if (!on)
+        L = 0.0;
     }
     // The accept rule of MHSampler.hpp:86-93 in chain order.  Every
     // evaluation of the round was built on the round's starting state, and
@@ -772,6 +884,12 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
     atomicAdd(stats + 1, n_rounds);
     atomicAdd(stats + 2, n_acc);
   }
+}
+
+// Dynamic shared memory of a generation kernel with P lanes per sample: one
+// staging ring pair per group.
+__host__ __device__ constexpr size_t stage_bytes(int P) {
+  return sizeof(float4) * (size_t)kWarps * (32 / P) * kGroupF4;
 }
 
 // One chunk per launch (the reference's RunHMMOnDevice granularity).
