@@ -44,10 +44,13 @@ def parse():
     ap.add_argument("--sites", type=int, default=0, help="override S (tests)")
     ap.add_argument("--cycles", type=int, default=100)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per sample (0 = auto)")
+    ap.add_argument("--evals", type=int, default=0, help="evaluations per lane (0 = auto)")
     ap.add_argument("--vq", action="store_true", help="score with 4-bit VQ GL codes")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--uniform", action="store_true",
+                    help="uniform surrogates instead of the configuration's kNN restriction")
     ap.add_argument("--chunks", type=int, default=64, help="uneven workload: chunk count")
     ap.add_argument("--scale", type=float, default=1.0, help="uneven workload: shrink shapes")
     ap.add_argument("--requests", type=int, default=24, help="serving: request count")
@@ -77,8 +80,17 @@ def workload(args, rank):
 
 
 def pen_for(gen, burnin):
-    p = min((gen + 1.0) / burnin, 1.0)
-    return p * p
+    """Annealing penalty of generation gen (insti.cpp:1670-1671), binary32."""
+    from glphase_gb300.batch import anneal_pen
+    return float(anneal_pen(gen, burnin))
+
+
+def surrogates(seed, gen, N, C, H, nbr):
+    """The surrogates the kernel draws for generation gen, materialised on
+    the host for the CPU reference (same counter-based streams)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    return O.sample_surrogates(seed, gen, N, C, 0, H, nbr=nbr)
 
 
 class ClockSampler:
@@ -203,36 +215,41 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    from glphase_gb300 import native as nat, synth
+    from glphase_gb300 import native as nat, replicas, synth
     from glphase_gb300.hmmlike import Engine
 
     w, m, haps = workload(args, rank)
     C = args.cycles
     N, S = m.N, m.S
     H, wn = haps.shape
-    rng = np.random.default_rng(5 + rank)
     packed = codebook = None
     if args.vq:
         from glphase_gb300.glpack import GLPack
         gp = GLPack(m.t, np.random.default_rng(1))
         packed, codebook = gp.packed_gls(), gp.code_book()
     eng = Engine(m.emit, m.t, m.tran, m.pc, haps, C, device=local, lanes=args.lanes,
-                 packed=packed, codebook=codebook)
+                 packed=packed, codebook=codebook, evals=args.evals)
     dev = torch.device("cuda", local)
-    total = args.warmup + args.steps
-    # every step's inputs are staged in HBM before timing starts
-    quads, propss = [], []
-    for g in range(total):
-        q, p = synth.uniform_proposals(N, H, C, rng)
-        quads.append(torch.from_numpy(q.view(np.int32)).to(dev))
-        propss.append(torch.from_numpy(p.view(np.int32)).to(dev))
     torch.cuda.synchronize()
+    # surrogate restriction: the K nearest haplotypes by Hamming distance
+    # (KNN::ClusterHaps) computed once on the device from the starting
+    # haplotypes; every generation then draws its surrogates in the kernel
+    nbr, knn_ms = None, None
+    if w.knn and not args.uniform:
+        k0 = torch.cuda.Event(enable_timing=True)
+        k1 = torch.cuda.Event(enable_timing=True)
+        k0.record(eng.stream)
+        nbr = eng.knn(w.knn)
+        k1.record(eng.stream)
+        eng.finish()
+        knn_ms = k0.elapsed_time(k1)
     peak = C_.c_double()
     eng.dev._c(eng.dev.L.glp_measure_fp32_peak(eng.dev.ctx, 200.0, C_.byref(peak)))
     stream = eng.stream
+    seed = replicas.plan(w.seed, rank=rank, world=max(world, rank + 1)).rng_seed
 
     def step(g):
-        a = eng.args(quads[g], propss[g], pen_for(g, w.burnin), seed=1234 + rank, generation=g)
+        a = eng.args(None, None, pen_for(g, w.burnin), seed=seed, generation=g, neighbors=nbr)
         eng.launch(a)
         eng.swap()
 
@@ -258,21 +275,26 @@ def run_ours(args):
     per = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     elapsed = evs[0].elapsed_time(evs[-1]) / 1e3
     ev, rounds, lanes = eng.dev.stats()
-    from glphase_gb300 import replicas
     elapsed = replicas.max_elapsed(elapsed, device=dev)
     updates_step = N * (C + 1) * S
     value = world * args.steps * updates_step / elapsed
     kernel_ms = float(np.mean(per))
     achieved = updates_step * FLOPS_PER_UPDATE / (kernel_ms * 1e-3) / 1e12
 
+    nbr_host = None if nbr is None else np.ascontiguousarray(
+        nbr.cpu().numpy().view(np.uint32)[:N])
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(eng, haps, N, S, C, H, wn, w, args, torch)
+        e2e = run_e2e(eng, haps, N, S, C, H, wn, w, args, torch, nbr_host)
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:
-        q0, p0 = synth.uniform_proposals(N, H, C, np.random.default_rng(99))
+        # the same surrogates the kernel draws, at full penalty
+        q0, p0 = surrogates(seed, args.warmup, N, C, H, nbr_host)
         base, _ = cpu_baseline(m, haps, q0, p0, C, 1.0, args.cpu_seconds)
+    sampler = (f"kNN K={w.knn} nearest by Hamming distance, device-built once "
+               f"({knn_ms:.1f} ms), drawn in-kernel" if nbr is not None
+               else "uniform over all other haplotypes, drawn in-kernel")
 
     if rank == 0:
         line = {
@@ -282,10 +304,12 @@ def run_ours(args):
             "data": "synthetic",
             "config": {
                 "workload": f"{args.config}: {N} samples x {S} sites x C={C} cycles per "
-                            "generation, uniform surrogates over all other haplotypes",
+                            f"generation, surrogates {sampler}",
                 "samples": N, "sites": S, "cycles": C, "haplotypes": H,
                 "emission": "vq4" if args.vq else "f32",
-                "lanes_per_sample": lanes, "evaluations_per_step": ev,
+                "lanes_per_sample": lanes,
+                "evals_per_lane": 2 if args.evals == 2 and lanes in (2, 4, 8) else 1,
+                "evaluations_per_step": ev,
                 "speculative_rounds": rounds,
                 "useful_fraction": round(N * (C + 1) / max(ev, 1), 4),
                 "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6),
@@ -308,11 +332,11 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def run_e2e(eng, haps, N, S, C, H, wn, w, args, torch):
+def run_e2e(eng, haps, N, S, C, H, wn, w, args, torch, nbr_host):
     """Same metric through the host-pointer C-ABI call: every step copies the
-    haplotypes, quadruples and proposals in from pinned host memory and the
-    quadruples, the new haplotype rows and the log-likelihoods back."""
-    from glphase_gb300 import synth
+    haplotypes (and the kNN table, when used) in from pinned host memory and
+    the quadruples, the new haplotype rows and the log-likelihoods back; the
+    surrogates are drawn in the kernel as in the device-resident run."""
 
     def pinned(shape, dtype):
         t = torch.empty(shape, dtype=dtype, pin_memory=True)
@@ -322,31 +346,24 @@ def run_e2e(eng, haps, N, S, C, H, wn, w, args, torch):
     h[:] = haps
     hn = pinned((H, wn), torch.int64).view(np.uint64)
     hn[:] = haps
-    rng = np.random.default_rng(17)
-    qs, ps = [], []
-    total = args.warmup + args.steps
-    for g in range(total):
-        q, p = synth.uniform_proposals(N, H, C, rng)
-        qq = pinned((4, N), torch.int32).view(np.uint32)
-        qq[:] = q
-        pp = pinned((C, N), torch.int32).view(np.uint32)
-        pp[:] = p
-        qs.append(qq)
-        ps.append(pp)
+    nb = None
+    if nbr_host is not None:
+        nb = pinned(nbr_host.shape, torch.int32).view(np.uint32)
+        nb[:] = nbr_host
     qout = pinned((4, N), torch.int32).view(np.uint32)
     like = pinned((N,), torch.float64)
     cur, nxt = h, hn
     for g in range(args.warmup):
-        eng.run_host(cur, qs[g], ps[g], pen_for(g, w.burnin), 99, g, nxt, qout, like)
+        eng.run_host(cur, None, None, pen_for(g, w.burnin), 99, g, nxt, qout, like, nb)
         nxt[2 * N:] = cur[2 * N:]
         cur, nxt = nxt, cur
     t0 = time.perf_counter()
     for i in range(args.steps):
         g = args.warmup + i
-        eng.run_host(cur, qs[g], ps[g], pen_for(g, w.burnin), 99, g, nxt, qout, like)
+        eng.run_host(cur, None, None, pen_for(g, w.burnin), 99, g, nxt, qout, like, nb)
         cur, nxt = nxt, cur
     dt = time.perf_counter() - t0
-    h2d = H * wn * 8 + 4 * N * 4 + C * N * 4
+    h2d = H * wn * 8 + (0 if nb is None else nb.nbytes)
     d2h = 4 * N * 4 + 2 * N * wn * 8 + N * 8
     return {"value": args.steps * N * (C + 1) * S / dt, "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

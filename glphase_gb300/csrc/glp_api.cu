@@ -75,6 +75,7 @@ struct glp_ctx {
          tr_work_cap = 0;
   // tuning and statistics
   uint32_t lanes = 0;  // 0 = automatic
+  uint32_t evals = 0;  // evaluations per lane and round, 0 = automatic
   uint32_t lanes_used = 4;
   double last_accept = -1.0;  // acceptance rate of the last generation
   uint64_t last_chain_cycles = 0;
@@ -253,34 +254,54 @@ int set_emission(glp_problem *pb, const float *emit, const float *prob, uint32_t
 using SingleFn = void (*)(const glp::GenParams);
 using MultiFn = void (*)(const glp::MultiParams);
 
-template <int P>
+template <int P, int V>
 SingleFn single_for(bool vq) {
-  return vq ? glp::generation_kernel<P, glp::EmitVQ> : glp::generation_kernel<P, glp::EmitF32>;
+  return vq ? glp::generation_kernel<P, V, glp::EmitVQ>
+            : glp::generation_kernel<P, V, glp::EmitF32>;
 }
-template <int P>
+template <int P, int V>
 MultiFn multi_for(bool vq) {
-  return vq ? glp::generation_multi_kernel<P, glp::EmitVQ>
-            : glp::generation_multi_kernel<P, glp::EmitF32>;
+  return vq ? glp::generation_multi_kernel<P, V, glp::EmitVQ>
+            : glp::generation_multi_kernel<P, V, glp::EmitF32>;
 }
 
-SingleFn single_kernel(uint32_t lanes, bool vq) {
-  switch (lanes) {
-    case 1: return single_for<1>(vq);
-    case 2: return single_for<2>(vq);
-    case 4: return single_for<4>(vq);
-    case 8: return single_for<8>(vq);
-    case 16: return single_for<16>(vq);
-    default: return single_for<32>(vq);
+// Speculation shape of a launch: P lanes per sample, V evaluations per lane.
+struct Shape {
+  uint32_t P = 1, V = 1;
+};
+
+SingleFn single_kernel(Shape sh, bool vq) {
+  if (sh.V == 2) {
+    switch (sh.P) {
+      case 2: return single_for<2, 2>(vq);
+      case 4: return single_for<4, 2>(vq);
+      default: return single_for<8, 2>(vq);
+    }
+  }
+  switch (sh.P) {
+    case 1: return single_for<1, 1>(vq);
+    case 2: return single_for<2, 1>(vq);
+    case 4: return single_for<4, 1>(vq);
+    case 8: return single_for<8, 1>(vq);
+    case 16: return single_for<16, 1>(vq);
+    default: return single_for<32, 1>(vq);
   }
 }
-MultiFn multi_kernel(uint32_t lanes, bool vq) {
-  switch (lanes) {
-    case 1: return multi_for<1>(vq);
-    case 2: return multi_for<2>(vq);
-    case 4: return multi_for<4>(vq);
-    case 8: return multi_for<8>(vq);
-    case 16: return multi_for<16>(vq);
-    default: return multi_for<32>(vq);
+MultiFn multi_kernel(Shape sh, bool vq) {
+  if (sh.V == 2) {
+    switch (sh.P) {
+      case 2: return multi_for<2, 2>(vq);
+      case 4: return multi_for<4, 2>(vq);
+      default: return multi_for<8, 2>(vq);
+    }
+  }
+  switch (sh.P) {
+    case 1: return multi_for<1, 1>(vq);
+    case 2: return multi_for<2, 1>(vq);
+    case 4: return multi_for<4, 1>(vq);
+    case 8: return multi_for<8, 1>(vq);
+    case 16: return multi_for<16, 1>(vq);
+    default: return multi_for<32, 1>(vq);
   }
 }
 
@@ -304,6 +325,15 @@ uint32_t choose_lanes(const glp_ctx *c, uint64_t N) {
     }
   }
   return best;
+}
+
+// Lanes from choose_lanes; two evaluations per lane only on request
+// (glp_set_evals_per_lane), and only where that kernel exists (P = 2, 4, 8).
+Shape choose_shape(const glp_ctx *c, uint64_t N) {
+  Shape sh;
+  sh.P = choose_lanes(c, N);
+  sh.V = (c->evals == 2 && (sh.P == 2 || sh.P == 4 || sh.P == 8)) ? 2u : 1u;
+  return sh;
 }
 
 // Validate one (problem, generation) pair and fill its kernel descriptor.
@@ -425,8 +455,9 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
   if (rc)
     return rc;
   const bool vq = (a->flags & GLP_GEN_VQ) != 0;
-  const uint32_t P = choose_lanes(c, a->num_samples);
-  SingleFn fn = single_kernel(P, vq);
+  const Shape sh = choose_shape(c, a->num_samples);
+  const uint32_t P = sh.P;
+  SingleFn fn = single_kernel(sh, vq);
   const unsigned grid = grid_for(c, fn, a->num_samples, P, &rc);
   if (rc)
     return rc;
@@ -699,8 +730,9 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   mp.counter = c->d_counter;
   mp.stats = c->d_stats;
   mp.error = c->d_error;
-  const uint32_t P = choose_lanes(c, total);
-  MultiFn fn = multi_kernel(P, vq);
+  const Shape sh = choose_shape(c, total);
+  const uint32_t P = sh.P;
+  MultiFn fn = multi_kernel(sh, vq);
   const unsigned grid = grid_for(c, fn, total, P, &rc);
   if (rc)
     return rc;
@@ -818,8 +850,9 @@ int glp_batch_prepare(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   b->mp.counter = c->d_counter;
   b->mp.stats = c->d_stats;
   b->mp.error = c->d_error;
-  b->P = choose_lanes(c, total);
-  b->fn = multi_kernel(b->P, vq);
+  const Shape sh = choose_shape(c, total);
+  b->P = sh.P;
+  b->fn = multi_kernel(sh, vq);
   b->grid = grid_for(c, b->fn, total, b->P, &rc);
   if (rc)
     return bail(rc);
@@ -1026,6 +1059,15 @@ int glp_set_lanes_per_sample(glp_ctx *c, uint32_t lanes) {
       lanes != 32)
     return fail(c, GLP_ERR_ARG, "lanes per sample must be 0, 1, 2, 4, 8, 16 or 32");
   c->lanes = lanes;
+  return GLP_OK;
+}
+
+int glp_set_evals_per_lane(glp_ctx *c, uint32_t evals) {
+  if (!c)
+    return GLP_ERR_ARG;
+  if (evals > 2)
+    return fail(c, GLP_ERR_ARG, "evaluations per lane must be 0, 1 or 2");
+  c->evals = evals;
   return GLP_OK;
 }
 
@@ -1294,7 +1336,9 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
       P = w;
     }
   }
-  SingleFn fn = single_kernel(P, false);
+  Shape sh;
+  sh.P = P;
+  SingleFn fn = single_kernel(sh, false);
   int occ = 0;
   const size_t smem = glp::stage_bytes((int)P);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=

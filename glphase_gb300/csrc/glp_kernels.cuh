@@ -116,6 +116,9 @@ __device__ __forceinline__ void cp_async_wait() {
 constexpr int kSlotF4 = 16;
 constexpr int kRing = 3;                   // slots per stream: two blocks in flight
 constexpr int kGroupF4 = 2 * kRing * kSlotF4;  // forward + backward rings
+// Rings of neighbouring groups are kGroupF4 + 1 float4 apart, so the 16-byte
+// reads of the 8 groups of a warp start 4 banks apart and never conflict.
+constexpr int kGroupStrideF4 = kGroupF4 + 1;
 
 // Sites are consumed in blocks of 8 (m0 a multiple of 8): prep8(m0) readies
 // a block, get8(m0, j) returns site m0 + j for a compile-time j; get1(m) is
@@ -302,111 +305,114 @@ __device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, u
           s00, s01, s10, s11);
 }
 
-// Forward over the 8 sites m0..m0+7 and backward over n0+7..n0 (both blocks
-// full), interleaved: 8 independent FMA chains per lane.
-template <class E>
-__device__ __forceinline__ void both_block8(FState &f, BState &b, const E &ef, const E &eb,
-                                            const float4 *tran4, const Bits8 &wf,
-                                            const Bits8 &wb, uint32_t m0, uint32_t n0) {
+// One staged block pair for V quadruples: forward over the 8 sites of slot
+// sf, backward over the 8 sites of slot sb (highest first).  Every staged
+// emission and transition row is read once and used by all V quadruples:
+// 8 V independent FMA chains per lane.
+template <int V, class E>
+__device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], const E &ef,
+                                             const E &eb, const float4 *sf, const float4 *sb,
+                                             const Bits8 (&wf)[V], const Bits8 (&wb)[V]) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
-    float s00, s01, s10, s11, r00, r01, r10, r11;
-    site_emission(ef.get8(m0, j), wf, j, s00, s01, s10, s11);
-    site_emission(eb.get8(n0, 7 - j), wb, 7 - j, r00, r01, r10, r11);
-    const float4 tf = __ldg(tran4 + m0 + j), tb = __ldg(tran4 + n0 + 7 - j);
-    fwd_step(f, tf, s00, s01, s10, s11);
-    bwd_step(b, tb, r00, r01, r10, r11);
+    const float4 ex = ef.staged(sf + 8, j), ey = eb.staged(sb + 8, 7 - j);
+    const float4 tx = sf[j], ty = sb[7 - j];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      float s00, s01, s10, s11, r00, r01, r10, r11;
+      site_emission(ex, wf[v], j, s00, s01, s10, s11);
+      site_emission(ey, wb[v], 7 - j, r00, r01, r10, r11);
+      fwd_step(f[v], tx, s00, s01, s10, s11);
+      bwd_step(b[v], ty, r00, r01, r10, r11);
+    }
   }
 }
 
-template <class E>
-__device__ __forceinline__ void fwd_block8(FState &f, const E &ef, const float4 *tran4,
-                                           const Bits8 &wf, uint32_t m0) {
+template <int V, class E>
+__device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const float4 *sf,
+                                            const Bits8 (&wf)[V]) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
-    float s00, s01, s10, s11;
-    site_emission(ef.get8(m0, j), wf, j, s00, s01, s10, s11);
-    fwd_step(f, __ldg(tran4 + m0 + j), s00, s01, s10, s11);
+    const float4 ex = ef.staged(sf + 8, j), tx = sf[j];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      float s00, s01, s10, s11;
+      site_emission(ex, wf[v], j, s00, s01, s10, s11);
+      fwd_step(f[v], tx, s00, s01, s10, s11);
+    }
   }
 }
 
-// The same blocks read from a staging slot (8 transition rows, then the
-// 8 sites' emission data).
-template <class E>
-__device__ __forceinline__ void both_staged8(FState &f, BState &b, const E &ef, const E &eb,
-                                             const float4 *sf, const float4 *sb,
-                                             const Bits8 &wf, const Bits8 &wb) {
-#pragma unroll
-  for (uint32_t j = 0; j < 8; ++j) {
-    float s00, s01, s10, s11, r00, r01, r10, r11;
-    site_emission(ef.staged(sf + 8, j), wf, j, s00, s01, s10, s11);
-    site_emission(eb.staged(sb + 8, 7 - j), wb, 7 - j, r00, r01, r10, r11);
-    fwd_step(f, sf[j], s00, s01, s10, s11);
-    bwd_step(b, sb[7 - j], r00, r01, r10, r11);
-  }
+__device__ __forceinline__ void prefetch_parents(const uint64_t *haps, uint32_t wn, uint4 q,
+                                                 uint32_t w) {
+  prefetch_l1(haps + (size_t)q.x * wn + w);
+  prefetch_l1(haps + (size_t)q.y * wn + w);
+  prefetch_l1(haps + (size_t)q.z * wn + w);
+  prefetch_l1(haps + (size_t)q.w * wn + w);
 }
 
-template <class E>
-__device__ __forceinline__ void fwd_staged8(FState &f, const E &ef, const float4 *sf,
-                                            const Bits8 &wf) {
-#pragma unroll
-  for (uint32_t j = 0; j < 8; ++j) {
-    float s00, s01, s10, s11;
-    site_emission(ef.staged(sf + 8, j), wf, j, s00, s01, s10, s11);
-    fwd_step(f, sf[j], s00, s01, s10, s11);
-  }
-}
-
-// Log-likelihood of one quadruple (natural log), binary64.
+// Log-likelihoods (natural log, binary64) of V quadruples of one sample.
 //
-// Words [0, wf) run forward and words [wf, wn) backward, two at a time in
-// one instruction stream; a ragged last word (S % 64 != 0) runs backward
-// alone, site by site, before the rest.  With wn == 1 the single word runs
-// forward, site by site.
-template <class E>
-__device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, uint4 q,
-                                            float4 *stage, uint32_t li, uint32_t P,
-                                            unsigned gmask) {
+// Words [0, wf) run forward and words [wf, wn) backward, one block of 8
+// sites of each at a time, in one instruction stream; the blocks' emission
+// and transition rows are staged by the P lanes of the group into the
+// group's shared-memory ring two block pairs ahead (cp.async), so the
+// arithmetic reads shared memory only.  A ragged last word (S % 64 != 0)
+// runs backward alone, site by site, before the rest; with wn == 1 the
+// single word runs forward, site by site.  All P lanes of the group call
+// this together (gmask).
+template <int V, class E>
+__device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
+                                          const uint4 (&q)[V], float4 *stage, uint32_t li,
+                                          uint32_t P, unsigned gmask, double (&out)[V]) {
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tran4 = p.tran4;
-  FState f;
-  f.l00 = f.l01 = f.l10 = f.l11 = 0.25f;
-  f.p1 = f.p2 = 0.5f;
-  f.k = 0;
-  BState b;
-  b.b00 = b.b01 = b.b10 = b.b11 = 1.0f;
-  b.k = 0;
+  FState f[V];
+  BState b[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    f[v].l00 = f[v].l01 = f[v].l10 = f[v].l11 = 0.25f;
+    f[v].p1 = f[v].p2 = 0.5f;
+    f[v].k = 0;
+    b[v].b00 = b[v].b01 = b[v].b10 = b[v].b11 = 1.0f;
+    b[v].k = 0;
+  }
   E ef = em0, eb = em0;
   if (wn == 1) {
-    const Parents pw = load_parents(p.haps, wn, q, 0);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const Parents pw = load_parents(p.haps, wn, q[v], 0);
 #pragma unroll 1
-    for (uint32_t m = 0; m < S; ++m) {
-      float s00, s01, s10, s11;
-      select4(ef.get1(m), (pw.f0 >> m) & 1, (pw.f1 >> m) & 1, (pw.m0 >> m) & 1,
-              (pw.m1 >> m) & 1, s00, s01, s10, s11);
-      fwd_step(f, __ldg(tran4 + m), s00, s01, s10, s11);
+      for (uint32_t m = 0; m < S; ++m) {
+        float s00, s01, s10, s11;
+        select4(ef.get1(m), (pw.f0 >> m) & 1, (pw.f1 >> m) & 1, (pw.m0 >> m) & 1,
+                (pw.m1 >> m) & 1, s00, s01, s10, s11);
+        fwd_step(f[v], __ldg(tran4 + m), s00, s01, s10, s11);
+      }
     }
   } else {
     const uint32_t wf = (wn + 1) >> 1;
     uint32_t wb = wn - 1;
     if (S & 63u) {
-      const Parents pw = load_parents(p.haps, wn, q, wb);
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const Parents pw = load_parents(p.haps, wn, q[v], wb);
 #pragma unroll 1
-      for (int m = (int)S - 1; m >= (int)(wb * 64); --m) {
-        const uint32_t j = (uint32_t)m & 63u;
-        float s00, s01, s10, s11;
-        select4(eb.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
-                (pw.m1 >> j) & 1, s00, s01, s10, s11);
-        bwd_step(b, __ldg(tran4 + m), s00, s01, s10, s11);
+        for (int m = (int)S - 1; m >= (int)(wb * 64); --m) {
+          const uint32_t j = (uint32_t)m & 63u;
+          float s00, s01, s10, s11;
+          select4(eb.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1,
+                  (pw.m0 >> j) & 1, (pw.m1 >> j) & 1, s00, s01, s10, s11);
+          bwd_step(b[v], __ldg(tran4 + m), s00, s01, s10, s11);
+        }
+        bwd_guard(b[v]);
       }
-      bwd_guard(b);
       --wb;
     }
     const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
     float4 *stF = stage, *stB = stage + kRing * kSlotF4;
     // Block pairs t = 8 i + blk: forward sites i*64 + 8*blk .. +7 and
-    // backward sites (wb - i)*64 + 8*(7 - blk) .. +7, each staged into the
-    // group's shared-memory ring two pairs ahead of use.
+    // backward sites (wb - i)*64 + 8*(7 - blk) .. +7.
     const uint32_t T = nb * 8;
     auto issue_pair = [&](uint32_t t) {
       const uint32_t i = t >> 3, blk = t & 7u;
@@ -425,7 +431,7 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
     if (T > 1)
       issue_pair(1);
     cp_async_commit();
-    Parents pf, pb;
+    Parents pf[V], pb[V];
 #pragma unroll 1
     for (uint32_t t = 0; t < T; ++t) {
       if (t + 2 < T)
@@ -433,27 +439,32 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
       cp_async_commit();
       const uint32_t i = t >> 3, blk = t & 7u;
       if (blk == 0) {
-        pf = load_parents(p.haps, wn, q, i);
-        pb = load_parents(p.haps, wn, q, wb - i);
-        if (i + 1 < nb) {  // next words' parents
-          prefetch_l1(p.haps + (size_t)q.x * wn + i + 1);
-          prefetch_l1(p.haps + (size_t)q.y * wn + i + 1);
-          prefetch_l1(p.haps + (size_t)q.z * wn + i + 1);
-          prefetch_l1(p.haps + (size_t)q.w * wn + i + 1);
-          prefetch_l1(p.haps + (size_t)q.x * wn + wb - i - 1);
-          prefetch_l1(p.haps + (size_t)q.y * wn + wb - i - 1);
-          prefetch_l1(p.haps + (size_t)q.z * wn + wb - i - 1);
-          prefetch_l1(p.haps + (size_t)q.w * wn + wb - i - 1);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          pf[v] = load_parents(p.haps, wn, q[v], i);
+          pb[v] = load_parents(p.haps, wn, q[v], wb - i);
+          if (i + 1 < nb) {  // next words' parents
+            prefetch_parents(p.haps, wn, q[v], i + 1);
+            prefetch_parents(p.haps, wn, q[v], wb - i - 1);
+          }
         }
+      }
+      Bits8 xf[V], xb[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        xf[v] = window8(pf[v], blk * 8);
+        xb[v] = window8(pb[v], (7 - blk) * 8);
       }
       cp_async_wait<2>();
       __syncwarp(gmask);
       const uint32_t slot = (t % kRing) * kSlotF4;
-      both_staged8(f, b, ef, eb, stF + slot, stB + slot, window8(pf, blk * 8),
-                   window8(pb, (7 - blk) * 8));
+      both_staged8<V>(f, b, ef, eb, stF + slot, stB + slot, xf, xb);
       if (blk == 7) {
-        fwd_guard(f);
-        bwd_guard(b);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          fwd_guard(f[v]);
+          bwd_guard(b[v]);
+        }
       }
       __syncwarp(gmask);
     }
@@ -478,19 +489,32 @@ __device__ __forceinline__ double eval_like(const GenParams &p, const E &em0, ui
         issue_fwd(t + 2);
       cp_async_commit();
       const uint32_t blk = t & 7u;
-      if (blk == 0)
-        pf = load_parents(p.haps, wn, q, nb + (t >> 3));
+      if (blk == 0) {
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+          pf[v] = load_parents(p.haps, wn, q[v], nb + (t >> 3));
+      }
+      Bits8 xf[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        xf[v] = window8(pf[v], blk * 8);
       cp_async_wait<2>();
       __syncwarp(gmask);
-      fwd_staged8(f, ef, stF + (t % kRing) * kSlotF4, window8(pf, blk * 8));
-      if (blk == 7)
-        fwd_guard(f);
+      fwd_staged8<V>(f, ef, stF + (t % kRing) * kSlotF4, xf);
+      if (blk == 7) {
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+          fwd_guard(f[v]);
+      }
       __syncwarp(gmask);
     }
   }
-  const double dot = (double)f.l00 * (double)b.b00 + (double)f.l01 * (double)b.b01 +
-                     (double)f.l10 * (double)b.b10 + (double)f.l11 * (double)b.b11;
-  return log(dot) + (double)(f.k + b.k) * 0.69314718055994530942;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const double dot = (double)f[v].l00 * (double)b[v].b00 + (double)f[v].l01 * (double)b[v].b01 +
+                       (double)f[v].l10 * (double)b[v].b10 + (double)f[v].l11 * (double)b[v].b11;
+    out[v] = log(dot) + (double)(f[v].k + b[v].k) * 0.69314718055994530942;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -689,17 +713,18 @@ struct ManyChunks {
   }
 };
 
-template <int P, class E, class Src>
+template <int P, int V, class E, class Src>
 __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counter,
                                                 unsigned long long *stats, int *error,
                                                 const float4 *vq_smem, const float *pc_smem) {
   static_assert(P == 1 || P == 2 || P == 4 || P == 8 || P == 16 || P == 32, "P");
+  static_assert(V == 1 || V == 2, "V");
   constexpr unsigned FULL = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t li = lane % P, gbase = lane - li;
   __shared__ Pending s_pend[kWarps][64];
   __shared__ uint32_t s_npend[kWarps];
-  extern __shared__ float4 glp_stage[];  // kWarps * (32/P) * kGroupF4 float4
+  extern __shared__ float4 glp_stage[];  // kWarps * (32/P) * kGroupStrideF4 float4
   if (lane == 0)
     s_npend[warp] = 0;
   __syncwarp();
@@ -755,59 +780,90 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
 
     const GenParams &p = src.chunk(c);
     const uint32_t N = p.N, C = p.C, H = p.H;
-    // one speculative round: lane li scores evaluation e + li
-    const uint32_t k = active ? min((uint32_t)P, C + 1 - e) : 0u;
-    const uint32_t ev = e + li;
-    const bool on = li < k;
-    uint32_t slot = 0, phap = 0;
-    double u = 0.0;
-    uint4 myq = q;
-    if (on && ev > 0) {
-      const uint32_t cyc = ev - 1;
-      if (p.tr_slot) {
-        slot = p.tr_slot[(size_t)s * C + cyc] & 3u;
-        u = p.tr_u[(size_t)s * C + cyc];
-      } else {
-        glp_mh_draw(p.seed, p.generation, s, cyc, &slot, &u);
+    // one speculative round of P V evaluations: lane li scores evaluations
+    // e + li V + v, v < V (round position r = li V + v)
+    constexpr uint32_t PV = (uint32_t)(P * V);
+    const uint32_t k = active ? min(PV, C + 1 - e) : 0u;
+    uint32_t slot[V], phap[V];
+    double u[V];
+    uint4 myq[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const uint32_t r = li * V + v, ev = e + r;
+      slot[v] = 0;
+      phap[v] = 0;
+      u[v] = 0.0;
+      myq[v] = q;
+      if (r < k && ev > 0) {
+        const uint32_t cyc = ev - 1;
+        if (p.tr_slot) {
+          slot[v] = p.tr_slot[(size_t)s * C + cyc] & 3u;
+          u[v] = p.tr_u[(size_t)s * C + cyc];
+        } else {
+          glp_mh_draw(p.seed, p.generation, s, cyc, &slot[v], &u[v]);
+        }
+        phap[v] = p.props ? __ldg(p.props + (size_t)cyc * N + s)
+                          : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP,
+                                          p.samp_lo, p.samp_hi, p.nbr, p.klen);
+        if (phap[v] >= H) {
+          atomicOr(error, 1);
+          phap[v] = 0;
+        }
+        set_slot(myq[v], slot[v], phap[v]);
       }
-      phap = p.props ? __ldg(p.props + (size_t)cyc * N + s)
-                     : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP, p.samp_lo,
-                                     p.samp_hi, p.nbr, p.klen);
-      if (phap >= H) {
-        atomicOr(error, 1);
-        phap = 0;
-      }
-      set_slot(myq, slot, phap);
     }
-    double L = 0.0;
+    double L[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+      L[v] = 0.0;
     if (active) {
-      // every lane of an active group evaluates (lanes past k score the base
-      // quadruple and drop the result) so the group shares its staging ring
+      // every lane of an active group evaluates (positions past k score the
+      // base quadruple and drop the result) so the group shares its ring
       E em;
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
       const unsigned gm = (P == 32) ? FULL : (((1u << P) - 1u) << gbase);
-      float4 *ring = glp_stage + ((size_t)warp * (32 / P) + lane / P) * kGroupF4;
-      L = eval_like<E>(p, em, myq, ring, li, (uint32_t)P, gm);
-      if (!on)
-        L = 0.0;
+      float4 *ring = glp_stage + ((size_t)warp * (32 / P) + lane / P) * kGroupStrideF4;
+      eval_like<V, E>(p, em, myq, ring, li, (uint32_t)P, gm, L);
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        if (li * V + v >= k)
+          L[v] = 0.0;
     }
     // The accept rule of MHSampler.hpp:86-93 in chain order.  Every
     // evaluation of the round was built on the round's starting state, and
     // until the first acceptance the chain's current likelihood is the
-    // starting one, so each lane tests its own proposal against it in
-    // parallel and the first accepting lane (in chain order) wins: the same
-    // decisions as the sequential loop, one binary64 exp per lane.
-    const double L0 = __shfl_sync(FULL, L, gbase);
+    // starting one, so each position tests its own proposal against it in
+    // parallel and the first accepting position (in chain order) wins: the
+    // same decisions as the sequential loop.  A lane's first accepting
+    // position is its candidate; the group's lowest candidate lane wins.
+    const double L0 = __shfl_sync(FULL, L[0], gbase);
     const double curr0 = (e == 0) ? L0 : curr;
-    const bool acc = on && ev > 0 &&
-                     (L >= curr0 || u < exp((L - curr0) * (double)p.pen));
+    uint32_t vfirst = V;
+#pragma unroll
+    for (int v = V - 1; v >= 0; --v) {
+      const uint32_t r = li * V + v;
+      const bool acc = r < k && e + r > 0 &&
+                       (L[v] >= curr0 || u[v] < exp((L[v] - curr0) * (double)p.pen));
+      if (acc)
+        vfirst = (uint32_t)v;
+    }
     const unsigned gmask = (P == 32) ? FULL : (((1u << P) - 1u) << gbase);
-    const unsigned abal = __ballot_sync(FULL, acc) & gmask;
-    const uint32_t first_acc = abal ? (uint32_t)(__ffs(abal) - 1) - gbase : (uint32_t)P;
-    const uint32_t srcl = gbase + (abal ? first_acc : 0u);
-    const double La = __shfl_sync(FULL, L, srcl);
-    const uint32_t sla = __shfl_sync(FULL, slot, srcl);
-    const uint32_t pha = __shfl_sync(FULL, phap, srcl);
+    const unsigned abal = __ballot_sync(FULL, vfirst < (uint32_t)V) & gmask;
+    const uint32_t srcl = abal ? (uint32_t)(__ffs(abal) - 1) : gbase;
+    const uint32_t vw = __shfl_sync(FULL, vfirst, srcl);
+    const uint32_t first_acc = abal ? (srcl - gbase) * V + vw : PV;
+    double Lw = L[0];
+    uint32_t slw = slot[0], phw = phap[0];
+#pragma unroll
+    for (int v = 1; v < V; ++v)
+      if ((uint32_t)v == vw) {
+        Lw = L[v];
+        slw = slot[v];
+        phw = phap[v];
+      }
+    const double La = __shfl_sync(FULL, Lw, srcl);
+    const uint32_t sla = __shfl_sync(FULL, slw, srcl);
+    const uint32_t pha = __shfl_sync(FULL, phw, srcl);
     if (active) {
       curr = curr0;
       if (abal) {
@@ -815,19 +871,22 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
         curr = La;
       }
     }
-    if (on) {
-      const bool valid = li <= first_acc;
-      if (valid && p.eval_trace)
-        p.eval_trace[(size_t)s * (C + 1) + ev] = L;
-      if (valid && ev > 0 && p.accept_trace)
-        p.accept_trace[(size_t)s * C + ev - 1] = (uint8_t)(li == first_acc);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const uint32_t r = li * V + v, ev = e + r;
+      if (r < k && r <= first_acc) {
+        if (p.eval_trace)
+          p.eval_trace[(size_t)s * (C + 1) + ev] = L[v];
+        if (ev > 0 && p.accept_trace)
+          p.accept_trace[(size_t)s * C + ev - 1] = (uint8_t)(r == first_acc);
+      }
     }
     if (active) {
-      e = (first_acc < (uint32_t)P) ? e + first_acc + 1 : e + k;
+      e = (first_acc < PV) ? e + first_acc + 1 : e + k;
       if (li == 0) {
         n_evals += k;
         ++n_rounds;
-        n_acc += first_acc < (uint32_t)P ? 1u : 0u;
+        n_acc += first_acc < PV ? 1u : 0u;
       }
     }
 
@@ -889,11 +948,12 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
 // Dynamic shared memory of a generation kernel with P lanes per sample: one
 // staging ring pair per group.
 __host__ __device__ constexpr size_t stage_bytes(int P) {
-  return sizeof(float4) * (size_t)kWarps * (32 / P) * kGroupF4;
+  return sizeof(float4) * (size_t)kWarps * (32 / P) * kGroupStrideF4;
 }
 
-// One chunk per launch (the reference's RunHMMOnDevice granularity).
-template <int P, class E>
+// One chunk per launch (the reference's RunHMMOnDevice granularity).  P lanes
+// per sample, V evaluations per lane and round.
+template <int P, int V, class E>
 __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p) {
   __shared__ float4 s_vq[16];
   __shared__ float s_pc[16];
@@ -904,7 +964,7 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
   }
   __syncthreads();
   const OneChunk src{p};
-  generation_body<P, E>(src, p.counter, p.stats, p.error, s_vq, s_pc);
+  generation_body<P, V, E>(src, p.counter, p.stats, p.error, s_vq, s_pc);
 }
 
 // Moves every chunk of a prepared batch to its next generation in place, so
@@ -936,10 +996,10 @@ __global__ void advance_kernel(GenParams *__restrict__ table, uint32_t n) {
 
 // Many chunks of uneven size in one persistent launch: one queue over all
 // samples of all chunks.
-template <int P, class E>
+template <int P, int V, class E>
 __global__ void __launch_bounds__(kThreads) generation_multi_kernel(const MultiParams mp) {
   const ManyChunks src{mp};
-  generation_body<P, E>(src, mp.counter, mp.stats, mp.error, nullptr, nullptr);
+  generation_body<P, V, E>(src, mp.counter, mp.stats, mp.error, nullptr, nullptr);
 }
 
 }  // namespace glp

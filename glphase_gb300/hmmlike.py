@@ -97,6 +97,9 @@ class HMMLikeCUDA:
     def set_lanes_per_sample(self, lanes: int) -> None:
         self._c(self.L.glp_set_lanes_per_sample(self.ctx, lanes))
 
+    def set_evals_per_lane(self, evals: int) -> None:
+        self._c(self.L.glp_set_evals_per_lane(self.ctx, evals))
+
     def stats(self) -> tuple[int, int, int]:
         ev, rd, ln = C.c_uint64(), C.c_uint64(), C.c_uint32()
         self._c(self.L.glp_get_stats(self.ctx, C.byref(ev), C.byref(rd), C.byref(ln)))
@@ -182,7 +185,8 @@ class Engine:
 
     def __init__(self, emit: np.ndarray, prob: np.ndarray, tran: np.ndarray, pc: np.ndarray,
                  haps: np.ndarray, num_cycles: int, device: int = 0, lanes: int = 0,
-                 packed: np.ndarray | None = None, codebook: np.ndarray | None = None):
+                 packed: np.ndarray | None = None, codebook: np.ndarray | None = None,
+                 evals: int = 0):
         import torch
         self.torch = torch
         self.dev = HMMLikeCUDA(device)
@@ -198,6 +202,7 @@ class Engine:
             self.dev.copy_code_book_to_device(codebook)
             self.dev.copy_packed_gls_to_device(packed)
         self.dev.set_lanes_per_sample(lanes)
+        self.dev.set_evals_per_lane(evals)
         h = torch.from_numpy(np.ascontiguousarray(haps).view(np.int64))
         self.haps = h.to(self.device)
         self.hnew = self.haps.clone()
@@ -209,15 +214,30 @@ class Engine:
         torch.cuda.current_stream(self.device).synchronize()
         self.dev._c(self.dev.L.glp_set_stream(self.dev.ctx, self.stream.cuda_stream))
 
+    def knn(self, k: int, freq_lb: float = 0.0, freq_ub: float = 1.0, use_maf: bool = False):
+        """Neighbour table of the current haplotypes on the device
+        (KNN::ClusterHaps, kNN.cpp:123-206); kept for the in-kernel draws."""
+        torch = self.torch
+        half = (k + 1) // 2
+        self.nbr = torch.zeros((self.H // 2, 2 * half), dtype=torch.int32, device=self.device)
+        self.dev._c(self.dev.L.glp_knn_neighbors(self.dev.ctx, self.haps.data_ptr(), self.H,
+                                                 self.S, k, freq_lb, freq_ub, int(use_maf),
+                                                 self.nbr.data_ptr()))
+        return self.nbr
+
     def args(self, quad_in, props, pen: float, seed: int, generation: int, work: bool = True,
-             eval_trace=None, accept_trace=None) -> nat.GenerationArgs:
+             eval_trace=None, accept_trace=None, neighbors=None) -> nat.GenerationArgs:
+        """quad_in / props None: drawn in the kernel (from `neighbors` when
+        given, else uniformly over all other haplotypes)."""
         a = nat.GenerationArgs()
         a.num_samples, a.num_sites, a.num_cycles, a.num_haps = self.N, self.S, self.C, self.H
         a.haps = self.haps.data_ptr()
         a.hnew = self.hnew.data_ptr()
-        a.hap_idxs_in = quad_in.data_ptr()
+        a.hap_idxs_in = None if quad_in is None else quad_in.data_ptr()
         a.hap_idxs_out = self.quad.data_ptr()
-        a.props = props.data_ptr()
+        a.props = None if props is None else props.data_ptr()
+        if neighbors is not None:
+            a.neighbors, a.neighbors_per_sample = neighbors.data_ptr(), neighbors.shape[1]
         a.pen = pen
         a.seed = seed
         a.generation = generation
@@ -238,14 +258,19 @@ class Engine:
         src/insti.cpp:1455); panel rows are identical in both buffers."""
         self.haps, self.hnew = self.hnew, self.haps
 
-    def run_host(self, haps: np.ndarray, quad: np.ndarray, props: np.ndarray, pen: float,
+    def run_host(self, haps: np.ndarray, quad, props, pen: float,
                  seed: int, generation: int, hnew: np.ndarray, quad_out: np.ndarray,
-                 like_out: np.ndarray | None = None) -> None:
-        """The same generation through the host-pointer entry point."""
+                 like_out: np.ndarray | None = None, neighbors: np.ndarray | None = None) -> None:
+        """The same generation through the host-pointer entry point (quad /
+        props None: drawn in the kernel, from `neighbors` when given)."""
         a = nat.GenerationArgs()
         a.num_samples, a.num_sites, a.num_cycles, a.num_haps = self.N, self.S, self.C, self.H
         a.haps, a.hnew = _ptr(haps), _ptr(hnew)
-        a.hap_idxs_in, a.hap_idxs_out, a.props = _ptr(quad), _ptr(quad_out), _ptr(props)
+        a.hap_idxs_in = None if quad is None else _ptr(quad)
+        a.hap_idxs_out = _ptr(quad_out)
+        a.props = None if props is None else _ptr(props)
+        if neighbors is not None:
+            a.neighbors, a.neighbors_per_sample = _ptr(neighbors), neighbors.shape[1]
         a.pen, a.seed, a.generation = pen, seed, generation
         a.flags = nat.GLP_GEN_VQ if self.vq else 0
         a.like_out = None if like_out is None else _ptr(like_out)

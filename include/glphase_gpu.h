@@ -170,6 +170,12 @@ int glp_finish(glp_ctx *ctx);
  * (0 = choose from the last generation's acceptance rate). */
 int glp_set_lanes_per_sample(glp_ctx *ctx, uint32_t lanes);
 
+/* Evaluations each lane scores per speculative round: 1, or 2 with 2, 4 or 8
+ * lanes per sample (a round then covers 2P chain positions with the same
+ * accept decisions); 0 = 1.  No reference counterpart (a tuning knob of the
+ * speculative scheme). */
+int glp_set_evals_per_lane(glp_ctx *ctx, uint32_t evals);
+
 /* Evaluations (scored quadruples, speculative ones included) and speculative
  * rounds of the most recent generation (after glp_finish). */
 int glp_get_stats(glp_ctx *ctx, uint64_t *evaluations, uint64_t *rounds,

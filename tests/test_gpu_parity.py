@@ -141,6 +141,37 @@ def test_speculation_width_is_exact(dev, oracle_lib, lanes):
     assert np.array_equal(out["hnew"], ref["hnew"])
 
 
+@pytest.mark.parametrize("lanes", [2, 4, 8])
+@pytest.mark.parametrize("S", [64, 257, 1000])
+def test_two_evaluations_per_lane_is_exact(dev, oracle_lib, lanes, S):
+    """Rounds of 2P evaluations (two per lane) give the sequential chain's
+    results, bit for bit, including the hmm_work haplotypes."""
+    m, haps, quad, props = make_problem(N=40, S=S, C=30, seed=5)
+    dev.set_lanes_per_sample(lanes)
+    dev.set_evals_per_lane(2)
+    try:
+        out = run_gpu(dev, m, haps, quad, props, 0.3, seed=3, gen=2)
+    finally:
+        dev.set_lanes_per_sample(0)
+        dev.set_evals_per_lane(0)
+    check_against_oracle(oracle_lib, m, haps, quad, props, 0.3, out, 3, 2)
+    dev.set_lanes_per_sample(1)
+    try:
+        ref = run_gpu(dev, m, haps, quad, props, 0.3, seed=3, gen=2)
+    finally:
+        dev.set_lanes_per_sample(0)
+    assert np.array_equal(out["quad"], ref["quad"])
+    assert np.array_equal(out["evals"], ref["evals"], equal_nan=True)
+    assert np.array_equal(out["acc"], ref["acc"])
+    assert np.array_equal(out["hnew"], ref["hnew"])
+
+
+def test_evals_per_lane_argument(dev):
+    with pytest.raises(nat.GlpError):
+        dev.set_evals_per_lane(3)
+    dev.set_evals_per_lane(0)
+
+
 @pytest.mark.parametrize("pen", [1.0, 0.25, 0.015625])
 def test_penalty_and_hmm_work(dev, oracle_lib, pen):
     m, haps, quad, props = make_problem(N=32, S=500, C=16, seed=9)
