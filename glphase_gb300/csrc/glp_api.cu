@@ -21,9 +21,40 @@
 #include <vector>
 
 #include "../../include/glphase_gpu.h"
-#include "glp_kernels.cuh"
 #include "glp_knn.cuh"
+#include "glp_launch.h"
 #include "glp_tally.cuh"
+
+namespace glp {
+
+// Moves every chunk of a prepared batch to its next generation in place, so
+// a captured CUDA graph can replay generation after generation: the new
+// haplotypes become the current ones (Insti::cudaSolve's swap,
+// insti.cpp:1455), the generation counter advances, the annealing penalty
+// follows Insti::estimate (insti.cpp:1670-1671, binary32), and the
+// kick-start restriction of the surrogates ends after generation 0.
+__global__ void advance_kernel(GenParams *__restrict__ table, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  GenParams &p = table[i];
+  if (p.do_work) {
+    uint64_t *cur = const_cast<uint64_t *>(p.haps);
+    p.haps = p.hnew;
+    p.hnew = cur;
+  }
+  p.generation += 1;
+  if (p.burnin) {
+    const float x = fminf(__fdiv_rn((float)p.generation + 1.0f, (float)p.burnin), 1.0f);
+    p.pen = x * x;
+  }
+  if (p.kick) {
+    p.samp_lo = 0;
+    p.kick = 0;
+  }
+}
+
+}  // namespace glp
 
 struct glp_problem {
   glp_ctx *ctx = nullptr;
@@ -188,9 +219,10 @@ int set_tran(glp_problem *pb, const float *tran, uint32_t S) {
   if (!tran || S == 0)
     return fail(c, GLP_ERR_ARG, "tran must be non-null with num_sites > 0");
   std::vector<float4> t4(S);
-  t4[0] = make_float4(1.f, 0.f, 0.f, 0.f);  // row 0 is unused by the recursion
+  t4[0] = make_float4(1.f, 0.f, 0.f, 1.f);  // row 0 is unused by the recursion
   for (uint32_t m = 1; m < S; ++m)
-    t4[m] = make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2], 0.f);
+    t4[m] = make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
+                        tran[3 * m] - tran[3 * m + 2]);
   if (pb->S != S) {
     release(pb->d_tran4);
     pb->S = 0;
@@ -251,19 +283,8 @@ int set_emission(glp_problem *pb, const float *emit, const float *prob, uint32_t
   return GLP_OK;
 }
 
-using SingleFn = void (*)(const glp::GenParams);
-using MultiFn = void (*)(const glp::MultiParams);
-
-template <int P, int V>
-SingleFn single_for(bool vq) {
-  return vq ? glp::generation_kernel<P, V, glp::EmitVQ>
-            : glp::generation_kernel<P, V, glp::EmitF32>;
-}
-template <int P, int V>
-MultiFn multi_for(bool vq) {
-  return vq ? glp::generation_multi_kernel<P, V, glp::EmitVQ>
-            : glp::generation_multi_kernel<P, V, glp::EmitF32>;
-}
+using glp::MultiFn;
+using glp::SingleFn;
 
 // Speculation shape of a launch: P lanes per sample, V evaluations per lane.
 struct Shape {
@@ -271,38 +292,10 @@ struct Shape {
 };
 
 SingleFn single_kernel(Shape sh, bool vq) {
-  if (sh.V == 2) {
-    switch (sh.P) {
-      case 2: return single_for<2, 2>(vq);
-      case 4: return single_for<4, 2>(vq);
-      default: return single_for<8, 2>(vq);
-    }
-  }
-  switch (sh.P) {
-    case 1: return single_for<1, 1>(vq);
-    case 2: return single_for<2, 1>(vq);
-    case 4: return single_for<4, 1>(vq);
-    case 8: return single_for<8, 1>(vq);
-    case 16: return single_for<16, 1>(vq);
-    default: return single_for<32, 1>(vq);
-  }
+  return vq ? glp::single_kernel_vq(sh.P, sh.V) : glp::single_kernel_f32(sh.P, sh.V);
 }
 MultiFn multi_kernel(Shape sh, bool vq) {
-  if (sh.V == 2) {
-    switch (sh.P) {
-      case 2: return multi_for<2, 2>(vq);
-      case 4: return multi_for<4, 2>(vq);
-      default: return multi_for<8, 2>(vq);
-    }
-  }
-  switch (sh.P) {
-    case 1: return multi_for<1, 1>(vq);
-    case 2: return multi_for<2, 1>(vq);
-    case 4: return multi_for<4, 1>(vq);
-    case 8: return multi_for<8, 1>(vq);
-    case 16: return multi_for<16, 1>(vq);
-    default: return multi_for<32, 1>(vq);
-  }
+  return vq ? glp::multi_kernel_vq(sh.P, sh.V) : glp::multi_kernel_f32(sh.P, sh.V);
 }
 
 // Speculation width: the expected useful fraction of a round of P
@@ -1225,13 +1218,14 @@ void *g_noalloc_addr[kNoallocMaxDevices];
 
 // Kernel layout of the reference's tran [S][3] (row 0 unused,
 // hmmLike.cu:325): row 0 becomes the identity so that the first forward step
-// reproduces l = e / 4.
+// reproduces l = e / 4; the fourth component is t0 - t2.
 __global__ void tran4_kernel(const float *__restrict__ tran, uint32_t S,
                              float4 *__restrict__ out) {
   const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m < S)
-    out[m] = m ? make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2], 0.f)
-               : make_float4(1.f, 0.f, 0.f, 0.f);
+    out[m] = m ? make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
+                             __fsub_rn(tran[3 * m], tran[3 * m + 2]))
+               : make_float4(1.f, 0.f, 0.f, 1.f);
 }
 
 size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }

@@ -47,6 +47,11 @@ namespace glp {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
+// resident blocks per SM the generation kernels are compiled for (register cap)
+#ifndef GLP_MIN_BLOCKS
+#define GLP_MIN_BLOCKS 1
+#endif
+constexpr int kMinBlocks = GLP_MIN_BLOCKS;
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr float kTiny = 0x1p-64f;
 constexpr float kHuge = 0x1p64f;
@@ -120,19 +125,14 @@ constexpr int kGroupF4 = 2 * kRing * kSlotF4;  // forward + backward rings
 // reads of the 8 groups of a warp start 4 banks apart and never conflict.
 constexpr int kGroupStrideF4 = kGroupF4 + 1;
 
-// Sites are consumed in blocks of 8 (m0 a multiple of 8): prep8(m0) readies
-// a block, get8(m0, j) returns site m0 + j for a compile-time j; get1(m) is
-// the unblocked form used on ragged tails; ahead(m) prefetches the block
-// holding site m (m must be a valid site).
+// Sites are consumed in blocks of 8 (m0 a multiple of 8): stage(dst, m0, ..)
+// copies a block's emission data into a staging slot and staged(src, j)
+// returns site m0 + j from it; get1(m) reads one site directly (ragged tails
+// and single-word chunks).
 struct EmitF32 {
   const float4 *row;
   __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *) {
     row = p.emit + (size_t)s * p.S;
-  }
-  __device__ __forceinline__ void ahead(uint32_t m) const { prefetch_l1(row + m); }
-  __device__ __forceinline__ void prep8(uint32_t) {}
-  __device__ __forceinline__ float4 get8(uint32_t m0, uint32_t j) const {
-    return __ldg(row + m0 + j);
   }
   __device__ __forceinline__ float4 get1(uint32_t m) const { return __ldg(row + m); }
   // copy the emission of sites m0..m0+7 into dst (lane li of P)
@@ -153,20 +153,10 @@ struct EmitVQ {
   const uint32_t *col;
   const float4 *table;
   uint32_t stride;
-  uint32_t pk;
   __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *tab) {
     col = p.packed + s;
     stride = p.N;
     table = tab;
-  }
-  __device__ __forceinline__ void ahead(uint32_t m) const {
-    prefetch_l1(col + (size_t)(m >> 3) * stride);
-  }
-  __device__ __forceinline__ void prep8(uint32_t m0) {
-    pk = __ldg(col + (size_t)(m0 >> 3) * stride);
-  }
-  __device__ __forceinline__ float4 get8(uint32_t, uint32_t j) const {
-    return table[(pk >> (28u - 4u * j)) & 15u];
   }
   __device__ __forceinline__ float4 get1(uint32_t m) const {
     const uint32_t w = __ldg(col + (size_t)(m >> 3) * stride);
@@ -249,6 +239,73 @@ __device__ __forceinline__ void bwd_step(BState &b, const float4 t, float s00, f
   b.b11 = fmaf(v00, t.z, fmaf(q1, t.y, v11 * t.x));
 }
 
+// The same steps without per-site rescaling, in a shared-term form of T:
+// with p1 = l01 + l10 and p2 = l00 + l11,
+//   (T l)_00 = (x - z) l00 + c1,  (T l)_11 = (x - z) l11 + c1,  c1 = y p1 + z p2
+//   (T l)_01 = (x - z) l01 + c2,  (T l)_10 = (x - z) l10 + c2,  c2 = y p2 + z p1
+// for t = (x, y, z, x - z): 14 operations a site instead of 18.  The caller
+// keeps the state in range by normalising at 8-site block boundaries.
+__device__ __forceinline__ void fwd_fast(FState &f, const float4 t, float s00, float s01,
+                                         float s10, float s11) {
+  const float c1 = fmaf(t.z, f.p2, t.y * f.p1);
+  const float c2 = fmaf(t.z, f.p1, t.y * f.p2);
+  f.l00 = fmaf(t.w, f.l00, c1) * s00;
+  f.l01 = fmaf(t.w, f.l01, c2) * s01;
+  f.l10 = fmaf(t.w, f.l10, c2) * s10;
+  f.l11 = fmaf(t.w, f.l11, c1) * s11;
+  f.p1 = f.l01 + f.l10;
+  f.p2 = f.l00 + f.l11;
+}
+
+__device__ __forceinline__ void bwd_fast(BState &b, const float4 t, float s00, float s01,
+                                         float s10, float s11) {
+  const float v00 = b.b00 * s00, v01 = b.b01 * s01, v10 = b.b10 * s10, v11 = b.b11 * s11;
+  const float q1 = v01 + v10, q2 = v00 + v11;
+  const float c1 = fmaf(t.z, q2, t.y * q1);
+  const float c2 = fmaf(t.z, q1, t.y * q2);
+  b.b00 = fmaf(t.w, v00, c1);
+  b.b01 = fmaf(t.w, v01, c2);
+  b.b10 = fmaf(t.w, v10, c2);
+  b.b11 = fmaf(t.w, v11, c1);
+}
+
+// Exact power-of-two normalisation at a block boundary: scales the state so
+// that its sum lies in [2^62, 2^63) (the exponent e of the sum is clamped so
+// the scale stays a normal float).  Starting a block of 8 sites in that range,
+// the sums stay normal floats as long as the block shrinks them by less than
+// 2^-124 (emissions are at most 1, so sums never grow); the return value is
+// false when the sum left [2^-62, 2^101) in the block just computed, i.e.
+// when range may have been lost and the evaluation must be redone with
+// per-site rescaling.
+__device__ __forceinline__ int norm_exponent(float sum) {
+  return (int)((__float_as_uint(sum) >> 23) & 0xffu);
+}
+__device__ __forceinline__ bool fwd_norm(FState &f) {
+  const int e = norm_exponent(f.p1 + f.p2);
+  const int ec = max(e, 62);
+  const float sc = __uint_as_float((uint32_t)(316 - ec) << 23);  // 2^(189 - ec)
+  f.l00 *= sc;
+  f.l01 *= sc;
+  f.l10 *= sc;
+  f.l11 *= sc;
+  f.p1 *= sc;
+  f.p2 *= sc;
+  f.k += ec - 189;
+  return (uint32_t)(e - 65) <= 162u;
+}
+__device__ __forceinline__ bool bwd_norm(BState &b) {
+  const int e = norm_exponent((b.b00 + b.b11) + (b.b01 + b.b10));
+  const int ec = max(e, 62);
+  const float sc = __uint_as_float((uint32_t)(316 - ec) << 23);
+  b.b00 *= sc;
+  b.b01 *= sc;
+  b.b10 *= sc;
+  b.b11 *= sc;
+  b.k += ec - 189;
+  return (uint32_t)(e - 65) <= 162u;
+}
+
+// Overflow guard of the site-by-site pass (emissions above 1 could grow it).
 __device__ __forceinline__ void fwd_guard(FState &f) {
   if (f.p1 + f.p2 > kHuge) {
     f.l00 *= kTiny;
@@ -258,15 +315,6 @@ __device__ __forceinline__ void fwd_guard(FState &f) {
     f.p1 *= kTiny;
     f.p2 *= kTiny;
     f.k += 64;
-  }
-}
-__device__ __forceinline__ void bwd_guard(BState &b) {
-  if ((b.b00 + b.b11) + (b.b01 + b.b10) > kHuge) {
-    b.b00 *= kTiny;
-    b.b01 *= kTiny;
-    b.b10 *= kTiny;
-    b.b11 *= kTiny;
-    b.k += 64;
   }
 }
 
@@ -306,13 +354,15 @@ __device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, u
 }
 
 // One staged block pair for V quadruples: forward over the 8 sites of slot
-// sf, backward over the 8 sites of slot sb (highest first).  Every staged
-// emission and transition row is read once and used by all V quadruples:
-// 8 V independent FMA chains per lane.
+// sf, backward over the 8 sites of slot sb (highest first), then both states
+// normalised; ok[v] turns false when quadruple v may have lost range.  Every
+// staged emission and transition row is read once and used by all V
+// quadruples: 8 V independent FMA chains per lane.
 template <int V, class E>
 __device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], const E &ef,
                                              const E &eb, const float4 *sf, const float4 *sb,
-                                             const Bits8 (&wf)[V], const Bits8 (&wb)[V]) {
+                                             const Bits8 (&wf)[V], const Bits8 (&wb)[V],
+                                             bool (&ok)[V]) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
     const float4 ex = ef.staged(sf + 8, j), ey = eb.staged(sb + 8, 7 - j);
@@ -322,15 +372,20 @@ __device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], con
       float s00, s01, s10, s11, r00, r01, r10, r11;
       site_emission(ex, wf[v], j, s00, s01, s10, s11);
       site_emission(ey, wb[v], 7 - j, r00, r01, r10, r11);
-      fwd_step(f[v], tx, s00, s01, s10, s11);
-      bwd_step(b[v], ty, r00, r01, r10, r11);
+      fwd_fast(f[v], tx, s00, s01, s10, s11);
+      bwd_fast(b[v], ty, r00, r01, r10, r11);
     }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const bool a = fwd_norm(f[v]), c = bwd_norm(b[v]);
+    ok[v] = ok[v] && a && c;
   }
 }
 
 template <int V, class E>
 __device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const float4 *sf,
-                                            const Bits8 (&wf)[V]) {
+                                            const Bits8 (&wf)[V], bool (&ok)[V]) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
     const float4 ex = ef.staged(sf + 8, j), tx = sf[j];
@@ -338,8 +393,13 @@ __device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const f
     for (int v = 0; v < V; ++v) {
       float s00, s01, s10, s11;
       site_emission(ex, wf[v], j, s00, s01, s10, s11);
-      fwd_step(f[v], tx, s00, s01, s10, s11);
+      fwd_fast(f[v], tx, s00, s01, s10, s11);
     }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const bool a = fwd_norm(f[v]);
+    ok[v] = ok[v] && a;
   }
 }
 
@@ -351,169 +411,188 @@ __device__ __forceinline__ void prefetch_parents(const uint64_t *haps, uint32_t 
   prefetch_l1(haps + (size_t)q.w * wn + w);
 }
 
+// Log-likelihood of one quadruple by a plain forward pass, site by site, with
+// the per-site power-of-two rescaling of fwd_step (the scheme of
+// impute.cpp:327-376), reading emission, transition and parent words straight
+// from global memory.  Used for single-word chunks and, rarely, for an
+// evaluation whose blocked pass may have lost range.
+template <class E>
+__device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, uint32_t wn,
+                                            uint32_t S, const float4 *__restrict__ tran4,
+                                            const E em, uint4 q) {
+  FState f;
+  f.l00 = f.l01 = f.l10 = f.l11 = 0.25f;
+  f.p1 = f.p2 = 0.5f;
+  f.k = 0;
+  for (uint32_t w = 0; w < wn; ++w) {
+    const Parents pw = load_parents(haps, wn, q, w);
+    const uint32_t end = min(S, (w + 1) * 64);
+    for (uint32_t m = w * 64; m < end; ++m) {
+      const uint32_t j = m & 63u;
+      float s00, s01, s10, s11;
+      select4(em.get1(m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
+              (pw.m1 >> j) & 1, s00, s01, s10, s11);
+      fwd_step(f, __ldg(tran4 + m), s00, s01, s10, s11);
+    }
+    fwd_guard(f);
+  }
+  const double sum = (((double)f.l00 + (double)f.l01) + (double)f.l10) + (double)f.l11;
+  return log(sum) + (double)f.k * 0.69314718055994530942;
+}
+
 // Log-likelihoods (natural log, binary64) of V quadruples of one sample.
 //
 // Words [0, wf) run forward and words [wf, wn) backward, one block of 8
 // sites of each at a time, in one instruction stream; the blocks' emission
 // and transition rows are staged by the P lanes of the group into the
 // group's shared-memory ring two block pairs ahead (cp.async), so the
-// arithmetic reads shared memory only.  A ragged last word (S % 64 != 0)
-// runs backward alone, site by site, before the rest; with wn == 1 the
-// single word runs forward, site by site.  All P lanes of the group call
-// this together (gmask).
+// arithmetic reads shared memory only.  States are normalised at block
+// boundaries (exact powers of two); a quadruple whose block sums left the
+// safe range is recomputed by like_forward.  A ragged last word
+// (S % 64 != 0) runs backward alone, site by site, before the rest; a
+// single-word chunk runs like_forward.  All P lanes of the group call this
+// together (gmask).
 template <int V, class E>
 __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
                                           const uint4 (&q)[V], float4 *stage, uint32_t li,
                                           uint32_t P, unsigned gmask, double (&out)[V]) {
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tran4 = p.tran4;
-  FState f[V];
-  BState b[V];
-#pragma unroll
-  for (int v = 0; v < V; ++v) {
-    f[v].l00 = f[v].l01 = f[v].l10 = f[v].l11 = 0.25f;
-    f[v].p1 = f[v].p2 = 0.5f;
-    f[v].k = 0;
-    b[v].b00 = b[v].b01 = b[v].b10 = b[v].b11 = 1.0f;
-    b[v].k = 0;
-  }
-  E ef = em0, eb = em0;
   if (wn == 1) {
 #pragma unroll
+    for (int v = 0; v < V; ++v)
+      out[v] = like_forward(p.haps, wn, S, tran4, em0, q[v]);
+    return;
+  }
+  // block-normalised states start at sum 2^62: the forward state 1/4 scaled
+  // by 2^62, the backward state 1 scaled by 2^60
+  FState f[V];
+  BState b[V];
+  bool ok[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    f[v].l00 = f[v].l01 = f[v].l10 = f[v].l11 = 0x1p60f;
+    f[v].p1 = f[v].p2 = 0x1p61f;
+    f[v].k = -62;
+    b[v].b00 = b[v].b01 = b[v].b10 = b[v].b11 = 0x1p60f;
+    b[v].k = -60;
+    ok[v] = true;
+  }
+  E ef = em0, eb = em0;
+  const uint32_t wf = (wn + 1) >> 1;
+  uint32_t wb = wn - 1;
+  if (S & 63u) {
+#pragma unroll
     for (int v = 0; v < V; ++v) {
-      const Parents pw = load_parents(p.haps, wn, q[v], 0);
+      const Parents pw = load_parents(p.haps, wn, q[v], wb);
 #pragma unroll 1
-      for (uint32_t m = 0; m < S; ++m) {
+      for (int m = (int)S - 1; m >= (int)(wb * 64); --m) {
+        const uint32_t j = (uint32_t)m & 63u;
         float s00, s01, s10, s11;
-        select4(ef.get1(m), (pw.f0 >> m) & 1, (pw.f1 >> m) & 1, (pw.m0 >> m) & 1,
-                (pw.m1 >> m) & 1, s00, s01, s10, s11);
-        fwd_step(f[v], __ldg(tran4 + m), s00, s01, s10, s11);
+        select4(eb.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1,
+                (pw.m0 >> j) & 1, (pw.m1 >> j) & 1, s00, s01, s10, s11);
+        bwd_step(b[v], __ldg(tran4 + m), s00, s01, s10, s11);
       }
+      bwd_norm(b[v]);  // rescaled per site: range kept, only the scale is reset
     }
-  } else {
-    const uint32_t wf = (wn + 1) >> 1;
-    uint32_t wb = wn - 1;
-    if (S & 63u) {
+    --wb;
+  }
+  const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
+  float4 *stF = stage, *stB = stage + kRing * kSlotF4;
+  // Block pairs t = 8 i + blk: forward sites i*64 + 8*blk .. +7 and
+  // backward sites (wb - i)*64 + 8*(7 - blk) .. +7.
+  const uint32_t T = nb * 8;
+  auto issue_pair = [&](uint32_t t) {
+    const uint32_t i = t >> 3, blk = t & 7u;
+    const uint32_t m0 = i * 64 + blk * 8, n0 = (wb - i) * 64 + (7 - blk) * 8;
+    float4 *sf = stF + (t % kRing) * kSlotF4, *sb = stB + (t % kRing) * kSlotF4;
+    for (uint32_t k = li; k < 8; k += P) {
+      cp_async16(sf + k, tran4 + m0 + k);
+      cp_async16(sb + k, tran4 + n0 + k);
+    }
+    ef.stage(sf + 8, m0, li, P);
+    eb.stage(sb + 8, n0, li, P);
+  };
+  if (T > 0)
+    issue_pair(0);
+  cp_async_commit();
+  if (T > 1)
+    issue_pair(1);
+  cp_async_commit();
+  Parents pf[V], pb[V];
+#pragma unroll 1
+  for (uint32_t t = 0; t < T; ++t) {
+    if (t + 2 < T)
+      issue_pair(t + 2);
+    cp_async_commit();
+    const uint32_t i = t >> 3, blk = t & 7u;
+    if (blk == 0) {
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        const Parents pw = load_parents(p.haps, wn, q[v], wb);
-#pragma unroll 1
-        for (int m = (int)S - 1; m >= (int)(wb * 64); --m) {
-          const uint32_t j = (uint32_t)m & 63u;
-          float s00, s01, s10, s11;
-          select4(eb.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1,
-                  (pw.m0 >> j) & 1, (pw.m1 >> j) & 1, s00, s01, s10, s11);
-          bwd_step(b[v], __ldg(tran4 + m), s00, s01, s10, s11);
+        pf[v] = load_parents(p.haps, wn, q[v], i);
+        pb[v] = load_parents(p.haps, wn, q[v], wb - i);
+        if (i + 1 < nb) {  // next words' parents
+          prefetch_parents(p.haps, wn, q[v], i + 1);
+          prefetch_parents(p.haps, wn, q[v], wb - i - 1);
         }
-        bwd_guard(b[v]);
       }
-      --wb;
     }
-    const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
-    float4 *stF = stage, *stB = stage + kRing * kSlotF4;
-    // Block pairs t = 8 i + blk: forward sites i*64 + 8*blk .. +7 and
-    // backward sites (wb - i)*64 + 8*(7 - blk) .. +7.
-    const uint32_t T = nb * 8;
-    auto issue_pair = [&](uint32_t t) {
-      const uint32_t i = t >> 3, blk = t & 7u;
-      const uint32_t m0 = i * 64 + blk * 8, n0 = (wb - i) * 64 + (7 - blk) * 8;
-      float4 *sf = stF + (t % kRing) * kSlotF4, *sb = stB + (t % kRing) * kSlotF4;
-      for (uint32_t k = li; k < 8; k += P) {
-        cp_async16(sf + k, tran4 + m0 + k);
-        cp_async16(sb + k, tran4 + n0 + k);
-      }
-      ef.stage(sf + 8, m0, li, P);
-      eb.stage(sb + 8, n0, li, P);
-    };
-    if (T > 0)
-      issue_pair(0);
-    cp_async_commit();
-    if (T > 1)
-      issue_pair(1);
-    cp_async_commit();
-    Parents pf[V], pb[V];
-#pragma unroll 1
-    for (uint32_t t = 0; t < T; ++t) {
-      if (t + 2 < T)
-        issue_pair(t + 2);
-      cp_async_commit();
-      const uint32_t i = t >> 3, blk = t & 7u;
-      if (blk == 0) {
+    Bits8 xf[V], xb[V];
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          pf[v] = load_parents(p.haps, wn, q[v], i);
-          pb[v] = load_parents(p.haps, wn, q[v], wb - i);
-          if (i + 1 < nb) {  // next words' parents
-            prefetch_parents(p.haps, wn, q[v], i + 1);
-            prefetch_parents(p.haps, wn, q[v], wb - i - 1);
-          }
-        }
-      }
-      Bits8 xf[V], xb[V];
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        xf[v] = window8(pf[v], blk * 8);
-        xb[v] = window8(pb[v], (7 - blk) * 8);
-      }
-      cp_async_wait<2>();
-      __syncwarp(gmask);
-      const uint32_t slot = (t % kRing) * kSlotF4;
-      both_staged8<V>(f, b, ef, eb, stF + slot, stB + slot, xf, xb);
-      if (blk == 7) {
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-          fwd_guard(f[v]);
-          bwd_guard(b[v]);
-        }
-      }
-      __syncwarp(gmask);
+    for (int v = 0; v < V; ++v) {
+      xf[v] = window8(pf[v], blk * 8);
+      xb[v] = window8(pb[v], (7 - blk) * 8);
     }
-    // forward-only words [nb, wf) (wn odd, or a ragged last word)
-    const uint32_t T2 = (wf - nb) * 8;
-    auto issue_fwd = [&](uint32_t t) {
-      const uint32_t m0 = (nb + (t >> 3)) * 64 + (t & 7u) * 8;
-      float4 *sf = stF + (t % kRing) * kSlotF4;
-      for (uint32_t k = li; k < 8; k += P)
-        cp_async16(sf + k, tran4 + m0 + k);
-      ef.stage(sf + 8, m0, li, P);
-    };
-    if (T2 > 0)
-      issue_fwd(0);
-    cp_async_commit();
-    if (T2 > 1)
-      issue_fwd(1);
-    cp_async_commit();
+    cp_async_wait<2>();
+    __syncwarp(gmask);
+    const uint32_t slot = (t % kRing) * kSlotF4;
+    both_staged8<V>(f, b, ef, eb, stF + slot, stB + slot, xf, xb, ok);
+    __syncwarp(gmask);
+  }
+  // forward-only words [nb, wf) (wn odd, or a ragged last word)
+  const uint32_t T2 = (wf - nb) * 8;
+  auto issue_fwd = [&](uint32_t t) {
+    const uint32_t m0 = (nb + (t >> 3)) * 64 + (t & 7u) * 8;
+    float4 *sf = stF + (t % kRing) * kSlotF4;
+    for (uint32_t k = li; k < 8; k += P)
+      cp_async16(sf + k, tran4 + m0 + k);
+    ef.stage(sf + 8, m0, li, P);
+  };
+  if (T2 > 0)
+    issue_fwd(0);
+  cp_async_commit();
+  if (T2 > 1)
+    issue_fwd(1);
+  cp_async_commit();
 #pragma unroll 1
-    for (uint32_t t = 0; t < T2; ++t) {
-      if (t + 2 < T2)
-        issue_fwd(t + 2);
-      cp_async_commit();
-      const uint32_t blk = t & 7u;
-      if (blk == 0) {
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-          pf[v] = load_parents(p.haps, wn, q[v], nb + (t >> 3));
-      }
-      Bits8 xf[V];
+  for (uint32_t t = 0; t < T2; ++t) {
+    if (t + 2 < T2)
+      issue_fwd(t + 2);
+    cp_async_commit();
+    const uint32_t blk = t & 7u;
+    if (blk == 0) {
 #pragma unroll
       for (int v = 0; v < V; ++v)
-        xf[v] = window8(pf[v], blk * 8);
-      cp_async_wait<2>();
-      __syncwarp(gmask);
-      fwd_staged8<V>(f, ef, stF + (t % kRing) * kSlotF4, xf);
-      if (blk == 7) {
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-          fwd_guard(f[v]);
-      }
-      __syncwarp(gmask);
+        pf[v] = load_parents(p.haps, wn, q[v], nb + (t >> 3));
     }
+    Bits8 xf[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+      xf[v] = window8(pf[v], blk * 8);
+    cp_async_wait<2>();
+    __syncwarp(gmask);
+    fwd_staged8<V>(f, ef, stF + (t % kRing) * kSlotF4, xf, ok);
+    __syncwarp(gmask);
   }
 #pragma unroll
   for (int v = 0; v < V; ++v) {
-    const double dot = (double)f[v].l00 * (double)b[v].b00 + (double)f[v].l01 * (double)b[v].b01 +
-                       (double)f[v].l10 * (double)b[v].b10 + (double)f[v].l11 * (double)b[v].b11;
-    out[v] = log(dot) + (double)(f[v].k + b[v].k) * 0.69314718055994530942;
+    if (ok[v]) {
+      const double dot = (double)f[v].l00 * (double)b[v].b00 + (double)f[v].l01 * (double)b[v].b01 +
+                         (double)f[v].l10 * (double)b[v].b10 + (double)f[v].l11 * (double)b[v].b11;
+      out[v] = log(dot) + (double)(f[v].k + b[v].k) * 0.69314718055994530942;
+    } else {
+      out[v] = like_forward(p.haps, wn, S, tran4, em0, q[v]);
+    }
   }
 }
 
@@ -538,7 +617,7 @@ __device__ __forceinline__ float fma3_rn(float a0, float b0, float a1, float b1,
                    __fmul_rn(a3, b3));
 }
 
-__device__ void hmm_work_lane(const GenParams &p, const float *pc, uint32_t s, uint4 q) {
+static __device__ void hmm_work_lane(const GenParams &p, const float *pc, uint32_t s, uint4 q) {
   const uint32_t S = p.S, wn = p.wn;
   const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
                  *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
@@ -954,7 +1033,7 @@ __host__ __device__ constexpr size_t stage_bytes(int P) {
 // One chunk per launch (the reference's RunHMMOnDevice granularity).  P lanes
 // per sample, V evaluations per lane and round.
 template <int P, int V, class E>
-__global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) generation_kernel(const GenParams p) {
   __shared__ float4 s_vq[16];
   __shared__ float s_pc[16];
   if (threadIdx.x < 16) {
@@ -967,37 +1046,10 @@ __global__ void __launch_bounds__(kThreads) generation_kernel(const GenParams p)
   generation_body<P, V, E>(src, p.counter, p.stats, p.error, s_vq, s_pc);
 }
 
-// Moves every chunk of a prepared batch to its next generation in place, so
-// a captured CUDA graph can replay generation after generation: the new
-// haplotypes become the current ones (Insti::cudaSolve's swap,
-// insti.cpp:1455), the generation counter advances, the annealing penalty
-// follows Insti::estimate (insti.cpp:1670-1671, binary32), and the
-// kick-start restriction of the surrogates ends after generation 0.
-__global__ void advance_kernel(GenParams *__restrict__ table, uint32_t n) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n)
-    return;
-  GenParams &p = table[i];
-  if (p.do_work) {
-    uint64_t *cur = const_cast<uint64_t *>(p.haps);
-    p.haps = p.hnew;
-    p.hnew = cur;
-  }
-  p.generation += 1;
-  if (p.burnin) {
-    const float x = fminf(__fdiv_rn((float)p.generation + 1.0f, (float)p.burnin), 1.0f);
-    p.pen = x * x;
-  }
-  if (p.kick) {
-    p.samp_lo = 0;
-    p.kick = 0;
-  }
-}
-
 // Many chunks of uneven size in one persistent launch: one queue over all
 // samples of all chunks.
 template <int P, int V, class E>
-__global__ void __launch_bounds__(kThreads) generation_multi_kernel(const MultiParams mp) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) generation_multi_kernel(const MultiParams mp) {
   const ManyChunks src{mp};
   generation_body<P, V, E>(src, mp.counter, mp.stats, mp.error, nullptr, nullptr);
 }

@@ -166,6 +166,19 @@ def test_two_evaluations_per_lane_is_exact(dev, oracle_lib, lanes, S):
     assert np.array_equal(out["hnew"], ref["hnew"])
 
 
+@pytest.mark.parametrize("S", [700, 1024])
+def test_tiny_emissions_take_the_site_by_site_path(dev, oracle_lib, S):
+    """Blocks of 8 sites that shrink the state by more than 2^-124 leave the
+    range of block normalisation; those evaluations are recomputed site by
+    site and still match the oracle."""
+    m, haps, quad, props = make_problem(N=16, S=S, C=12, seed=13)
+    m.emit = m.emit.copy()
+    m.emit[:, 200:240] *= np.float32(1e-7)        # forward half
+    m.emit[::2, S - 100:S - 80] *= np.float32(1e-9)  # backward half
+    out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
+    check_against_oracle(oracle_lib, m, haps, quad, props, 1.0, out, 7, 1)
+
+
 def test_evals_per_lane_argument(dev):
     with pytest.raises(nat.GlpError):
         dev.set_evals_per_lane(3)
