@@ -424,8 +424,8 @@ int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
 }
 
 template <class Fn>
-unsigned grid_for(glp_ctx *c, Fn fn, uint64_t samples, uint32_t P, int *rc) {
-  const size_t smem = glp::stage_bytes((int)P);
+unsigned grid_for(glp_ctx *c, Fn fn, uint64_t samples, uint32_t P, uint32_t V, int *rc) {
+  const size_t smem = glp::stage_bytes((int)P, (int)V);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
   if (e == cudaSuccess)
@@ -451,12 +451,12 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
   const Shape sh = choose_shape(c, a->num_samples);
   const uint32_t P = sh.P;
   SingleFn fn = single_kernel(sh, vq);
-  const unsigned grid = grid_for(c, fn, a->num_samples, P, &rc);
+  const unsigned grid = grid_for(c, fn, a->num_samples, P, sh.V, &rc);
   if (rc)
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
-  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P), c->stream>>>(p);
+  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(p);
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = (uint64_t)a->num_samples * a->num_cycles;
@@ -726,12 +726,12 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   const Shape sh = choose_shape(c, total);
   const uint32_t P = sh.P;
   MultiFn fn = multi_kernel(sh, vq);
-  const unsigned grid = grid_for(c, fn, total, P, &rc);
+  const unsigned grid = grid_for(c, fn, total, P, sh.V, &rc);
   if (rc)
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
-  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P), c->stream>>>(mp);
+  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(mp);
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = chain_cycles;
@@ -744,7 +744,7 @@ struct glp_batch {
   glp_ctx *c = nullptr;
   uint32_t count = 0;
   uint64_t total = 0, chain_cycles = 0;
-  uint32_t P = 4;
+  uint32_t P = 4, V = 1;
   unsigned grid = 1;
   glp::GenParams *d_table = nullptr;
   uint32_t *d_offsets = nullptr;
@@ -760,7 +760,7 @@ int batch_enqueue(glp_batch *b, cudaStream_t st) {
   glp_ctx *c = b->c;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), st));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), st));
-  b->fn<<<b->grid, glp::kThreads, glp::stage_bytes((int)b->P), st>>>(b->mp);
+  b->fn<<<b->grid, glp::kThreads, glp::stage_bytes((int)b->P, (int)b->V), st>>>(b->mp);
   GLP_CUDA(c, cudaGetLastError());
   glp::advance_kernel<<<(b->count + 127) / 128, 128, 0, st>>>(b->d_table, b->count);
   GLP_CUDA(c, cudaGetLastError());
@@ -845,8 +845,9 @@ int glp_batch_prepare(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   b->mp.error = c->d_error;
   const Shape sh = choose_shape(c, total);
   b->P = sh.P;
+  b->V = sh.V;
   b->fn = multi_kernel(sh, vq);
-  b->grid = grid_for(c, b->fn, total, b->P, &rc);
+  b->grid = grid_for(c, b->fn, total, b->P, b->V, &rc);
   if (rc)
     return bail(rc);
   if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
@@ -907,6 +908,8 @@ int glp_finish(glp_ctx *c) {
     c->last_accept = (double)c->last_stats[2] / (double)c->last_chain_cycles;
   if (h_err) {
     GLP_CUDA(c, cudaMemset(c->d_error, 0, sizeof(int)));
+    if (h_err & ~1)
+      return fail(c, GLP_ERR_INDEX, "device self-check failed: flag 0x%x", (unsigned)h_err);
     return fail(c, GLP_ERR_INDEX, "a haplotype index >= num_haps reached the device");
   }
   return GLP_OK;
@@ -1334,7 +1337,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   sh.P = P;
   SingleFn fn = single_kernel(sh, false);
   int occ = 0;
-  const size_t smem = glp::stage_bytes((int)P);
+  const size_t smem = glp::stage_bytes((int)P, 1);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, smem) != cudaSuccess)

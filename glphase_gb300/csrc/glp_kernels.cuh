@@ -1024,9 +1024,9 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
   }
 }
 
-// Dynamic shared memory of a generation kernel with P lanes per sample: one
-// staging ring pair per group.
-__host__ __device__ constexpr size_t stage_bytes(int P) {
+// Dynamic shared memory of a generation kernel with P lanes per sample and V
+// evaluations per lane: one staging ring pair per group.
+__host__ __device__ constexpr size_t stage_bytes(int P, int /*V*/) {
   return sizeof(float4) * (size_t)kWarps * (32 / P) * kGroupStrideF4;
 }
 
