@@ -79,6 +79,19 @@ def workload(args, rank):
     return w, m, haps
 
 
+# DRAM bytes (read + write) of one generation_kernel launch measured by ncu on
+# the batched workload at S = 1,024 (N = 10,000, C = 100, 8 lanes, float
+# emission); the traffic grows in proportion to S (emission rows per scored
+# site), so the full-size figure is this one scaled by S / 1,024.
+NCU_TRAFFIC_S1024 = 1.292713e9 + 0.168870e9
+
+
+def traffic_per_launch(N, S, C, args):
+    if N != 10000 or C != 100 or args.vq or args.config != "batched":
+        return None
+    return NCU_TRAFFIC_S1024 * S / 1024
+
+
 def pen_for(gen, burnin):
     """Annealing penalty of generation gen (insti.cpp:1670-1671), binary32."""
     from glphase_gb300.batch import anneal_pen
@@ -316,9 +329,11 @@ def run_ours(args):
                 "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value,
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
-                         "traffic": None,
+                         "traffic": traffic_per_launch(N, S, C, args),
                          "note": "29 algorithmic FP32 flops per update; peak = measured FP32 "
-                                 "FMA rate on this GPU (glp_measure_fp32_peak)"},
+                                 "FMA rate on this GPU (glp_measure_fp32_peak); traffic = "
+                                 "DRAM bytes per launch from one ncu capture at S=1024 scaled "
+                                 "by S (profiles/generation_kernel_10000x1024_full.md)"},
             "clocks": ck,
             "gpu_launches": args.steps,
             "kernel_ms": kernel_ms,
