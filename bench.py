@@ -288,6 +288,7 @@ def run_ours(args):
     per = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     elapsed = evs[0].elapsed_time(evs[-1]) / 1e3
     ev, rounds, lanes = eng.dev.stats()
+    cnt = eng.dev.counters()
     elapsed = replicas.max_elapsed(elapsed, device=dev)
     updates_step = N * (C + 1) * S
     value = world * args.steps * updates_step / elapsed
@@ -324,6 +325,8 @@ def run_ours(args):
                 "evals_per_lane": 2 if args.evals == 2 and lanes in (2, 4, 8) else 1,
                 "evaluations_per_step": ev,
                 "speculative_rounds": rounds,
+                "site_by_site_redos": cnt[3],
+                "lane_occupancy": round(cnt[5] / max(32 * cnt[4], 1), 4),
                 "useful_fraction": round(N * (C + 1) / max(ev, 1), 4),
                 "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6),
                 "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},

@@ -110,7 +110,7 @@ struct glp_ctx {
   uint32_t lanes_used = 4;
   double last_accept = -1.0;  // acceptance rate of the last generation
   uint64_t last_chain_cycles = 0;
-  unsigned long long last_stats[3] = {0, 0, 0};
+  unsigned long long last_stats[glp::kStats] = {};
 };
 
 namespace {
@@ -455,9 +455,14 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
   if (rc)
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
-  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
+  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), c->stream));
   fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(p);
   GLP_CUDA(c, cudaGetLastError());
+  if (p.do_work) {
+    glp::hmm_work_kernel<><<<(a->num_samples + glp::kThreads - 1) / glp::kThreads, glp::kThreads,
+                             0, c->stream>>>(p);
+    GLP_CUDA(c, cudaGetLastError());
+  }
   c->lanes_used = P;
   c->last_chain_cycles = (uint64_t)a->num_samples * a->num_cycles;
   return GLP_OK;
@@ -510,7 +515,7 @@ int glp_create(int device, glp_ctx **out) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc((void **)&c->d_counter, sizeof(uint32_t)) != cudaSuccess ||
-      cudaMalloc((void **)&c->d_stats, 3 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc((void **)&c->d_stats, glp::kStats * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc((void **)&c->d_error, sizeof(int)) != cudaSuccess ||
       cudaMemset(c->d_error, 0, sizeof(int)) != cudaSuccess) {
     glp_destroy(c);
@@ -730,8 +735,11 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   if (rc)
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
-  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
+  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), c->stream));
   fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(mp);
+  GLP_CUDA(c, cudaGetLastError());
+  glp::hmm_work_multi_kernel<><<<(unsigned)((total + glp::kThreads - 1) / glp::kThreads),
+                                 glp::kThreads, 0, c->stream>>>(mp);
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = chain_cycles;
@@ -759,8 +767,11 @@ namespace {
 int batch_enqueue(glp_batch *b, cudaStream_t st) {
   glp_ctx *c = b->c;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), st));
-  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), st));
+  GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), st));
   b->fn<<<b->grid, glp::kThreads, glp::stage_bytes((int)b->P, (int)b->V), st>>>(b->mp);
+  GLP_CUDA(c, cudaGetLastError());
+  glp::hmm_work_multi_kernel<><<<(unsigned)((b->total + glp::kThreads - 1) / glp::kThreads),
+                                 glp::kThreads, 0, st>>>(b->mp);
   GLP_CUDA(c, cudaGetLastError());
   glp::advance_kernel<<<(b->count + 127) / 128, 128, 0, st>>>(b->d_table, b->count);
   GLP_CUDA(c, cudaGetLastError());
@@ -1079,6 +1090,16 @@ int glp_get_stats(glp_ctx *c, uint64_t *evaluations, uint64_t *rounds, uint32_t 
   return GLP_OK;
 }
 
+int glp_get_counters(glp_ctx *c, uint64_t *counters, uint32_t n) {
+  if (!c)
+    return GLP_ERR_ARG;
+  if (!counters && n)
+    return fail(c, GLP_ERR_ARG, "counters must be non-null");
+  for (uint32_t i = 0; i < n; ++i)
+    counters[i] = i < (uint32_t)glp::kStats ? c->last_stats[i] : 0;
+  return GLP_OK;
+}
+
 int glp_tally(glp_ctx *c, const uint64_t *haps, uint32_t N, uint32_t S, uint32_t *hsum) {
   int rc = check_ctx(c);
   if (rc)
@@ -1203,8 +1224,8 @@ extern "C" int glp_measure_fp32_peak(glp_ctx *c, float ms_target, double *tflops
 // The scratch of one generation lives in a file-scope device array instead
 // of memory from cudaMalloc.  Layout, in bytes from the start:
 //   [0, 4)     work-queue counter          (cleared by every call)
-//   [8, 32)    statistics, 3 x uint64      (cleared by every call)
-//   [32, 36)   device error flag           (cleared by every call)
+//   [8, 56)    generation counters, 6 x uint64 (cleared by every call)
+//   [64, 68)   device error flag           (cleared by every call)
 //   [256, 256 + round_up(16 S, 256))        transition table, float4 [S]
 //   then       hmm_work rows, float4 [N][S] (written before they are read)
 // Host code never dereferences g_noalloc_scratch: its name there is a host
@@ -1232,6 +1253,9 @@ __global__ void tran4_kernel(const float *__restrict__ tran, uint32_t S,
 }
 
 size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static_assert(8 + glp::kStats * sizeof(unsigned long long) <= 64,
+              "generation counters overlap the error flag in the scratch layout");
 
 }  // namespace
 
@@ -1310,7 +1334,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   p.beta = reinterpret_cast<float4 *>(base + beta_off);
   p.counter = reinterpret_cast<uint32_t *>(base);
   p.stats = reinterpret_cast<unsigned long long *>(base + 8);
-  p.error = reinterpret_cast<int *>(base + 32);
+  p.error = reinterpret_cast<int *>(base + 64);
   p.nbr = a->neighbors;
   p.klen = a->neighbors_per_sample;
   p.samp_lo = lo;
@@ -1351,10 +1375,12 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
     return GLP_ERR_CUDA;
   tran4_kernel<<<(S + 255) / 256, 256, 0, st>>>(tran, S, (float4 *)(base + tran_off));
   fn<<<grid, glp::kThreads, smem, st>>>(p);
+  if (work)
+    glp::hmm_work_kernel<><<<(N + glp::kThreads - 1) / glp::kThreads, glp::kThreads, 0, st>>>(p);
   if (cudaGetLastError() != cudaSuccess)
     return GLP_ERR_CUDA;
   int h_err = 0;
-  if (cudaMemcpyAsync(&h_err, base + 32, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+  if (cudaMemcpyAsync(&h_err, base + 64, sizeof(int), cudaMemcpyDeviceToHost, st) !=
           cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return GLP_ERR_CUDA;

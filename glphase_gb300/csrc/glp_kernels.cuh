@@ -26,9 +26,9 @@
 //    plain forward pass, half the latency.
 //  * Scaling is by exact powers of two with an integer exponent per half;
 //    the log-likelihood is assembled in binary64 (log(dot) + k*ln2).
-//  * hmm_work runs one sample per lane in the reference's exact binary32
-//    operation order (no contraction), on batches of 32 finished samples
-//    collected per warp, so its output bits match the CPU reference.
+//  * hmm_work runs one sample per thread in a second kernel over the final
+//    quadruples, in the reference's exact binary32 operation order (no
+//    contraction), so its output bits match the CPU reference.
 //
 // Memory (all resident in HBM across generations):
 //   haps/hnew  uint64 [H][wn] hap-major   (parent words: L2-resident gathers)
@@ -47,12 +47,18 @@ namespace glp {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-// resident blocks per SM the generation kernels are compiled for (register cap)
+// Resident blocks per SM the one-evaluation-per-lane generation kernels are
+// compiled for: a register cap of 168 per thread keeps 12 warps per SM.
 #ifndef GLP_MIN_BLOCKS
-#define GLP_MIN_BLOCKS 1
+#define GLP_MIN_BLOCKS 3
 #endif
 constexpr int kMinBlocks = GLP_MIN_BLOCKS;
 constexpr uint32_t kNone = 0xffffffffu;
+// Generation counters (GenParams::stats): scored evaluations, speculative
+// rounds, accepted proposals, evaluations redone site by site after a block
+// left the normalisation range, warp rounds, and active lanes summed over
+// warp rounds.
+constexpr int kStats = 6;
 constexpr float kTiny = 0x1p-64f;
 constexpr float kHuge = 0x1p64f;
 
@@ -97,6 +103,12 @@ struct GenParams {
 // load of the same line then hits L1).
 __device__ __forceinline__ void prefetch_l1(const void *ptr) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+}
+
+// Bulk prefetch of [ptr, ptr + bytes) into L2 (a hint: nothing is written);
+// ptr and bytes must be multiples of 16 and the range inside one allocation.
+__device__ __forceinline__ void prefetch_l2_bulk(const void *ptr, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
 }
 
 // Asynchronous global -> shared copies (cp.async): the data lands in shared
@@ -451,7 +463,8 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
 // safe range is recomputed by like_forward.  A ragged last word
 // (S % 64 != 0) runs backward alone, site by site, before the rest; a
 // single-word chunk runs like_forward.  All P lanes of the group call this
-// together (gmask).
+// together; gmask names the lanes that synchronise at each block (the group,
+// or the whole warp when every group runs the same loop).
 template <int V, class E>
 __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
                                           const uint4 (&q)[V], float4 *stage, uint32_t li,
@@ -591,6 +604,8 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
                          (double)f[v].l10 * (double)b[v].b10 + (double)f[v].l11 * (double)b[v].b11;
       out[v] = log(dot) + (double)(f[v].k + b[v].k) * 0.69314718055994530942;
     } else {
+      if (p.stats)
+        atomicAdd(p.stats + 3, 1ull);
       out[v] = like_forward(p.haps, wn, S, tran4, em0, q[v]);
     }
   }
@@ -605,9 +620,6 @@ __device__ __forceinline__ float pick(const float4 e, uint32_t i) {
   return (i & 2u) ? ((i & 1u) ? e.w : e.z) : ((i & 1u) ? e.y : e.x);
 }
 
-__device__ __forceinline__ uint32_t hbit(const uint64_t *h, uint32_t m) {
-  return (uint32_t)((__ldg(h + (m >> 6)) >> (m & 63u)) & 1u);
-}
 
 __device__ __forceinline__ float fma3_rn(float a0, float b0, float a1, float b1, float a2,
                                          float b2, float a3, float b3) {
@@ -617,127 +629,213 @@ __device__ __forceinline__ float fma3_rn(float a0, float b0, float a1, float b1,
                    __fmul_rn(a3, b3));
 }
 
-static __device__ void hmm_work_lane(const GenParams &p, const float *pc, uint32_t s, uint4 q) {
+// Rows of one 4-site step of hmm_work: emission and transition rows (and, in
+// the forward pass, the backward vectors and genotype probabilities).  Steps
+// are aligned to multiples of 4 sites, so a step never straddles a parent
+// word and matches the reference's 4-site random draws; indices outside
+// [0, S) are clamped (the rows loaded there are never used).
+struct WorkRows {
+  float4 e[4], t[4];
+};
+struct WorkRowsF {
+  float4 e[4], t[4], b[4];
+  float g[12];
+};
+
+__device__ __forceinline__ uint32_t clamp_site(int m, uint32_t S) {
+  return m < 0 ? 0u : ((uint32_t)m >= S ? S - 1 : (uint32_t)m);
+}
+
+__device__ __forceinline__ void load_rows(WorkRows &r, const float4 *e, const float4 *tr,
+                                          int m0, uint32_t S) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t m = clamp_site(m0 + j, S);
+    r.e[j] = __ldg(e + m);
+    r.t[j] = __ldg(tr + m);
+  }
+}
+
+__device__ __forceinline__ void load_rows(WorkRowsF &r, const float4 *e, const float4 *tr,
+                                          const float4 *beta, const float *pr, int m0,
+                                          uint32_t S) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t m = clamp_site(m0 + j, S);
+    r.e[j] = __ldg(e + m);
+    r.t[j] = __ldg(tr + m);
+    r.b[j] = beta[m];
+    r.g[3 * j] = __ldg(pr + 3 * m);
+    r.g[3 * j + 1] = __ldg(pr + 3 * m + 1);
+    r.g[3 * j + 2] = __ldg(pr + 3 * m + 2);
+  }
+}
+
+// hmm_work of sample s with final quadruple q, in the reference's binary32
+// operation order (impute.cpp:380-485).  pcr holds the mutation matrix rows
+// pc[i][0..3] as four float4 (shared memory).  The next 4-site step's rows
+// are loaded before the current step is computed; the arithmetic is the
+// site-by-site recursion of the reference, unchanged.
+__device__ __forceinline__ void hmm_work_lane(const GenParams &p, const float4 *pcr, uint32_t s,
+                                              uint4 q) {
   const uint32_t S = p.S, wn = p.wn;
   const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
                  *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
   const float4 *e = p.emit + (size_t)s * S;
+  const float4 *tr = p.tran4;
   float4 *beta = p.beta + (size_t)s * S;
-  // backward recursion (impute.cpp:389-414)
+  // backward recursion (impute.cpp:389-414): sites S-1 .. 1
   float b0 = 1.f, b1 = 1.f, b2 = 1.f, b3 = 1.f;
   beta[S - 1] = make_float4(1.f, 1.f, 1.f, 1.f);
-  for (uint32_t m = S - 1; m; --m) {
-    const float4 em = __ldg(e + m);
-    const float4 t = __ldg(p.tran4 + m);
-    const uint32_t a0 = hbit(f0, m), a1 = hbit(f1, m), c0 = hbit(m0, m), c1 = hbit(m1, m);
-    const float b00 = __fmul_rn(b0, pick(em, (a0 << 1) | c0));
-    const float b01 = __fmul_rn(b1, pick(em, (a0 << 1) | c1));
-    const float b10 = __fmul_rn(b2, pick(em, (a1 << 1) | c0));
-    const float b11 = __fmul_rn(b3, pick(em, (a1 << 1) | c1));
-    b0 = __fadd_rn(__fadd_rn(__fmul_rn(b00, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
-                   __fmul_rn(b11, t.z));
-    b1 = __fadd_rn(__fadd_rn(__fmul_rn(b01, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
-                   __fmul_rn(b10, t.z));
-    b2 = __fadd_rn(__fadd_rn(__fmul_rn(b10, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
-                   __fmul_rn(b01, t.z));
-    b3 = __fadd_rn(__fadd_rn(__fmul_rn(b11, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
-                   __fmul_rn(b00, t.z));
-    const float sum = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(__fadd_rn(b0, b1), b2), b3));
-    b0 = __fmul_rn(b0, sum);
-    b1 = __fmul_rn(b1, sum);
-    b2 = __fmul_rn(b2, sum);
-    b3 = __fmul_rn(b3, sum);
-    beta[m - 1] = make_float4(b0, b1, b2, b3);
+  {
+    const int top = (int)((S - 1) & ~3u);
+    WorkRows cur, nxt;
+    load_rows(cur, e, tr, top, S);
+    for (int c0 = top; c0 >= 0; c0 -= 4) {
+      // sites [c0 - 64, c0 - 32) of the emission row into L2, a block ahead
+      if ((c0 & 31) == 0 && c0 >= 64)
+        prefetch_l2_bulk(e + (c0 - 64), 32 * sizeof(float4));
+      load_rows(nxt, e, tr, c0 - 4, S);
+      const uint32_t w = (uint32_t)c0 >> 6;
+      const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
+                     C1 = __ldg(m1 + w);
+#pragma unroll
+      for (int j = 3; j >= 0; --j) {
+        const int m = c0 + j;
+        if (m >= 1 && m <= (int)S - 1) {
+          const uint32_t sh = (uint32_t)m & 63u;
+          const uint32_t a0 = (uint32_t)(A0 >> sh) & 1u, a1 = (uint32_t)(A1 >> sh) & 1u,
+                         c0b = (uint32_t)(C0 >> sh) & 1u, c1b = (uint32_t)(C1 >> sh) & 1u;
+          const float4 em = cur.e[j], t = cur.t[j];
+          const float b00 = __fmul_rn(b0, pick(em, (a0 << 1) | c0b));
+          const float b01 = __fmul_rn(b1, pick(em, (a0 << 1) | c1b));
+          const float b10 = __fmul_rn(b2, pick(em, (a1 << 1) | c0b));
+          const float b11 = __fmul_rn(b3, pick(em, (a1 << 1) | c1b));
+          b0 = __fadd_rn(__fadd_rn(__fmul_rn(b00, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                         __fmul_rn(b11, t.z));
+          b1 = __fadd_rn(__fadd_rn(__fmul_rn(b01, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                         __fmul_rn(b10, t.z));
+          b2 = __fadd_rn(__fadd_rn(__fmul_rn(b10, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                         __fmul_rn(b01, t.z));
+          b3 = __fadd_rn(__fadd_rn(__fmul_rn(b11, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                         __fmul_rn(b00, t.z));
+          const float sum = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(__fadd_rn(b0, b1), b2), b3));
+          b0 = __fmul_rn(b0, sum);
+          b1 = __fmul_rn(b1, sum);
+          b2 = __fmul_rn(b2, sum);
+          b3 = __fmul_rn(b3, sum);
+          beta[m - 1] = make_float4(b0, b1, b2, b3);
+        }
+      }
+      cur = nxt;
+    }
   }
-  // forward sampling (impute.cpp:416-484)
+  // forward sampling (impute.cpp:416-484): sites 0 .. S-1
   const float *pr = p.prob + (size_t)s * S * 3;
   uint64_t *ha = p.hnew + (size_t)2 * s * wn, *hb = ha + wn;
   uint64_t wa = 0, wb = 0;
   float l00 = 0, l01 = 0, l10 = 0, l11 = 0;
   const bool use_pow = p.pen != 1.0f;
-  glp_u32x4 ux;
-  for (uint32_t m = 0; m < S; ++m) {
-    const float4 em = __ldg(e + m);
-    const float4 t = __ldg(p.tran4 + m);
-    const uint32_t a0 = hbit(f0, m), a1 = hbit(f1, m), c0 = hbit(m0, m), c1 = hbit(m1, m);
-    const uint32_t s00 = (a0 << 1) | c0, s01 = (a0 << 1) | c1, s10 = (a1 << 1) | c0,
-                   s11 = (a1 << 1) | c1;
-    if (m) {
-      const float b00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
-      const float b01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
-      const float b10 = fma3_rn(l00, t.y, l01, t.z, l10, t.x, l11, t.y);
-      const float b11 = fma3_rn(l00, t.z, l01, t.y, l10, t.y, l11, t.x);
-      l00 = __fmul_rn(b00, pick(em, s00));
-      l01 = __fmul_rn(b01, pick(em, s01));
-      l10 = __fmul_rn(b10, pick(em, s10));
-      l11 = __fmul_rn(b11, pick(em, s11));
-    } else {
-      l00 = __fmul_rn(0.25f, pick(em, s00));
-      l01 = __fmul_rn(0.25f, pick(em, s01));
-      l10 = __fmul_rn(0.25f, pick(em, s10));
-      l11 = __fmul_rn(0.25f, pick(em, s11));
+  WorkRowsF cur, nxt;
+  load_rows(cur, e, tr, beta, pr, 0, S);
+  // the genotype-probability row is 16-byte aligned when S is a multiple of 4
+  const bool pr_aligned = (((uintptr_t)pr) & 15u) == 0;
+  for (uint32_t c0 = 0; c0 < S; c0 += 4) {
+    // sites [c0 + 64, c0 + 96) of the emission, backward and probability
+    // rows into L2, a block ahead
+    if ((c0 & 31u) == 0 && c0 + 96 <= S) {
+      prefetch_l2_bulk(e + c0 + 64, 32 * sizeof(float4));
+      prefetch_l2_bulk(beta + c0 + 64, 32 * sizeof(float4));
+      if (pr_aligned)
+        prefetch_l2_bulk(pr + 3 * (c0 + 64), 96 * sizeof(float));
     }
-    const float sum = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(__fadd_rn(l00, l01), l10), l11));
-    l00 = __fmul_rn(l00, sum);
-    l01 = __fmul_rn(l01, sum);
-    l10 = __fmul_rn(l10, sum);
-    l11 = __fmul_rn(l11, sum);
-    const float4 bb = beta[m];
-    const float p00 = __fmul_rn(l00, bb.x), p01 = __fmul_rn(l01, bb.y),
-                p10 = __fmul_rn(l10, bb.z), p11 = __fmul_rn(l11, bb.w);
-    const float g0 = __ldg(pr + 3 * m), g1 = __ldg(pr + 3 * m + 1),
-                g2 = __ldg(pr + 3 * m + 2);
-    float c[4];
+    load_rows(nxt, e, tr, beta, pr, (int)c0 + 4, S);
+    const uint32_t w = c0 >> 6;
+    const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
+                   C1 = __ldg(m1 + w);
+    glp_u32x4 ux;
+    if (!p.tr_work)
+      ux = glp_draw(p.seed, p.generation, s, c0 >> 2, GLP_TAG_WORK);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float inner = fma3_rn(p00, pc[s00 * 4 + k], p01, pc[s01 * 4 + k], p10,
-                                  pc[s10 * 4 + k], p11, pc[s11 * 4 + k]);
-      const float g = k == 0 ? g0 : (k == 3 ? g2 : g1);
-      const float x = __fmul_rn(g, inner);
-      c[k] = use_pow ? powf(x, p.pen) : x;
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t m = c0 + (uint32_t)j;
+      if (m < S) {
+        const uint32_t sh = m & 63u;
+        const uint32_t a0 = (uint32_t)(A0 >> sh) & 1u, a1 = (uint32_t)(A1 >> sh) & 1u,
+                       c0b = (uint32_t)(C0 >> sh) & 1u, c1b = (uint32_t)(C1 >> sh) & 1u;
+        const uint32_t s00 = (a0 << 1) | c0b, s01 = (a0 << 1) | c1b, s10 = (a1 << 1) | c0b,
+                       s11 = (a1 << 1) | c1b;
+        const float4 em = cur.e[j], t = cur.t[j];
+        if (m) {
+          const float b00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
+          const float b01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
+          const float b10 = fma3_rn(l00, t.y, l01, t.z, l10, t.x, l11, t.y);
+          const float b11 = fma3_rn(l00, t.z, l01, t.y, l10, t.y, l11, t.x);
+          l00 = __fmul_rn(b00, pick(em, s00));
+          l01 = __fmul_rn(b01, pick(em, s01));
+          l10 = __fmul_rn(b10, pick(em, s10));
+          l11 = __fmul_rn(b11, pick(em, s11));
+        } else {
+          l00 = __fmul_rn(0.25f, pick(em, s00));
+          l01 = __fmul_rn(0.25f, pick(em, s01));
+          l10 = __fmul_rn(0.25f, pick(em, s10));
+          l11 = __fmul_rn(0.25f, pick(em, s11));
+        }
+        const float sum = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(__fadd_rn(l00, l01), l10), l11));
+        l00 = __fmul_rn(l00, sum);
+        l01 = __fmul_rn(l01, sum);
+        l10 = __fmul_rn(l10, sum);
+        l11 = __fmul_rn(l11, sum);
+        const float4 bb = cur.b[j];
+        const float p00 = __fmul_rn(l00, bb.x), p01 = __fmul_rn(l01, bb.y),
+                    p10 = __fmul_rn(l10, bb.z), p11 = __fmul_rn(l11, bb.w);
+        const float4 r00 = pcr[s00], r01 = pcr[s01], r10 = pcr[s10], r11 = pcr[s11];
+        const float gk[3] = {cur.g[3 * j], cur.g[3 * j + 1], cur.g[3 * j + 2]};
+        const float inner0 = fma3_rn(p00, r00.x, p01, r01.x, p10, r10.x, p11, r11.x);
+        const float inner1 = fma3_rn(p00, r00.y, p01, r01.y, p10, r10.y, p11, r11.y);
+        const float inner2 = fma3_rn(p00, r00.z, p01, r01.z, p10, r10.z, p11, r11.z);
+        const float inner3 = fma3_rn(p00, r00.w, p01, r01.w, p10, r10.w, p11, r11.w);
+        float c[4] = {__fmul_rn(gk[0], inner0), __fmul_rn(gk[1], inner1),
+                      __fmul_rn(gk[1], inner2), __fmul_rn(gk[2], inner3)};
+        if (use_pow) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            c[k] = powf(c[k], p.pen);
+        }
+        const float u = p.tr_work ? __ldg(p.tr_work + (size_t)s * S + m) : glp_u24(ux.v[j]);
+        const float c01 = __fadd_rn(c[0], c[1]);
+        const float c012 = __fadd_rn(c01, c[2]);
+        const float r = __fmul_rn(u, __fadd_rn(c012, c[3]));
+        uint32_t bit_a, bit_b;
+        if (r < c[0]) {
+          bit_a = 0;
+          bit_b = 0;
+        } else if (r < c01) {
+          bit_a = 0;
+          bit_b = 1;
+        } else if (r < c012) {
+          bit_a = 1;
+          bit_b = 0;
+        } else {
+          bit_a = 1;
+          bit_b = 1;
+        }
+        wa |= (uint64_t)bit_a << sh;
+        wb |= (uint64_t)bit_b << sh;
+        if (sh == 63u || m == S - 1) {
+          ha[m >> 6] = wa;
+          hb[m >> 6] = wb;
+          wa = 0;
+          wb = 0;
+        }
+      }
     }
-    float u;
-    if (p.tr_work) {
-      u = __ldg(p.tr_work + (size_t)s * S + m);
-    } else {
-      if ((m & 3u) == 0 || m == 0)
-        ux = glp_draw(p.seed, p.generation, s, m >> 2, GLP_TAG_WORK);
-      u = glp_u24(ux.v[m & 3u]);
-    }
-    const float c01 = __fadd_rn(c[0], c[1]);
-    const float c012 = __fadd_rn(c01, c[2]);
-    const float r = __fmul_rn(u, __fadd_rn(c012, c[3]));
-    uint32_t bit_a, bit_b;
-    if (r < c[0]) {
-      bit_a = 0;
-      bit_b = 0;
-    } else if (r < c01) {
-      bit_a = 0;
-      bit_b = 1;
-    } else if (r < c012) {
-      bit_a = 1;
-      bit_b = 0;
-    } else {
-      bit_a = 1;
-      bit_b = 1;
-    }
-    wa |= (uint64_t)bit_a << (m & 63u);
-    wb |= (uint64_t)bit_b << (m & 63u);
-    if ((m & 63u) == 63u || m == S - 1) {
-      ha[m >> 6] = wa;
-      hb[m >> 6] = wb;
-      wa = 0;
-      wb = 0;
-    }
+    cur = nxt;
   }
 }
 
 // ---------------------------------------------------------------------------
 // The generation kernels.
-
-struct Pending {
-  uint32_t c, s, q0, q1, q2, q3;
-};
 
 __device__ __forceinline__ void set_slot(uint4 &q, uint32_t r, uint32_t v) {
   if (r == 0)
@@ -792,35 +890,78 @@ struct ManyChunks {
   }
 };
 
+// Lane groups of a warp.  A warp starts as 32/P groups of P lanes (P is the
+// smallest group size the kernel is instantiated for).  Once the sample queue
+// is exhausted and some of the warp's groups have no sample left, the warp's
+// 32 lanes are re-partitioned among its remaining samples: na samples get
+// groups of p = 32 / nextpow2(na) or 2p lanes (the 2p-groups first, every
+// group aligned to its size), so the longest chains of a generation finish
+// with wider speculation instead of leaving lanes idle.
+struct LaneGroups {
+  uint32_t size, base, index, count;
+};
+
+__device__ __forceinline__ LaneGroups regroup(uint32_t lane, uint32_t na) {
+  const uint32_t np2 = 1u << (32 - __clz(na - 1u));  // nextpow2(na), na >= 1
+  const uint32_t p = 32u / (na > 1 ? np2 : 1u);
+  const uint32_t nbig = 32u / p - na;  // groups of 2p lanes
+  LaneGroups g;
+  g.count = na;
+  if (lane < nbig * 2 * p) {
+    g.size = 2 * p;
+    g.index = lane / (2 * p);
+    g.base = g.index * 2 * p;
+  } else {
+    g.size = p;
+    g.index = nbig + (lane - nbig * 2 * p) / p;
+    g.base = nbig * 2 * p + (g.index - nbig) * p;
+  }
+  return g;
+}
+
 template <int P, int V, class E, class Src>
 __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counter,
                                                 unsigned long long *stats, int *error,
-                                                const float4 *vq_smem, const float *pc_smem) {
+                                                const float4 *vq_smem) {
   static_assert(P == 1 || P == 2 || P == 4 || P == 8 || P == 16 || P == 32, "P");
   static_assert(V == 1 || V == 2, "V");
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr uint32_t G0 = 32u / P;  // group slots (staging rings) per warp
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t li = lane % P, gbase = lane - li;
-  __shared__ Pending s_pend[kWarps][64];
-  __shared__ uint32_t s_npend[kWarps];
+  // current partition of the warp's lanes
+  uint32_t Pc = P, gbase = lane - lane % P, gidx = lane / P, ngroups = G0;
+  uint32_t li = lane - gbase;
   extern __shared__ float4 glp_stage[];  // kWarps * (32/P) * kGroupStrideF4 float4
-  if (lane == 0)
-    s_npend[warp] = 0;
-  __syncwarp();
 
   const uint32_t total = src.total();
+  // The first sample of group slot g of global warp w is g * W + w, which
+  // spreads the samples evenly over the warps; later samples come from the
+  // queue counter, offset past those.
+  const uint32_t nwarps = gridDim.x * (uint32_t)kWarps;
+  const uint32_t gwarp = blockIdx.x * (uint32_t)kWarps + warp;
+  const uint32_t spread = (uint32_t)min((unsigned long long)total,
+                                        (unsigned long long)G0 * nwarps);
+  bool first = true;
   uint32_t c = 0, s = kNone, e = 0;
   uint4 q = make_uint4(0, 0, 0, 0);
   double curr = 0.0;
   bool exhausted = false;
   unsigned long long n_evals = 0, n_rounds = 0, n_acc = 0;
+  unsigned long long n_warp_rounds = 0, n_active_lanes = 0;
 
   while (true) {
     // idle groups take the next sample from the generation's queue
     const bool need = (s == kNone) && !exhausted;
     uint32_t ns = 0;
-    if (need && li == 0)
-      ns = atomicAdd(counter, 1u);
+    if (need && li == 0) {
+      if (first) {
+        const unsigned long long f = (unsigned long long)gidx * nwarps + gwarp;
+        ns = f < spread ? (uint32_t)f : total;
+      } else {
+        ns = spread + atomicAdd(counter, 1u);
+      }
+    }
+    first = false;
     ns = __shfl_sync(FULL, ns, gbase);
     if (need) {
       if (ns < total) {
@@ -853,15 +994,42 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
         exhausted = true;
       }
     }
-    const bool active = s != kNone;
-    if (!__any_sync(FULL, active))
+    // groups still without a sample cannot get one any more: hand their
+    // lanes to the warp's remaining samples
+    const unsigned lead = __ballot_sync(FULL, li == 0 && s != kNone);
+    if (lead == 0)
       break;
+    const uint32_t na = __popc(lead);
+    if (na < ngroups) {
+      const LaneGroups ng = regroup(lane, na);
+      const uint32_t from = __fns(lead, 0, (int)ng.index + 1);
+      c = __shfl_sync(FULL, c, from);
+      s = __shfl_sync(FULL, s, from);
+      e = __shfl_sync(FULL, e, from);
+      q.x = __shfl_sync(FULL, q.x, from);
+      q.y = __shfl_sync(FULL, q.y, from);
+      q.z = __shfl_sync(FULL, q.z, from);
+      q.w = __shfl_sync(FULL, q.w, from);
+      curr = __shfl_sync(FULL, curr, from);
+      Pc = ng.size;
+      gbase = ng.base;
+      gidx = ng.index;
+      ngroups = ng.count;
+      li = lane - gbase;
+      exhausted = true;
+    }
+    const bool active = s != kNone;
+    const unsigned amask = __ballot_sync(FULL, active);
+    if (lane == 0) {
+      ++n_warp_rounds;
+      n_active_lanes += __popc(amask);
+    }
 
     const GenParams &p = src.chunk(c);
     const uint32_t N = p.N, C = p.C, H = p.H;
-    // one speculative round of P V evaluations: lane li scores evaluations
+    // one speculative round of Pc V evaluations: lane li scores evaluations
     // e + li V + v, v < V (round position r = li V + v)
-    constexpr uint32_t PV = (uint32_t)(P * V);
+    const uint32_t PV = Pc * (uint32_t)V;
     const uint32_t k = active ? min(PV, C + 1 - e) : 0u;
     uint32_t slot[V], phap[V];
     double u[V];
@@ -895,14 +1063,21 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
 #pragma unroll
     for (int v = 0; v < V; ++v)
       L[v] = 0.0;
+    // When every lane of the warp scores a chunk of the same length, all
+    // groups run the same block loop and synchronise as one warp: a
+    // group-masked __syncwarp would let the groups drift apart and issue the
+    // loop body once per group.
+    unsigned same = 0;
+    __match_all_sync(FULL, active ? p.S : 0u, (int *)&same);
+    const bool warp_lockstep = same && amask == FULL;
     if (active) {
       // every lane of an active group evaluates (positions past k score the
       // base quadruple and drop the result) so the group shares its ring
       E em;
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
-      const unsigned gm = (P == 32) ? FULL : (((1u << P) - 1u) << gbase);
-      float4 *ring = glp_stage + ((size_t)warp * (32 / P) + lane / P) * kGroupStrideF4;
-      eval_like<V, E>(p, em, myq, ring, li, (uint32_t)P, gm, L);
+      const unsigned gm = (Pc == 32 || warp_lockstep) ? FULL : (((1u << Pc) - 1u) << gbase);
+      float4 *ring = glp_stage + ((size_t)warp * G0 + gidx) * kGroupStrideF4;
+      eval_like<V, E>(p, em, myq, ring, li, Pc, gm, L);
 #pragma unroll
       for (int v = 0; v < V; ++v)
         if (li * V + v >= k)
@@ -926,7 +1101,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       if (acc)
         vfirst = (uint32_t)v;
     }
-    const unsigned gmask = (P == 32) ? FULL : (((1u << P) - 1u) << gbase);
+    const unsigned gmask = (Pc == 32) ? FULL : (((1u << Pc) - 1u) << gbase);
     const unsigned abal = __ballot_sync(FULL, vfirst < (uint32_t)V) & gmask;
     const uint32_t srcl = abal ? (uint32_t)(__ffs(abal) - 1) : gbase;
     const uint32_t vw = __shfl_sync(FULL, vfirst, srcl);
@@ -969,7 +1144,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       }
     }
 
-    // finished chains: publish, queue for hmm_work
+    // finished chains: publish (hmm_work_kernel samples their haplotypes)
     const bool done = active && e > C;
     if (done && li == 0) {
       p.quad_out[s] = q.x;
@@ -979,48 +1154,17 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       if (p.like_out)
         p.like_out[s] = curr;
     }
-    const bool queue = done && li == 0 && p.do_work;
-    const unsigned dmask = __ballot_sync(FULL, queue);
-    const uint32_t s_done = s;
     if (done)
       s = kNone;
-    if (dmask) {
-      // at most 31 entries wait between batches and at most 32 groups finish
-      // per round, so the 64-entry list never overflows
-      const uint32_t base = s_npend[warp];
-      if (queue) {
-        const uint32_t pos = base + __popc(dmask & ((1u << lane) - 1u));
-        s_pend[warp][pos] = Pending{c, s_done, q.x, q.y, q.z, q.w};
-      }
-      __syncwarp();
-      uint32_t n = base + __popc(dmask);
-      if (n >= 32) {
-        const Pending pe = s_pend[warp][lane];
-        const GenParams &pw = src.chunk(pe.c);
-        hmm_work_lane(pw, Src::kMulti ? pw.pc : pc_smem, pe.s,
-                      make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
-        __syncwarp();
-        if (lane < n - 32)
-          s_pend[warp][lane] = s_pend[warp][lane + 32];
-        n -= 32;
-      }
-      __syncwarp();
-      if (lane == 0)
-        s_npend[warp] = n;
-      __syncwarp();
-    }
   }
-  const uint32_t n = s_npend[warp];
-  if (lane < n) {
-    const Pending pe = s_pend[warp][lane];
-    const GenParams &pw = src.chunk(pe.c);
-    hmm_work_lane(pw, Src::kMulti ? pw.pc : pc_smem, pe.s,
-                  make_uint4(pe.q0, pe.q1, pe.q2, pe.q3));
-  }
-  if (stats && li == 0 && n_rounds) {
+  if (stats && n_rounds) {  // per-lane counts of the rounds this lane led
     atomicAdd(stats, n_evals);
     atomicAdd(stats + 1, n_rounds);
     atomicAdd(stats + 2, n_acc);
+  }
+  if (stats && n_warp_rounds) {
+    atomicAdd(stats + 4, n_warp_rounds);
+    atomicAdd(stats + 5, n_active_lanes);
   }
 }
 
@@ -1033,25 +1177,60 @@ __host__ __device__ constexpr size_t stage_bytes(int P, int /*V*/) {
 // One chunk per launch (the reference's RunHMMOnDevice granularity).  P lanes
 // per sample, V evaluations per lane and round.
 template <int P, int V, class E>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) generation_kernel(const GenParams p) {
+__global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
+    generation_kernel(const GenParams p) {
   __shared__ float4 s_vq[16];
-  __shared__ float s_pc[16];
-  if (threadIdx.x < 16) {
-    s_pc[threadIdx.x] = p.pc[threadIdx.x];
-    if (p.vq_table)
-      s_vq[threadIdx.x] = p.vq_table[threadIdx.x];
-  }
+  if (threadIdx.x < 16 && p.vq_table)
+    s_vq[threadIdx.x] = p.vq_table[threadIdx.x];
   __syncthreads();
   const OneChunk src{p};
-  generation_body<P, V, E>(src, p.counter, p.stats, p.error, s_vq, s_pc);
+  generation_body<P, V, E>(src, p.counter, p.stats, p.error, s_vq);
 }
 
 // Many chunks of uneven size in one persistent launch: one queue over all
 // samples of all chunks.
 template <int P, int V, class E>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) generation_multi_kernel(const MultiParams mp) {
+__global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
+    generation_multi_kernel(const MultiParams mp) {
   const ManyChunks src{mp};
-  generation_body<P, V, E>(src, mp.counter, mp.stats, mp.error, nullptr, nullptr);
+  generation_body<P, V, E>(src, mp.counter, mp.stats, mp.error, nullptr);
+}
+
+// hmm_work of every sample after the generation kernel: one sample per
+// thread over the published final quadruples, so whole warps run the
+// sequential per-site recursion together.  Chunks without hmm_work skip it.
+template <class Src>
+__device__ __forceinline__ void work_body(const Src &src) {
+  // each thread's mutation-matrix rows, 5 float4 apart (no bank conflicts)
+  __shared__ float4 s_pcr[kThreads][5];
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= src.total())
+    return;
+  uint32_t c, s;
+  src.locate(g, c, s);
+  const GenParams &p = src.chunk(c);
+  if (!p.do_work)
+    return;
+  float4 *pcr = s_pcr[threadIdx.x];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    pcr[i] = make_float4(p.pc[4 * i], p.pc[4 * i + 1], p.pc[4 * i + 2], p.pc[4 * i + 3]);
+  const uint32_t N = p.N;
+  const uint4 q = make_uint4(p.quad_out[s], p.quad_out[N + s], p.quad_out[2 * (size_t)N + s],
+                             p.quad_out[3 * (size_t)N + s]);
+  hmm_work_lane(p, pcr, s, q);
+}
+
+template <int = 0>
+__global__ void __launch_bounds__(kThreads) hmm_work_kernel(const GenParams p) {
+  const OneChunk src{p};
+  work_body(src);
+}
+
+template <int = 0>
+__global__ void __launch_bounds__(kThreads) hmm_work_multi_kernel(const MultiParams mp) {
+  const ManyChunks src{mp};
+  work_body(src);
 }
 
 }  // namespace glp

@@ -100,6 +100,13 @@ class HMMLikeCUDA:
     def set_evals_per_lane(self, evals: int) -> None:
         self._c(self.L.glp_set_evals_per_lane(self.ctx, evals))
 
+    def counters(self) -> list[int]:
+        """[evaluations, rounds, accepts, site-by-site redos, warp rounds,
+        active lanes over warp rounds] of the last generation."""
+        buf = (C.c_uint64 * 6)()
+        self._c(self.L.glp_get_counters(self.ctx, buf, 6))
+        return list(buf)
+
     def stats(self) -> tuple[int, int, int]:
         ev, rd, ln = C.c_uint64(), C.c_uint64(), C.c_uint32()
         self._c(self.L.glp_get_stats(self.ctx, C.byref(ev), C.byref(rd), C.byref(ln)))

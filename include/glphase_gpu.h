@@ -181,6 +181,14 @@ int glp_set_evals_per_lane(glp_ctx *ctx, uint32_t evals);
 int glp_get_stats(glp_ctx *ctx, uint64_t *evaluations, uint64_t *rounds,
                   uint32_t *lanes_used);
 
+/* Generation counters of the most recent generation (after glp_finish), the
+ * first n of: [0] scored evaluations, [1] speculative rounds, [2] accepted
+ * proposals, [3] evaluations recomputed site by site (a block left the
+ * normalisation range), [4] warp rounds, [5] active lanes summed over warp
+ * rounds.  Entries past the sixth are 0.  No reference counterpart
+ * (diagnostics of the speculative kernel). */
+int glp_get_counters(glp_ctx *ctx, uint64_t *counters, uint32_t n);
+
 /* ---- Many phasing chunks per launch (no reference counterpart: the
  * reference runs one chunk per RunHMMOnDevice call, src/hmmLike.cu:399). ----
  * A problem holds one chunk's device-resident model inputs, the same ones

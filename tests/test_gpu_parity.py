@@ -176,7 +176,17 @@ def test_tiny_emissions_take_the_site_by_site_path(dev, oracle_lib, S):
     m.emit[:, 200:240] *= np.float32(1e-7)        # forward half
     m.emit[::2, S - 100:S - 80] *= np.float32(1e-9)  # backward half
     out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
+    assert dev.counters()[3] > 0  # some evaluations took the site-by-site path
     check_against_oracle(oracle_lib, m, haps, quad, props, 1.0, out, 7, 1)
+
+
+def test_counters_describe_the_generation(dev):
+    m, haps, quad, props = make_problem(N=40, S=512, C=20, seed=8)
+    run_gpu(dev, m, haps, quad, props, 1.0, seed=2, gen=0)
+    ev, rounds, acc, redo, warp_rounds, lanes = dev.counters()
+    assert ev >= 40 * 21 and rounds > 0 and 0 <= acc <= 40 * 20
+    assert redo == 0  # ordinary emissions never leave the block range
+    assert warp_rounds > 0 and 0 < lanes <= 32 * warp_rounds
 
 
 def test_evals_per_lane_argument(dev):
