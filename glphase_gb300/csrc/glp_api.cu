@@ -298,6 +298,20 @@ MultiFn multi_kernel(Shape sh, bool vq) {
   return vq ? glp::multi_kernel_vq(sh.P, sh.V) : glp::multi_kernel_f32(sh.P, sh.V);
 }
 
+// hmm_work of a generation: the recursions (one thread per sample), then the
+// sampling (one warp per sample).
+void launch_work(const glp::GenParams &p, uint64_t samples, cudaStream_t st) {
+  glp::work_chains_kernel<><<<(unsigned)((samples + glp::kWorkThreads - 1) / glp::kWorkThreads),
+                              glp::kWorkThreads, 0, st>>>(p);
+  glp::work_sample_kernel<><<<(unsigned)samples, 32, 0, st>>>(p);
+}
+void launch_work(const glp::MultiParams &mp, uint64_t samples, cudaStream_t st) {
+  glp::work_chains_multi_kernel<><<<(unsigned)((samples + glp::kWorkThreads - 1) /
+                                               glp::kWorkThreads),
+                                    glp::kWorkThreads, 0, st>>>(mp);
+  glp::work_sample_multi_kernel<><<<(unsigned)samples, 32, 0, st>>>(mp);
+}
+
 // Speculation width: the expected useful fraction of a round of P
 // evaluations at acceptance rate a is (1 - (1-a)^P) / (a P); lanes are
 // useful only while N*P does not exceed the threads the GPU keeps resident.
@@ -459,8 +473,7 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
   fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(p);
   GLP_CUDA(c, cudaGetLastError());
   if (p.do_work) {
-    glp::hmm_work_kernel<><<<(a->num_samples + glp::kThreads - 1) / glp::kThreads, glp::kThreads,
-                             0, c->stream>>>(p);
+    launch_work(p, a->num_samples, c->stream);
     GLP_CUDA(c, cudaGetLastError());
   }
   c->lanes_used = P;
@@ -738,8 +751,7 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), c->stream));
   fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(mp);
   GLP_CUDA(c, cudaGetLastError());
-  glp::hmm_work_multi_kernel<><<<(unsigned)((total + glp::kThreads - 1) / glp::kThreads),
-                                 glp::kThreads, 0, c->stream>>>(mp);
+  launch_work(mp, total, c->stream);
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = chain_cycles;
@@ -770,8 +782,7 @@ int batch_enqueue(glp_batch *b, cudaStream_t st) {
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), st));
   b->fn<<<b->grid, glp::kThreads, glp::stage_bytes((int)b->P, (int)b->V), st>>>(b->mp);
   GLP_CUDA(c, cudaGetLastError());
-  glp::hmm_work_multi_kernel<><<<(unsigned)((b->total + glp::kThreads - 1) / glp::kThreads),
-                                 glp::kThreads, 0, st>>>(b->mp);
+  launch_work(b->mp, b->total, st);
   GLP_CUDA(c, cudaGetLastError());
   glp::advance_kernel<<<(b->count + 127) / 128, 128, 0, st>>>(b->d_table, b->count);
   GLP_CUDA(c, cudaGetLastError());
@@ -1376,7 +1387,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   tran4_kernel<<<(S + 255) / 256, 256, 0, st>>>(tran, S, (float4 *)(base + tran_off));
   fn<<<grid, glp::kThreads, smem, st>>>(p);
   if (work)
-    glp::hmm_work_kernel<><<<(N + glp::kThreads - 1) / glp::kThreads, glp::kThreads, 0, st>>>(p);
+    launch_work(p, N, st);
   if (cudaGetLastError() != cudaSuccess)
     return GLP_ERR_CUDA;
   int h_err = 0;

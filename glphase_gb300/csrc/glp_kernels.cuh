@@ -629,22 +629,28 @@ __device__ __forceinline__ float fma3_rn(float a0, float b0, float a1, float b1,
                    __fmul_rn(a3, b3));
 }
 
-// Rows of one 4-site step of hmm_work: emission and transition rows (and, in
-// the forward pass, the backward vectors and genotype probabilities).  Steps
-// are aligned to multiples of 4 sites, so a step never straddles a parent
-// word and matches the reference's 4-site random draws; indices outside
-// [0, S) are clamped (the rows loaded there are never used).
-struct WorkRows {
-  float4 e[4], t[4];
-};
-struct WorkRowsF {
-  float4 e[4], t[4], b[4];
-  float g[12];
-};
+// hmm_work is split in two passes with the reference's arithmetic unchanged.
+// The forward state l_m of impute.cpp:416-447 does not depend on the sampled
+// bits, so (1) one thread per sample runs the two sequential recursions --
+// the backward vectors beta_m (impute.cpp:389-414) and then the forward l_m --
+// and stores p_m = l_m * beta_m (the products of impute.cpp:449-452) in place
+// of beta_m; (2) the sampling of impute.cpp:453-484 then runs for every site
+// in parallel, one warp per sample and 32 sites per instruction.
 
 __device__ __forceinline__ uint32_t clamp_site(int m, uint32_t S) {
   return m < 0 ? 0u : ((uint32_t)m >= S ? S - 1 : (uint32_t)m);
 }
+
+// Rows of one 4-site step of pass 1: emission and transition rows (and, in
+// the forward recursion, the backward vectors).  Steps are aligned to
+// multiples of 4 sites, so a step never straddles a parent word; indices
+// outside [0, S) are clamped (the rows loaded there are never used).
+struct WorkRows {
+  float4 e[4], t[4];
+};
+struct WorkRowsB {
+  float4 e[4], t[4], b[4];
+};
 
 __device__ __forceinline__ void load_rows(WorkRows &r, const float4 *e, const float4 *tr,
                                           int m0, uint32_t S) {
@@ -656,28 +662,22 @@ __device__ __forceinline__ void load_rows(WorkRows &r, const float4 *e, const fl
   }
 }
 
-__device__ __forceinline__ void load_rows(WorkRowsF &r, const float4 *e, const float4 *tr,
-                                          const float4 *beta, const float *pr, int m0,
-                                          uint32_t S) {
+__device__ __forceinline__ void load_rows(WorkRowsB &r, const float4 *e, const float4 *tr,
+                                          const float4 *beta, int m0, uint32_t S) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const uint32_t m = clamp_site(m0 + j, S);
     r.e[j] = __ldg(e + m);
     r.t[j] = __ldg(tr + m);
     r.b[j] = beta[m];
-    r.g[3 * j] = __ldg(pr + 3 * m);
-    r.g[3 * j + 1] = __ldg(pr + 3 * m + 1);
-    r.g[3 * j + 2] = __ldg(pr + 3 * m + 2);
   }
 }
 
-// hmm_work of sample s with final quadruple q, in the reference's binary32
-// operation order (impute.cpp:380-485).  pcr holds the mutation matrix rows
-// pc[i][0..3] as four float4 (shared memory).  The next 4-site step's rows
-// are loaded before the current step is computed; the arithmetic is the
-// site-by-site recursion of the reference, unchanged.
-__device__ __forceinline__ void hmm_work_lane(const GenParams &p, const float4 *pcr, uint32_t s,
-                                              uint4 q) {
+// Pass 1 of hmm_work for sample s with final quadruple q: beta_m for
+// m = S-1 .. 0, then l_m for m = 0 .. S-1, leaving p_m = l_m * beta_m in
+// p.beta[s][m].  The next 4-site step's rows are loaded before the current
+// step is computed.
+__device__ __forceinline__ void work_chains(const GenParams &p, uint32_t s, uint4 q) {
   const uint32_t S = p.S, wn = p.wn;
   const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
                  *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
@@ -685,16 +685,16 @@ __device__ __forceinline__ void hmm_work_lane(const GenParams &p, const float4 *
   const float4 *tr = p.tran4;
   float4 *beta = p.beta + (size_t)s * S;
   // backward recursion (impute.cpp:389-414): sites S-1 .. 1
-  float b0 = 1.f, b1 = 1.f, b2 = 1.f, b3 = 1.f;
-  beta[S - 1] = make_float4(1.f, 1.f, 1.f, 1.f);
   {
+    float b0 = 1.f, b1 = 1.f, b2 = 1.f, b3 = 1.f;
+    beta[S - 1] = make_float4(1.f, 1.f, 1.f, 1.f);
     const int top = (int)((S - 1) & ~3u);
     WorkRows cur, nxt;
     load_rows(cur, e, tr, top, S);
     for (int c0 = top; c0 >= 0; c0 -= 4) {
-      // sites [c0 - 64, c0 - 32) of the emission row into L2, a block ahead
-      if ((c0 & 31) == 0 && c0 >= 64)
-        prefetch_l2_bulk(e + (c0 - 64), 32 * sizeof(float4));
+      // emission sites [c0 - 96, c0 - 64) into L2, two 32-site blocks ahead
+      if ((c0 & 31) == 0 && c0 >= 96)
+        prefetch_l2_bulk(e + (c0 - 96), 32 * sizeof(float4));
       load_rows(nxt, e, tr, c0 - 4, S);
       const uint32_t w = (uint32_t)c0 >> 6;
       const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
@@ -730,32 +730,20 @@ __device__ __forceinline__ void hmm_work_lane(const GenParams &p, const float4 *
       cur = nxt;
     }
   }
-  // forward sampling (impute.cpp:416-484): sites 0 .. S-1
-  const float *pr = p.prob + (size_t)s * S * 3;
-  uint64_t *ha = p.hnew + (size_t)2 * s * wn, *hb = ha + wn;
-  uint64_t wa = 0, wb = 0;
+  // forward recursion (impute.cpp:416-452): sites 0 .. S-1, p_m = l_m * beta_m
   float l00 = 0, l01 = 0, l10 = 0, l11 = 0;
-  const bool use_pow = p.pen != 1.0f;
-  WorkRowsF cur, nxt;
-  load_rows(cur, e, tr, beta, pr, 0, S);
-  // the genotype-probability row is 16-byte aligned when S is a multiple of 4
-  const bool pr_aligned = (((uintptr_t)pr) & 15u) == 0;
+  WorkRowsB cur, nxt;
+  load_rows(cur, e, tr, beta, 0, S);
   for (uint32_t c0 = 0; c0 < S; c0 += 4) {
-    // sites [c0 + 64, c0 + 96) of the emission, backward and probability
-    // rows into L2, a block ahead
+    // emission and backward sites [c0 + 64, c0 + 96) into L2, two blocks ahead
     if ((c0 & 31u) == 0 && c0 + 96 <= S) {
       prefetch_l2_bulk(e + c0 + 64, 32 * sizeof(float4));
       prefetch_l2_bulk(beta + c0 + 64, 32 * sizeof(float4));
-      if (pr_aligned)
-        prefetch_l2_bulk(pr + 3 * (c0 + 64), 96 * sizeof(float));
     }
-    load_rows(nxt, e, tr, beta, pr, (int)c0 + 4, S);
+    load_rows(nxt, e, tr, beta, (int)c0 + 4, S);
     const uint32_t w = c0 >> 6;
     const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
                    C1 = __ldg(m1 + w);
-    glp_u32x4 ux;
-    if (!p.tr_work)
-      ux = glp_draw(p.seed, p.generation, s, c0 >> 2, GLP_TAG_WORK);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const uint32_t m = c0 + (uint32_t)j;
@@ -765,7 +753,7 @@ __device__ __forceinline__ void hmm_work_lane(const GenParams &p, const float4 *
                        c0b = (uint32_t)(C0 >> sh) & 1u, c1b = (uint32_t)(C1 >> sh) & 1u;
         const uint32_t s00 = (a0 << 1) | c0b, s01 = (a0 << 1) | c1b, s10 = (a1 << 1) | c0b,
                        s11 = (a1 << 1) | c1b;
-        const float4 em = cur.e[j], t = cur.t[j];
+        const float4 em = cur.e[j], t = cur.t[j], bb = cur.b[j];
         if (m) {
           const float b00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
           const float b01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
@@ -786,51 +774,84 @@ __device__ __forceinline__ void hmm_work_lane(const GenParams &p, const float4 *
         l01 = __fmul_rn(l01, sum);
         l10 = __fmul_rn(l10, sum);
         l11 = __fmul_rn(l11, sum);
-        const float4 bb = cur.b[j];
-        const float p00 = __fmul_rn(l00, bb.x), p01 = __fmul_rn(l01, bb.y),
-                    p10 = __fmul_rn(l10, bb.z), p11 = __fmul_rn(l11, bb.w);
-        const float4 r00 = pcr[s00], r01 = pcr[s01], r10 = pcr[s10], r11 = pcr[s11];
-        const float gk[3] = {cur.g[3 * j], cur.g[3 * j + 1], cur.g[3 * j + 2]};
-        const float inner0 = fma3_rn(p00, r00.x, p01, r01.x, p10, r10.x, p11, r11.x);
-        const float inner1 = fma3_rn(p00, r00.y, p01, r01.y, p10, r10.y, p11, r11.y);
-        const float inner2 = fma3_rn(p00, r00.z, p01, r01.z, p10, r10.z, p11, r11.z);
-        const float inner3 = fma3_rn(p00, r00.w, p01, r01.w, p10, r10.w, p11, r11.w);
-        float c[4] = {__fmul_rn(gk[0], inner0), __fmul_rn(gk[1], inner1),
-                      __fmul_rn(gk[1], inner2), __fmul_rn(gk[2], inner3)};
-        if (use_pow) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            c[k] = powf(c[k], p.pen);
-        }
-        const float u = p.tr_work ? __ldg(p.tr_work + (size_t)s * S + m) : glp_u24(ux.v[j]);
-        const float c01 = __fadd_rn(c[0], c[1]);
-        const float c012 = __fadd_rn(c01, c[2]);
-        const float r = __fmul_rn(u, __fadd_rn(c012, c[3]));
-        uint32_t bit_a, bit_b;
-        if (r < c[0]) {
-          bit_a = 0;
-          bit_b = 0;
-        } else if (r < c01) {
-          bit_a = 0;
-          bit_b = 1;
-        } else if (r < c012) {
-          bit_a = 1;
-          bit_b = 0;
-        } else {
-          bit_a = 1;
-          bit_b = 1;
-        }
-        wa |= (uint64_t)bit_a << sh;
-        wb |= (uint64_t)bit_b << sh;
-        if (sh == 63u || m == S - 1) {
-          ha[m >> 6] = wa;
-          hb[m >> 6] = wb;
-          wa = 0;
-          wb = 0;
-        }
+        beta[m] = make_float4(__fmul_rn(l00, bb.x), __fmul_rn(l01, bb.y), __fmul_rn(l10, bb.z),
+                              __fmul_rn(l11, bb.w));
       }
     }
     cur = nxt;
+  }
+}
+
+// Pass 2 of hmm_work: the sampling of impute.cpp:453-484 for sites m0 + lane
+// and m0 + 32 + lane of sample s (one warp per sample and 64-site word),
+// from p_m (pass 1), the genotype probabilities, the mutation-matrix rows pcr
+// (pc[i][0..3] as float4) and the reference's 4-site draws.  Returns the two
+// haplotype bits of the site as bits 0 and 1 (0 for sites past S).
+__device__ __forceinline__ uint32_t work_sample_site(const GenParams &p, const float4 *pcr,
+                                                     uint32_t s, uint32_t m, uint64_t A0,
+                                                     uint64_t A1, uint64_t C0, uint64_t C1) {
+  const uint32_t S = p.S;
+  if (m >= S)
+    return 0;
+  const uint32_t sh = m & 63u;
+  const uint32_t a0 = (uint32_t)(A0 >> sh) & 1u, a1 = (uint32_t)(A1 >> sh) & 1u,
+                 c0b = (uint32_t)(C0 >> sh) & 1u, c1b = (uint32_t)(C1 >> sh) & 1u;
+  const uint32_t s00 = (a0 << 1) | c0b, s01 = (a0 << 1) | c1b, s10 = (a1 << 1) | c0b,
+                 s11 = (a1 << 1) | c1b;
+  const float4 pp = p.beta[(size_t)s * S + m];
+  const float *pr = p.prob + ((size_t)s * S + m) * 3;
+  const float g0 = __ldg(pr), g1 = __ldg(pr + 1), g2 = __ldg(pr + 2);
+  const float4 r00 = pcr[s00], r01 = pcr[s01], r10 = pcr[s10], r11 = pcr[s11];
+  const float inner0 = fma3_rn(pp.x, r00.x, pp.y, r01.x, pp.z, r10.x, pp.w, r11.x);
+  const float inner1 = fma3_rn(pp.x, r00.y, pp.y, r01.y, pp.z, r10.y, pp.w, r11.y);
+  const float inner2 = fma3_rn(pp.x, r00.z, pp.y, r01.z, pp.z, r10.z, pp.w, r11.z);
+  const float inner3 = fma3_rn(pp.x, r00.w, pp.y, r01.w, pp.z, r10.w, pp.w, r11.w);
+  float c[4] = {__fmul_rn(g0, inner0), __fmul_rn(g1, inner1), __fmul_rn(g1, inner2),
+                __fmul_rn(g2, inner3)};
+  if (p.pen != 1.0f) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      c[k] = powf(c[k], p.pen);
+  }
+  float u;
+  if (p.tr_work) {
+    u = __ldg(p.tr_work + (size_t)s * S + m);
+  } else {
+    const glp_u32x4 ux = glp_draw(p.seed, p.generation, s, m >> 2, GLP_TAG_WORK);
+    u = glp_u24(ux.v[m & 3u]);
+  }
+  const float c01 = __fadd_rn(c[0], c[1]);
+  const float c012 = __fadd_rn(c01, c[2]);
+  const float r = __fmul_rn(u, __fadd_rn(c012, c[3]));
+  if (r < c[0])
+    return 0u;  // (0, 0)
+  if (r < c01)
+    return 2u;  // (0, 1)
+  if (r < c012)
+    return 1u;  // (1, 0)
+  return 3u;    // (1, 1)
+}
+
+// Pass 2 for all words of sample s (called by a whole warp): bits of sites
+// w*64 + lane and w*64 + 32 + lane, gathered into the two new haplotype words
+// with ballots.
+__device__ __forceinline__ void work_sample(const GenParams &p, const float4 *pcr, uint32_t s,
+                                            uint4 q, uint32_t lane) {
+  const uint32_t wn = p.wn;
+  const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
+                 *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
+  uint64_t *ha = p.hnew + (size_t)2 * s * wn, *hb = ha + wn;
+  for (uint32_t w = 0; w < wn; ++w) {
+    const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
+                   C1 = __ldg(m1 + w);
+    const uint32_t lo = work_sample_site(p, pcr, s, w * 64 + lane, A0, A1, C0, C1);
+    const uint32_t hi = work_sample_site(p, pcr, s, w * 64 + 32 + lane, A0, A1, C0, C1);
+    const uint32_t alo = __ballot_sync(0xffffffffu, lo & 1u), ahi = __ballot_sync(0xffffffffu, hi & 1u);
+    const uint32_t blo = __ballot_sync(0xffffffffu, lo & 2u), bhi = __ballot_sync(0xffffffffu, hi & 2u);
+    if (lane == 0) {
+      ha[w] = ((uint64_t)ahi << 32) | alo;
+      hb[w] = ((uint64_t)bhi << 32) | blo;
+    }
   }
 }
 
@@ -1196,13 +1217,22 @@ __global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
   generation_body<P, V, E>(src, mp.counter, mp.stats, mp.error, nullptr);
 }
 
-// hmm_work of every sample after the generation kernel: one sample per
-// thread over the published final quadruples, so whole warps run the
-// sequential per-site recursion together.  Chunks without hmm_work skip it.
+// hmm_work after the generation kernel, over the published final
+// quadruples.  Pass 1: one thread per sample runs the two recursions (blocks
+// of one warp, so the few hundred warps of a generation spread over every
+// SM).  Pass 2: one warp per sample samples all sites.  Chunks without
+// hmm_work skip both.
+constexpr int kWorkThreads = 32;
+
 template <class Src>
-__device__ __forceinline__ void work_body(const Src &src) {
-  // each thread's mutation-matrix rows, 5 float4 apart (no bank conflicts)
-  __shared__ float4 s_pcr[kThreads][5];
+__device__ __forceinline__ uint4 final_quad(const Src &, const GenParams &p, uint32_t s) {
+  const uint32_t N = p.N;
+  return make_uint4(p.quad_out[s], p.quad_out[N + s], p.quad_out[2 * (size_t)N + s],
+                    p.quad_out[3 * (size_t)N + s]);
+}
+
+template <class Src>
+__device__ __forceinline__ void chains_body(const Src &src) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= src.total())
     return;
@@ -1211,26 +1241,50 @@ __device__ __forceinline__ void work_body(const Src &src) {
   const GenParams &p = src.chunk(c);
   if (!p.do_work)
     return;
-  float4 *pcr = s_pcr[threadIdx.x];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-    pcr[i] = make_float4(p.pc[4 * i], p.pc[4 * i + 1], p.pc[4 * i + 2], p.pc[4 * i + 3]);
-  const uint32_t N = p.N;
-  const uint4 q = make_uint4(p.quad_out[s], p.quad_out[N + s], p.quad_out[2 * (size_t)N + s],
-                             p.quad_out[3 * (size_t)N + s]);
-  hmm_work_lane(p, pcr, s, q);
+  work_chains(p, s, final_quad(src, p, s));
+}
+
+template <class Src>
+__device__ __forceinline__ void sample_body(const Src &src) {
+  __shared__ float4 s_pcr[kWorkThreads / 32][4];  // the warp's mutation-matrix rows
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint32_t g = blockIdx.x * (blockDim.x >> 5) + wib;  // one sample per warp
+  if (g >= src.total())
+    return;
+  uint32_t c, s;
+  src.locate(g, c, s);
+  const GenParams &p = src.chunk(c);
+  if (!p.do_work)
+    return;
+  if (lane < 4)
+    s_pcr[wib][lane] = make_float4(p.pc[4 * lane], p.pc[4 * lane + 1], p.pc[4 * lane + 2],
+                                   p.pc[4 * lane + 3]);
+  __syncwarp();
+  work_sample(p, s_pcr[wib], s, final_quad(src, p, s), lane);
 }
 
 template <int = 0>
-__global__ void __launch_bounds__(kThreads) hmm_work_kernel(const GenParams p) {
+__global__ void __launch_bounds__(kWorkThreads) work_chains_kernel(const GenParams p) {
   const OneChunk src{p};
-  work_body(src);
+  chains_body(src);
 }
 
 template <int = 0>
-__global__ void __launch_bounds__(kThreads) hmm_work_multi_kernel(const MultiParams mp) {
+__global__ void __launch_bounds__(kWorkThreads) work_chains_multi_kernel(const MultiParams mp) {
   const ManyChunks src{mp};
-  work_body(src);
+  chains_body(src);
+}
+
+template <int = 0>
+__global__ void __launch_bounds__(kWorkThreads) work_sample_kernel(const GenParams p) {
+  const OneChunk src{p};
+  sample_body(src);
+}
+
+template <int = 0>
+__global__ void __launch_bounds__(kWorkThreads) work_sample_multi_kernel(const MultiParams mp) {
+  const ManyChunks src{mp};
+  sample_body(src);
 }
 
 }  // namespace glp
