@@ -629,6 +629,62 @@ __device__ __forceinline__ float fma3_rn(float a0, float b0, float a1, float b1,
                    __fmul_rn(a3, b3));
 }
 
+// The reference's normalisation factor 1.0f / sum (impute.cpp:404, 441): the
+// correctly rounded reciprocal, which is what __frcp_rn returns for every
+// input, with a shorter dependency chain than the general division.
+__device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
+
+// One backward step of impute.cpp:389-414: b <- normalise(T (b * e)), with
+// the emission picks i_ab = (father bit << 1) | mother bit of the site.
+__device__ __forceinline__ void work_bwd_step(float &b0, float &b1, float &b2, float &b3,
+                                              const float4 em, const float4 t, uint32_t i00,
+                                              uint32_t i01, uint32_t i10, uint32_t i11) {
+  const float b00 = __fmul_rn(b0, pick(em, i00));
+  const float b01 = __fmul_rn(b1, pick(em, i01));
+  const float b10 = __fmul_rn(b2, pick(em, i10));
+  const float b11 = __fmul_rn(b3, pick(em, i11));
+  b0 = __fadd_rn(__fadd_rn(__fmul_rn(b00, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                 __fmul_rn(b11, t.z));
+  b1 = __fadd_rn(__fadd_rn(__fmul_rn(b01, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                 __fmul_rn(b10, t.z));
+  b2 = __fadd_rn(__fadd_rn(__fmul_rn(b10, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                 __fmul_rn(b01, t.z));
+  b3 = __fadd_rn(__fadd_rn(__fmul_rn(b11, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                 __fmul_rn(b00, t.z));
+  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(b0, b1), b2), b3));
+  b0 = __fmul_rn(b0, sum);
+  b1 = __fmul_rn(b1, sum);
+  b2 = __fmul_rn(b2, sum);
+  b3 = __fmul_rn(b3, sum);
+}
+
+// One forward step of impute.cpp:416-447 (site 0 when first).
+__device__ __forceinline__ void work_fwd_step(float &l00, float &l01, float &l10, float &l11,
+                                              const float4 em, const float4 t, uint32_t i00,
+                                              uint32_t i01, uint32_t i10, uint32_t i11,
+                                              bool first) {
+  if (!first) {
+    const float c00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
+    const float c01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
+    const float c10 = fma3_rn(l00, t.y, l01, t.z, l10, t.x, l11, t.y);
+    const float c11 = fma3_rn(l00, t.z, l01, t.y, l10, t.y, l11, t.x);
+    l00 = __fmul_rn(c00, pick(em, i00));
+    l01 = __fmul_rn(c01, pick(em, i01));
+    l10 = __fmul_rn(c10, pick(em, i10));
+    l11 = __fmul_rn(c11, pick(em, i11));
+  } else {
+    l00 = __fmul_rn(0.25f, pick(em, i00));
+    l01 = __fmul_rn(0.25f, pick(em, i01));
+    l10 = __fmul_rn(0.25f, pick(em, i10));
+    l11 = __fmul_rn(0.25f, pick(em, i11));
+  }
+  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(l00, l01), l10), l11));
+  l00 = __fmul_rn(l00, sum);
+  l01 = __fmul_rn(l01, sum);
+  l10 = __fmul_rn(l10, sum);
+  l11 = __fmul_rn(l11, sum);
+}
+
 // hmm_work is split in two passes with the reference's arithmetic unchanged.
 // The forward state l_m of impute.cpp:416-447 does not depend on the sampled
 // bits, so (1) one thread per sample runs the two sequential recursions --
@@ -779,6 +835,146 @@ __device__ __forceinline__ void work_chains(const GenParams &p, uint32_t s, uint
       }
     }
     cur = nxt;
+  }
+}
+
+// Pass 1 for the 32 samples of a warp that share one chunk, with coalesced
+// staging: each 16-site tile of the 32 per-sample rows (emission, and in the
+// forward recursion the backward vectors) is copied into shared memory by the
+// whole warp, one 256-byte row segment per half-warp instruction (cp.async,
+// one tile in flight ahead), so every lane then reads its own row from shared
+// memory.  The recursions and their arithmetic are those of work_chains.
+constexpr int kTile = 16;
+constexpr int kTileStrideF4 = kTile + 1;  // odd number of 16-byte units: no bank conflicts
+
+struct ChainTiles {
+  float4 e[2][32 * kTileStrideF4];
+  float4 b[2][32 * kTileStrideF4];
+  float4 t[2][kTile];
+  const float4 *erow[32];
+  float4 *brow[32];
+};
+
+// Copy sites [base, base + kTile) of every row (rows with a null pointer are
+// skipped) and of the transition table; indices are clamped to [0, S).
+__device__ __forceinline__ void stage_tile(float4 *dst, const float4 *const *rows, int base,
+                                           uint32_t S, uint32_t lane) {
+  const uint32_t half = lane >> 4, j = lane & 15u;
+  const uint32_t m = clamp_site(base + (int)j, S);
+#pragma unroll 4
+  for (uint32_t r = 0; r < 32; r += 2) {
+    const float4 *row = rows[r + half];
+    if (row)
+      cp_async16(dst + (r + half) * kTileStrideF4 + j, row + m);
+  }
+}
+
+__device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s, uint4 q,
+                                                  bool valid, uint32_t lane, ChainTiles &sm) {
+  const uint32_t S = p.S, wn = p.wn;
+  const float4 *tr = p.tran4;
+  const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
+                 *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
+  float4 *beta = p.beta + (size_t)s * S;
+  sm.erow[lane] = valid ? p.emit + (size_t)s * S : nullptr;
+  sm.brow[lane] = valid ? beta : nullptr;
+  if (valid)
+    beta[S - 1] = make_float4(1.f, 1.f, 1.f, 1.f);
+  __syncwarp();
+  const int ntiles = (int)((S + kTile - 1) / kTile);
+  const float4 *const *erows = sm.erow;
+  const float4 *const *brows = sm.brow;
+  auto stage = [&](int buf, int base, bool with_beta) {
+    stage_tile(sm.e[buf], erows, base, S, lane);
+    if (with_beta)
+      stage_tile(sm.b[buf], brows, base, S, lane);
+    if (lane < kTile)
+      cp_async16(&sm.t[buf][lane], tr + clamp_site(base + (int)lane, S));
+    cp_async_commit();
+  };
+  // backward recursion (impute.cpp:389-414): sites S-1 .. 1, tiles from the top
+  {
+    float b0 = 1.f, b1 = 1.f, b2 = 1.f, b3 = 1.f;
+    const int top = (int)((S - 1) & ~(uint32_t)(kTile - 1));
+    stage(0, top, false);
+    for (int i = 0; i < ntiles; ++i) {
+      const int base = top - kTile * i, buf = i & 1;
+      if (i + 1 < ntiles)
+        stage(buf ^ 1, base - kTile, false);
+      else
+        cp_async_commit();
+      cp_async_wait<1>();
+      __syncwarp();
+      if (valid) {
+        const uint32_t w = (uint32_t)base >> 6;
+        const uint32_t A0 = (uint32_t)(__ldg(f0 + w) >> (base & 63)),
+                       A1 = (uint32_t)(__ldg(f1 + w) >> (base & 63)),
+                       C0 = (uint32_t)(__ldg(m0 + w) >> (base & 63)),
+                       C1 = (uint32_t)(__ldg(m1 + w) >> (base & 63));
+        const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
+        auto site = [&](int j) {
+          const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
+                         c1b = (C1 >> j) & 1u;
+          work_bwd_step(b0, b1, b2, b3, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
+                        (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b);
+          beta[base + j - 1] = make_float4(b0, b1, b2, b3);
+        };
+        if (base >= 1 && base + kTile - 1 <= (int)S - 1) {
+#pragma unroll
+          for (int j = kTile - 1; j >= 0; --j)
+            site(j);
+        } else {
+#pragma unroll 1
+          for (int j = kTile - 1; j >= 0; --j)
+            if (base + j >= 1 && base + j <= (int)S - 1)
+              site(j);
+        }
+      }
+      __syncwarp();  // the buffer is refilled next iteration
+    }
+  }
+  // every lane's backward vectors are stored before the warp copies them
+  __syncwarp();
+  // forward recursion (impute.cpp:416-452): p_m = l_m * beta_m
+  float l00 = 0, l01 = 0, l10 = 0, l11 = 0;
+  stage(0, 0, true);
+  for (int i = 0; i < ntiles; ++i) {
+    const int base = kTile * i, buf = i & 1;
+    if (i + 1 < ntiles)
+      stage(buf ^ 1, base + kTile, true);
+    else
+      cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    if (valid) {
+      const uint32_t w = (uint32_t)base >> 6;
+      const uint32_t A0 = (uint32_t)(__ldg(f0 + w) >> (base & 63)),
+                     A1 = (uint32_t)(__ldg(f1 + w) >> (base & 63)),
+                     C0 = (uint32_t)(__ldg(m0 + w) >> (base & 63)),
+                     C1 = (uint32_t)(__ldg(m1 + w) >> (base & 63));
+      const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
+      const float4 *brow = sm.b[buf] + lane * kTileStrideF4;
+      auto site = [&](int j) {
+        const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
+                       c1b = (C1 >> j) & 1u;
+        work_fwd_step(l00, l01, l10, l11, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
+                      (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b, base + j == 0);
+        const float4 bb = brow[j];
+        beta[base + j] = make_float4(__fmul_rn(l00, bb.x), __fmul_rn(l01, bb.y),
+                                     __fmul_rn(l10, bb.z), __fmul_rn(l11, bb.w));
+      };
+      if (base >= 1 && base + kTile <= (int)S) {
+#pragma unroll
+        for (int j = 0; j < kTile; ++j)
+          site(j);
+      } else {
+#pragma unroll 1
+        for (int j = 0; j < kTile; ++j)
+          if (base + j < (int)S)
+            site(j);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -1233,15 +1429,27 @@ __device__ __forceinline__ uint4 final_quad(const Src &, const GenParams &p, uin
 
 template <class Src>
 __device__ __forceinline__ void chains_body(const Src &src) {
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= src.total())
-    return;
-  uint32_t c, s;
-  src.locate(g, c, s);
+  __shared__ ChainTiles s_tiles;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;  // blocks are one warp
+  const uint32_t total = src.total();
+  uint32_t c = 0, s = 0;
+  if (g < total)
+    src.locate(g, c, s);
+  else
+    src.locate(total - 1, c, s);  // idle lanes borrow a valid chunk (they skip the work)
   const GenParams &p = src.chunk(c);
-  if (!p.do_work)
-    return;
-  work_chains(p, s, final_quad(src, p, s));
+  const bool valid = g < total && p.do_work;
+  // the warp stages rows together when all its lanes share one chunk
+  int same = 0;
+  __match_all_sync(0xffffffffu, c, &same);
+  if (same) {
+    if (__any_sync(0xffffffffu, valid))
+      work_chains_tiled(p, s, valid ? final_quad(src, p, s) : make_uint4(0, 0, 0, 0), valid,
+                        lane, s_tiles);
+  } else if (valid) {
+    work_chains(p, s, final_quad(src, p, s));
+  }
 }
 
 template <class Src>
