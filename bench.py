@@ -83,7 +83,7 @@ def workload(args, rank):
 # the batched workload at S = 1,024 (N = 10,000, C = 100, 8 lanes, float
 # emission); the traffic grows in proportion to S (emission rows per scored
 # site), so the full-size figure is this one scaled by S / 1,024.
-NCU_TRAFFIC_S1024 = 1.292713e9 + 0.168870e9
+NCU_TRAFFIC_S1024 = 0.946160e9 + 0.004023e9
 
 
 def traffic_per_launch(N, S, C, args):
@@ -292,7 +292,12 @@ def run_ours(args):
     elapsed = replicas.max_elapsed(elapsed, device=dev)
     updates_step = N * (C + 1) * S
     value = world * args.steps * updates_step / elapsed
-    kernel_ms = float(np.mean(per))
+    step_ms = float(np.mean(per))
+    # device time of the generation kernel itself (CUDA events the library
+    # records around it on the same stream) and of the hmm_work kernels
+    gen_t, work_t = eng.dev.kernel_times(args.steps)
+    kernel_ms = float(np.mean(gen_t))
+    work_ms = float(np.mean(work_t))
     achieved = updates_step * FLOPS_PER_UPDATE / (kernel_ms * 1e-3) / 1e12
 
     nbr_host = None if nbr is None else np.ascontiguousarray(
@@ -338,8 +343,10 @@ def run_ours(args):
                                  "DRAM bytes per launch from one ncu capture at S=1024 scaled "
                                  "by S (profiles/generation_kernel_10000x1024_full.md)"},
             "clocks": ck,
-            "gpu_launches": args.steps,
+            "gpu_launches": 3 * args.steps,
+            "step_ms": step_ms,
             "kernel_ms": kernel_ms,
+            "hmm_work_ms": work_ms,
         }
         if e2e:
             line["e2e"] = e2e
@@ -472,7 +479,7 @@ def run_uneven(args):
                    "batched_over_plain": v_b / v_p,
                    "form": "batched = one persistent launch per generation replayed from a "
                            "captured CUDA graph; plain = one launch per chunk"},
-        "clocks": ck, "gpu_launches": 2 * args.steps,
+        "clocks": ck, "gpu_launches": 4 * args.steps,
     }
     print(json.dumps(line), flush=True)
     for p in probs:

@@ -107,10 +107,19 @@ struct glp_ctx {
   // tuning and statistics
   uint32_t lanes = 0;  // 0 = automatic
   uint32_t evals = 0;  // evaluations per lane and round, 0 = automatic
+  // resident threads per lane width (1 .. 32), per [multi-chunk][VQ] kernel
+  double resident[2][2][6] = {};
+  bool resident_known[2][2] = {};
   uint32_t lanes_used = 4;
   double last_accept = -1.0;  // acceptance rate of the last generation
   uint64_t last_chain_cycles = 0;
   unsigned long long last_stats[glp::kStats] = {};
+  // device-time record of the last kTimed generations launched from the host
+  // (glp_run_generation, glp_run_batch): events before the generation kernel,
+  // after it and after the hmm_work kernels, on the launching stream
+  static constexpr uint32_t kTimed = 64;
+  cudaEvent_t ev[kTimed][3] = {};
+  uint64_t ev_count = 0;
 };
 
 namespace {
@@ -312,20 +321,49 @@ void launch_work(const glp::MultiParams &mp, uint64_t samples, cudaStream_t st) 
   glp::work_sample_multi_kernel<><<<(unsigned)samples, 32, 0, st>>>(mp);
 }
 
-// Speculation width: the expected useful fraction of a round of P
-// evaluations at acceptance rate a is (1 - (1-a)^P) / (a P); lanes are
-// useful only while N*P does not exceed the threads the GPU keeps resident.
-uint32_t choose_lanes(const glp_ctx *c, uint64_t N) {
-  if (c->lanes)
-    return c->lanes;
-  const double a = c->last_accept < 0 ? 0.12 : std::max(c->last_accept, 1e-3);
-  const double resident = (double)c->sms * 512.0;
+// Threads of the generation kernel with P lanes per sample that the GPU keeps
+// resident (registers and the per-group staging rings limit the blocks per
+// SM), or 0 when the occupancy query fails.
+template <class Fn>
+double resident_threads(Fn fn, uint32_t P, int sms) {
+  const size_t smem = glp::stage_bytes((int)P, 1);
+  int occ = 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, smem) !=
+          cudaSuccess)
+    return 0.0;
+  return (double)occ * glp::kThreads * sms;
+}
+
+// Speculation width for N samples at acceptance rate a.  A round of P
+// evaluations keeps (1 - (1-a)^P) / (a P) of them useful; the lanes in use
+// are min(N P, threads resident with P lanes), which shrinks for small P when
+// the staging rings limit the blocks per SM.  The score is the useful
+// fraction times the share of the GPU's lanes in use.
+template <class FnOf>
+uint32_t pick_lanes(double a, uint64_t N, int sms, FnOf kernel_for, double *cache = nullptr,
+                    bool *known = nullptr) {
+  double local[6];
+  double *res = cache ? cache : local;
+  if (!known || !*known) {
+    for (int i = 0; i < 6; ++i)
+      res[i] = resident_threads(kernel_for(1u << i), 1u << i, sms);
+    if (known)
+      *known = true;
+  }
+  double most = 0;
+  for (int i = 0; i < 6; ++i)
+    most = std::max(most, res[i]);
+  if (most <= 0)
+    return 8;
   uint32_t best = 1;
   double best_score = 0;
-  for (uint32_t P = 1; P <= 32; P <<= 1) {
+  for (int i = 0; i < 6; ++i) {
+    const uint32_t P = 1u << i;
     const double eff = (1.0 - std::pow(1.0 - a, (double)P)) / (a * P);
-    const double fill = std::min(1.0, (double)N * P / resident);
-    const double score = eff * fill;
+    const double used = std::min((double)N * P, res[i]) / most;
+    const double score = eff * used;
     if (score > best_score * 1.02) {
       best_score = score;
       best = P;
@@ -334,11 +372,25 @@ uint32_t choose_lanes(const glp_ctx *c, uint64_t N) {
   return best;
 }
 
+uint32_t choose_lanes(glp_ctx *c, uint64_t N, bool multi, bool vq) {
+  if (c->lanes)
+    return c->lanes;
+  const double a = c->last_accept < 0 ? 0.12 : std::max(c->last_accept, 1e-3);
+  return pick_lanes(
+      a, N, c->sms,
+      [&](uint32_t P) {
+        Shape sh;
+        sh.P = P;
+        return multi ? (const void *)multi_kernel(sh, vq) : (const void *)single_kernel(sh, vq);
+      },
+      c->resident[multi][vq], &c->resident_known[multi][vq]);
+}
+
 // Lanes from choose_lanes; two evaluations per lane only on request
 // (glp_set_evals_per_lane), and only where that kernel exists (P = 2, 4, 8).
-Shape choose_shape(const glp_ctx *c, uint64_t N) {
+Shape choose_shape(glp_ctx *c, uint64_t N, bool multi, bool vq) {
   Shape sh;
-  sh.P = choose_lanes(c, N);
+  sh.P = choose_lanes(c, N, multi, vq);
   sh.V = (c->evals == 2 && (sh.P == 2 || sh.P == 4 || sh.P == 8)) ? 2u : 1u;
   return sh;
 }
@@ -462,7 +514,7 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
   if (rc)
     return rc;
   const bool vq = (a->flags & GLP_GEN_VQ) != 0;
-  const Shape sh = choose_shape(c, a->num_samples);
+  const Shape sh = choose_shape(c, a->num_samples, false, vq);
   const uint32_t P = sh.P;
   SingleFn fn = single_kernel(sh, vq);
   const unsigned grid = grid_for(c, fn, a->num_samples, P, sh.V, &rc);
@@ -470,12 +522,16 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), c->stream));
+  cudaEvent_t *ev = c->ev[c->ev_count++ % glp_ctx::kTimed];
+  GLP_CUDA(c, cudaEventRecord(ev[0], c->stream));
   fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(p);
   GLP_CUDA(c, cudaGetLastError());
+  GLP_CUDA(c, cudaEventRecord(ev[1], c->stream));
   if (p.do_work) {
     launch_work(p, a->num_samples, c->stream);
     GLP_CUDA(c, cudaGetLastError());
   }
+  GLP_CUDA(c, cudaEventRecord(ev[2], c->stream));
   c->lanes_used = P;
   c->last_chain_cycles = (uint64_t)a->num_samples * a->num_cycles;
   return GLP_OK;
@@ -534,6 +590,12 @@ int glp_create(int device, glp_ctx **out) {
     glp_destroy(c);
     return GLP_ERR_CUDA;
   }
+  for (uint32_t i = 0; i < glp_ctx::kTimed; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (cudaEventCreate(&c->ev[i][j]) != cudaSuccess) {
+        glp_destroy(c);
+        return GLP_ERR_CUDA;
+      }
   c->sms = prop.multiProcessorCount;
   c->stream = c->own_stream;
   *out = c;
@@ -569,6 +631,10 @@ void glp_destroy(glp_ctx *c) {
   release(c->d_like);
   release(c->d_evals);
   release(c->d_tr_work);
+  for (uint32_t i = 0; i < glp_ctx::kTimed; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (c->ev[i][j])
+        cudaEventDestroy(c->ev[i][j]);
   if (c->own_stream)
     cudaStreamDestroy(c->own_stream);
   delete c;
@@ -741,7 +807,7 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   mp.counter = c->d_counter;
   mp.stats = c->d_stats;
   mp.error = c->d_error;
-  const Shape sh = choose_shape(c, total);
+  const Shape sh = choose_shape(c, total, true, vq);
   const uint32_t P = sh.P;
   MultiFn fn = multi_kernel(sh, vq);
   const unsigned grid = grid_for(c, fn, total, P, sh.V, &rc);
@@ -749,9 +815,13 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), c->stream));
+  cudaEvent_t *ev = c->ev[c->ev_count++ % glp_ctx::kTimed];
+  GLP_CUDA(c, cudaEventRecord(ev[0], c->stream));
   fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(mp);
   GLP_CUDA(c, cudaGetLastError());
+  GLP_CUDA(c, cudaEventRecord(ev[1], c->stream));
   launch_work(mp, total, c->stream);
+  GLP_CUDA(c, cudaEventRecord(ev[2], c->stream));
   GLP_CUDA(c, cudaGetLastError());
   c->lanes_used = P;
   c->last_chain_cycles = chain_cycles;
@@ -865,7 +935,7 @@ int glp_batch_prepare(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   b->mp.counter = c->d_counter;
   b->mp.stats = c->d_stats;
   b->mp.error = c->d_error;
-  const Shape sh = choose_shape(c, total);
+  const Shape sh = choose_shape(c, total, true, vq);
   b->P = sh.P;
   b->V = sh.V;
   b->fn = multi_kernel(sh, vq);
@@ -1098,6 +1168,26 @@ int glp_get_stats(glp_ctx *c, uint64_t *evaluations, uint64_t *rounds, uint32_t 
     *rounds = c->last_stats[1];
   if (lanes_used)
     *lanes_used = c->lanes_used;
+  return GLP_OK;
+}
+
+int glp_kernel_times(glp_ctx *c, uint32_t n, float *gen_ms, float *work_ms) {
+  if (!c)
+    return GLP_ERR_ARG;
+  if (n > glp_ctx::kTimed || n > c->ev_count)
+    return fail(c, GLP_ERR_ARG, "at most %u of the %llu timed generations are kept",
+                glp_ctx::kTimed, (unsigned long long)c->ev_count);
+  for (uint32_t i = 0; i < n; ++i) {
+    cudaEvent_t *ev = c->ev[(c->ev_count - n + i) % glp_ctx::kTimed];
+    float g = 0.f, w = 0.f;
+    GLP_CUDA(c, cudaEventSynchronize(ev[2]));
+    GLP_CUDA(c, cudaEventElapsedTime(&g, ev[0], ev[1]));
+    GLP_CUDA(c, cudaEventElapsedTime(&w, ev[1], ev[2]));
+    if (gen_ms)
+      gen_ms[i] = g;
+    if (work_ms)
+      work_ms[i] = w;
+  }
   return GLP_OK;
 }
 
@@ -1358,16 +1448,11 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
 
   // speculation width for an acceptance rate of about 0.12 (the rule of
   // choose_lanes without a context's history)
-  uint32_t P = 1;
-  double best = 0;
-  for (uint32_t w = 1; w <= 32; w <<= 1) {
-    const double eff = (1.0 - std::pow(0.88, (double)w)) / (0.12 * w);
-    const double score = eff * std::min(1.0, (double)N * w / ((double)sms * 512.0));
-    if (score > best * 1.02) {
-      best = score;
-      P = w;
-    }
-  }
+  const uint32_t P = pick_lanes(0.12, N, sms, [](uint32_t w) {
+    Shape s1;
+    s1.P = w;
+    return (const void *)single_kernel(s1, false);
+  });
   Shape sh;
   sh.P = P;
   SingleFn fn = single_kernel(sh, false);

@@ -8,8 +8,9 @@
   returns quadruples transposed to [sample][4].
 * :class:`Engine` -- the device-resident generation loop used for
   throughput: haplotypes, quadruples, proposals and outputs stay in HBM and
-  each generation is one launch with the fused hmm_work (Insti::cudaSolve,
-  src/insti.cpp:1433-1463, without the host hmm_work loop).
+  each generation is the generation kernel followed by the two hmm_work
+  kernels on the same stream (Insti::cudaSolve, src/insti.cpp:1433-1463,
+  without the host hmm_work loop).
 
 Every call goes through the CUDA library; there is no CPU fallback.
 """
@@ -106,6 +107,13 @@ class HMMLikeCUDA:
         buf = (C.c_uint64 * 6)()
         self._c(self.L.glp_get_counters(self.ctx, buf, 6))
         return list(buf)
+
+    def kernel_times(self, n: int) -> tuple[list[float], list[float]]:
+        """Device ms of the generation kernel and of hmm_work for the last n
+        generations launched from this context."""
+        g, w = (C.c_float * n)(), (C.c_float * n)()
+        self._c(self.L.glp_kernel_times(self.ctx, n, g, w))
+        return list(g), list(w)
 
     def stats(self) -> tuple[int, int, int]:
         ev, rd, ln = C.c_uint64(), C.c_uint64(), C.c_uint32()

@@ -31,7 +31,7 @@ EXPORTED = [
     "glp_problem_destroy", "glp_problem_set_model", "glp_problem_set_vq", "glp_run_batch",
     "glp_problem_set_model_device", "glp_batch_prepare", "glp_batch_run", "glp_batch_launch",
     "glp_batch_destroy", "glp_run_generation_noalloc", "glp_tally", "glp_result",
-    "glp_set_evals_per_lane", "glp_get_counters",
+    "glp_set_evals_per_lane", "glp_get_counters", "glp_kernel_times",
 ]
 
 
@@ -101,6 +101,7 @@ def load(build_if_missing: bool = False):
     L.glp_set_lanes_per_sample.argtypes = [vp, u32]
     L.glp_set_evals_per_lane.argtypes = [vp, u32]
     L.glp_get_counters.argtypes = [vp, C.POINTER(u64), u32]
+    L.glp_kernel_times.argtypes = [vp, u32, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.glp_get_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u32)]
     L.glp_measure_fp32_peak.argtypes = [vp, C.c_float, C.POINTER(C.c_double)]
     L.glp_knn_neighbors.argtypes = [vp, vp, u32, u32, u32, C.c_double, C.c_double, i32, vp]

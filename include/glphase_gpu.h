@@ -189,6 +189,13 @@ int glp_get_stats(glp_ctx *ctx, uint64_t *evaluations, uint64_t *rounds,
  * (diagnostics of the speculative kernel). */
 int glp_get_counters(glp_ctx *ctx, uint64_t *counters, uint32_t n);
 
+/* Device time of the last n generations launched by glp_run_generation or
+ * glp_run_batch (n <= 64, oldest first): the generation kernel (gen_ms) and
+ * the two hmm_work kernels (work_ms), from CUDA events on the launching
+ * stream; waits for those generations to finish.  No reference counterpart
+ * (measurement support). */
+int glp_kernel_times(glp_ctx *ctx, uint32_t n, float *gen_ms, float *work_ms);
+
 /* ---- Many phasing chunks per launch (no reference counterpart: the
  * reference runs one chunk per RunHMMOnDevice call, src/hmmLike.cu:399). ----
  * A problem holds one chunk's device-resident model inputs, the same ones
