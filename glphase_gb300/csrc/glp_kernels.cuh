@@ -137,6 +137,20 @@ constexpr int kGroupF4 = 2 * kRing * kSlotF4;  // forward + backward rings
 // reads of the 8 groups of a warp start 4 banks apart and never conflict.
 constexpr int kGroupStrideF4 = kGroupF4 + 1;
 
+// Copies 8 consecutive float4 from src into dst, shared by the P lanes of a
+// group (lane li takes rows li, li + P, ...); with kWide (P >= 8) lanes 0..7
+// take one row each.
+template <bool kWide>
+__device__ __forceinline__ void stage8(float4 *dst, const float4 *src, uint32_t li, uint32_t P) {
+  if (kWide) {
+    if (li < 8)
+      cp_async16(dst + li, src + li);
+  } else {
+    for (uint32_t k = li; k < 8; k += P)
+      cp_async16(dst + k, src + k);
+  }
+}
+
 // Sites are consumed in blocks of 8 (m0 a multiple of 8): stage(dst, m0, ..)
 // copies a block's emission data into a staging slot and staged(src, j)
 // returns site m0 + j from it; get1(m) reads one site directly (ragged tails
@@ -148,10 +162,10 @@ struct EmitF32 {
   }
   __device__ __forceinline__ float4 get1(uint32_t m) const { return __ldg(row + m); }
   // copy the emission of sites m0..m0+7 into dst (lane li of P)
+  template <bool kWide>
   __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, uint32_t li,
                                         uint32_t P) const {
-    for (uint32_t k = li; k < 8; k += P)
-      cp_async16(dst + k, row + m0 + k);
+    stage8<kWide>(dst, row + m0, li, P);
   }
   __device__ __forceinline__ float4 staged(const float4 *src, uint32_t j) const {
     return src[j];
@@ -174,6 +188,7 @@ struct EmitVQ {
     const uint32_t w = __ldg(col + (size_t)(m >> 3) * stride);
     return table[(w >> (28u - 4u * (m & 7u))) & 15u];
   }
+  template <bool kWide>
   __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, uint32_t li,
                                         uint32_t) const {
     if (li == 0)
@@ -282,39 +297,48 @@ __device__ __forceinline__ void bwd_fast(BState &b, const float4 t, float s00, f
 }
 
 // Exact power-of-two normalisation at a block boundary: scales the state so
-// that its sum lies in [2^62, 2^63) (the exponent e of the sum is clamped so
-// the scale stays a normal float).  Starting a block of 8 sites in that range,
-// the sums stay normal floats as long as the block shrinks them by less than
-// 2^-124 (emissions are at most 1, so sums never grow); the return value is
-// false when the sum left [2^-62, 2^101) in the block just computed, i.e.
-// when range may have been lost and the evaluation must be redone with
-// per-site rescaling.
-__device__ __forceinline__ int norm_exponent(float sum) {
-  return (int)((__float_as_uint(sum) >> 23) & 0xffu);
-}
-__device__ __forceinline__ bool fwd_norm(FState &f) {
-  const int e = norm_exponent(f.p1 + f.p2);
-  const int ec = max(e, 62);
-  const float sc = __uint_as_float((uint32_t)(316 - ec) << 23);  // 2^(189 - ec)
+// that its sum lies in [2^62, 2^63).  Starting a block of 8 sites in that
+// range, the sums stay normal floats as long as the block shrinks them by less
+// than 2^-124 (emissions are at most 1, so sums never grow).  The return
+// value is e - 65 for the sum's biased exponent e: it lies outside [0, 127]
+// exactly when the sum left [2^-62, 2^66), i.e. when range may have been lost
+// in the block just computed (the scale is then meaningless too) and the
+// evaluation must be redone with per-site rescaling.
+__device__ __forceinline__ uint32_t fwd_norm(FState &f) {
+  const uint32_t eb = __float_as_uint(f.p1 + f.p2) & 0x7f800000u;
+  const float sc = __uint_as_float(0x9e000000u - eb);  // 2^(189 - e)
   f.l00 *= sc;
   f.l01 *= sc;
   f.l10 *= sc;
   f.l11 *= sc;
   f.p1 *= sc;
   f.p2 *= sc;
-  f.k += ec - 189;
-  return (uint32_t)(e - 65) <= 162u;
+  const int e = (int)(eb >> 23);
+  f.k += e - 189;
+  return (uint32_t)(e - 65);
 }
-__device__ __forceinline__ bool bwd_norm(BState &b) {
-  const int e = norm_exponent((b.b00 + b.b11) + (b.b01 + b.b10));
+__device__ __forceinline__ uint32_t bwd_norm(BState &b) {
+  const uint32_t eb = __float_as_uint((b.b00 + b.b11) + (b.b01 + b.b10)) & 0x7f800000u;
+  const float sc = __uint_as_float(0x9e000000u - eb);
+  b.b00 *= sc;
+  b.b01 *= sc;
+  b.b10 *= sc;
+  b.b11 *= sc;
+  const int e = (int)(eb >> 23);
+  b.k += e - 189;
+  return (uint32_t)(e - 65);
+}
+// The same for a state kept in range site by site (any sum down to 2^-65 is
+// legitimate there): the exponent is clamped so the scale stays a normal float.
+__device__ __forceinline__ void bwd_renorm(BState &b) {
+  const int e = (int)((__float_as_uint((b.b00 + b.b11) + (b.b01 + b.b10)) >> 23) & 0xffu);
   const int ec = max(e, 62);
-  const float sc = __uint_as_float((uint32_t)(316 - ec) << 23);
+  const float sc = __uint_as_float((uint32_t)(316 - ec) << 23);  // 2^(189 - ec)
   b.b00 *= sc;
   b.b01 *= sc;
   b.b10 *= sc;
   b.b11 *= sc;
   b.k += ec - 189;
-  return (uint32_t)(e - 65) <= 162u;
 }
 
 // Overflow guard of the site-by-site pass (emissions above 1 could grow it).
@@ -374,7 +398,7 @@ template <int V, class E>
 __device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], const E &ef,
                                              const E &eb, const float4 *sf, const float4 *sb,
                                              const Bits8 (&wf)[V], const Bits8 (&wb)[V],
-                                             bool (&ok)[V]) {
+                                             uint32_t (&eacc)[V]) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
     const float4 ex = ef.staged(sf + 8, j), ey = eb.staged(sb + 8, 7 - j);
@@ -389,15 +413,13 @@ __device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], con
     }
   }
 #pragma unroll
-  for (int v = 0; v < V; ++v) {
-    const bool a = fwd_norm(f[v]), c = bwd_norm(b[v]);
-    ok[v] = ok[v] && a && c;
-  }
+  for (int v = 0; v < V; ++v)
+    eacc[v] |= fwd_norm(f[v]) | bwd_norm(b[v]);
 }
 
 template <int V, class E>
 __device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const float4 *sf,
-                                            const Bits8 (&wf)[V], bool (&ok)[V]) {
+                                            const Bits8 (&wf)[V], uint32_t (&eacc)[V]) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
     const float4 ex = ef.staged(sf + 8, j), tx = sf[j];
@@ -409,10 +431,8 @@ __device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const f
     }
   }
 #pragma unroll
-  for (int v = 0; v < V; ++v) {
-    const bool a = fwd_norm(f[v]);
-    ok[v] = ok[v] && a;
-  }
+  for (int v = 0; v < V; ++v)
+    eacc[v] |= fwd_norm(f[v]);
 }
 
 __device__ __forceinline__ void prefetch_parents(const uint64_t *haps, uint32_t wn, uint4 q,
@@ -465,7 +485,7 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
 // single-word chunk runs like_forward.  All P lanes of the group call this
 // together; gmask names the lanes that synchronise at each block (the group,
 // or the whole warp when every group runs the same loop).
-template <int V, class E>
+template <int V, bool kWide, class E>
 __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
                                           const uint4 (&q)[V], float4 *stage, uint32_t li,
                                           uint32_t P, unsigned gmask, double (&out)[V]) {
@@ -481,7 +501,7 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
   // by 2^62, the backward state 1 scaled by 2^60
   FState f[V];
   BState b[V];
-  bool ok[V];
+  uint32_t eacc[V];  // OR of the blocks' range codes (fwd_norm)
 #pragma unroll
   for (int v = 0; v < V; ++v) {
     f[v].l00 = f[v].l01 = f[v].l10 = f[v].l11 = 0x1p60f;
@@ -489,7 +509,7 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
     f[v].k = -62;
     b[v].b00 = b[v].b01 = b[v].b10 = b[v].b11 = 0x1p60f;
     b[v].k = -60;
-    ok[v] = true;
+    eacc[v] = 0;
   }
   E ef = em0, eb = em0;
   const uint32_t wf = (wn + 1) >> 1;
@@ -506,7 +526,7 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
                 (pw.m0 >> j) & 1, (pw.m1 >> j) & 1, s00, s01, s10, s11);
         bwd_step(b[v], __ldg(tran4 + m), s00, s01, s10, s11);
       }
-      bwd_norm(b[v]);  // rescaled per site: range kept, only the scale is reset
+      bwd_renorm(b[v]);
     }
     --wb;
   }
@@ -519,12 +539,10 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
     const uint32_t i = t >> 3, blk = t & 7u;
     const uint32_t m0 = i * 64 + blk * 8, n0 = (wb - i) * 64 + (7 - blk) * 8;
     float4 *sf = stF + (t % kRing) * kSlotF4, *sb = stB + (t % kRing) * kSlotF4;
-    for (uint32_t k = li; k < 8; k += P) {
-      cp_async16(sf + k, tran4 + m0 + k);
-      cp_async16(sb + k, tran4 + n0 + k);
-    }
-    ef.stage(sf + 8, m0, li, P);
-    eb.stage(sb + 8, n0, li, P);
+    stage8<kWide>(sf, tran4 + m0, li, P);
+    stage8<kWide>(sb, tran4 + n0, li, P);
+    ef.template stage<kWide>(sf + 8, m0, li, P);
+    eb.template stage<kWide>(sb + 8, n0, li, P);
   };
   if (T > 0)
     issue_pair(0);
@@ -559,7 +577,7 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
     cp_async_wait<2>();
     __syncwarp(gmask);
     const uint32_t slot = (t % kRing) * kSlotF4;
-    both_staged8<V>(f, b, ef, eb, stF + slot, stB + slot, xf, xb, ok);
+    both_staged8<V>(f, b, ef, eb, stF + slot, stB + slot, xf, xb, eacc);
     __syncwarp(gmask);
   }
   // forward-only words [nb, wf) (wn odd, or a ragged last word)
@@ -567,9 +585,8 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
   auto issue_fwd = [&](uint32_t t) {
     const uint32_t m0 = (nb + (t >> 3)) * 64 + (t & 7u) * 8;
     float4 *sf = stF + (t % kRing) * kSlotF4;
-    for (uint32_t k = li; k < 8; k += P)
-      cp_async16(sf + k, tran4 + m0 + k);
-    ef.stage(sf + 8, m0, li, P);
+    stage8<kWide>(sf, tran4 + m0, li, P);
+    ef.template stage<kWide>(sf + 8, m0, li, P);
   };
   if (T2 > 0)
     issue_fwd(0);
@@ -594,12 +611,12 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
       xf[v] = window8(pf[v], blk * 8);
     cp_async_wait<2>();
     __syncwarp(gmask);
-    fwd_staged8<V>(f, ef, stF + (t % kRing) * kSlotF4, xf, ok);
+    fwd_staged8<V>(f, ef, stF + (t % kRing) * kSlotF4, xf, eacc);
     __syncwarp(gmask);
   }
 #pragma unroll
   for (int v = 0; v < V; ++v) {
-    if (ok[v]) {
+    if ((eacc[v] & ~127u) == 0) {
       const double dot = (double)f[v].l00 * (double)b[v].b00 + (double)f[v].l01 * (double)b[v].b01 +
                          (double)f[v].l10 * (double)b[v].b10 + (double)f[v].l11 * (double)b[v].b11;
       out[v] = log(dot) + (double)(f[v].k + b[v].k) * 0.69314718055994530942;
@@ -1294,7 +1311,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
       const unsigned gm = (Pc == 32 || warp_lockstep) ? FULL : (((1u << Pc) - 1u) << gbase);
       float4 *ring = glp_stage + ((size_t)warp * G0 + gidx) * kGroupStrideF4;
-      eval_like<V, E>(p, em, myq, ring, li, Pc, gm, L);
+      eval_like<V, (P >= 8), E>(p, em, myq, ring, li, Pc, gm, L);
 #pragma unroll
       for (int v = 0; v < V; ++v)
         if (li * V + v >= k)
