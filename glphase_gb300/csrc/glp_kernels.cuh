@@ -653,6 +653,57 @@ __device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
 
 // One backward step of impute.cpp:389-414: b <- normalise(T (b * e)), with
 // the emission picks i_ab = (father bit << 1) | mother bit of the site.
+__device__ __forceinline__ float4 pick4(const float4 em, uint32_t i00, uint32_t i01,
+                                        uint32_t i10, uint32_t i11) {
+  return make_float4(pick(em, i00), pick(em, i01), pick(em, i10), pick(em, i11));
+}
+
+// The same step with the four emission values already picked (e = pick4(...)).
+__device__ __forceinline__ void work_bwd_math(float &b0, float &b1, float &b2, float &b3,
+                                              const float4 e, const float4 t) {
+  const float b00 = __fmul_rn(b0, e.x);
+  const float b01 = __fmul_rn(b1, e.y);
+  const float b10 = __fmul_rn(b2, e.z);
+  const float b11 = __fmul_rn(b3, e.w);
+  b0 = __fadd_rn(__fadd_rn(__fmul_rn(b00, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                 __fmul_rn(b11, t.z));
+  b1 = __fadd_rn(__fadd_rn(__fmul_rn(b01, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                 __fmul_rn(b10, t.z));
+  b2 = __fadd_rn(__fadd_rn(__fmul_rn(b10, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
+                 __fmul_rn(b01, t.z));
+  b3 = __fadd_rn(__fadd_rn(__fmul_rn(b11, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
+                 __fmul_rn(b00, t.z));
+  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(b0, b1), b2), b3));
+  b0 = __fmul_rn(b0, sum);
+  b1 = __fmul_rn(b1, sum);
+  b2 = __fmul_rn(b2, sum);
+  b3 = __fmul_rn(b3, sum);
+}
+
+__device__ __forceinline__ void work_fwd_math(float &l00, float &l01, float &l10, float &l11,
+                                              const float4 e, const float4 t, bool first) {
+  if (!first) {
+    const float c00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
+    const float c01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
+    const float c10 = fma3_rn(l00, t.y, l01, t.z, l10, t.x, l11, t.y);
+    const float c11 = fma3_rn(l00, t.z, l01, t.y, l10, t.y, l11, t.x);
+    l00 = __fmul_rn(c00, e.x);
+    l01 = __fmul_rn(c01, e.y);
+    l10 = __fmul_rn(c10, e.z);
+    l11 = __fmul_rn(c11, e.w);
+  } else {
+    l00 = __fmul_rn(0.25f, e.x);
+    l01 = __fmul_rn(0.25f, e.y);
+    l10 = __fmul_rn(0.25f, e.z);
+    l11 = __fmul_rn(0.25f, e.w);
+  }
+  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(l00, l01), l10), l11));
+  l00 = __fmul_rn(l00, sum);
+  l01 = __fmul_rn(l01, sum);
+  l10 = __fmul_rn(l10, sum);
+  l11 = __fmul_rn(l11, sum);
+}
+
 __device__ __forceinline__ void work_bwd_step(float &b0, float &b1, float &b2, float &b3,
                                               const float4 em, const float4 t, uint32_t i00,
                                               uint32_t i01, uint32_t i10, uint32_t i11) {
@@ -855,6 +906,21 @@ __device__ __forceinline__ void work_chains(const GenParams &p, uint32_t s, uint
   }
 }
 
+// The four parent words of one 64-site word index, with the next word in the
+// traversal direction already loaded (a word lasts four 16-site tiles).
+struct ParentWords {
+  uint64_t cur[4], nxt[4];
+  uint32_t w;
+};
+__device__ __forceinline__ void load_words(uint64_t (&d)[4], const uint64_t *f0,
+                                           const uint64_t *f1, const uint64_t *m0,
+                                           const uint64_t *m1, uint32_t w) {
+  d[0] = __ldg(f0 + w);
+  d[1] = __ldg(f1 + w);
+  d[2] = __ldg(m0 + w);
+  d[3] = __ldg(m1 + w);
+}
+
 // Pass 1 for the 32 samples of a warp that share one chunk, with coalesced
 // staging: each 16-site tile of the 32 per-sample rows (emission, and in the
 // forward recursion the backward vectors) is copied into shared memory by the
@@ -913,6 +979,13 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
   {
     float b0 = 1.f, b1 = 1.f, b2 = 1.f, b3 = 1.f;
     const int top = (int)((S - 1) & ~(uint32_t)(kTile - 1));
+    ParentWords pw;
+    pw.w = (uint32_t)top >> 6;
+    if (valid) {
+      load_words(pw.cur, f0, f1, m0, m1, pw.w);
+      if (pw.w >= 1)
+        load_words(pw.nxt, f0, f1, m0, m1, pw.w - 1);
+    }
     stage(0, top, false);
     for (int i = 0; i < ntiles; ++i) {
       const int base = top - kTile * i, buf = i & 1;
@@ -924,10 +997,18 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
       __syncwarp();
       if (valid) {
         const uint32_t w = (uint32_t)base >> 6;
-        const uint32_t A0 = (uint32_t)(__ldg(f0 + w) >> (base & 63)),
-                       A1 = (uint32_t)(__ldg(f1 + w) >> (base & 63)),
-                       C0 = (uint32_t)(__ldg(m0 + w) >> (base & 63)),
-                       C1 = (uint32_t)(__ldg(m1 + w) >> (base & 63));
+        if (w != pw.w) {  // entered the next word (downwards): prefetch the one after
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            pw.cur[k] = pw.nxt[k];
+          pw.w = w;
+          if (w >= 1)
+            load_words(pw.nxt, f0, f1, m0, m1, w - 1);
+        }
+        const uint32_t A0 = (uint32_t)(pw.cur[0] >> (base & 63)),
+                       A1 = (uint32_t)(pw.cur[1] >> (base & 63)),
+                       C0 = (uint32_t)(pw.cur[2] >> (base & 63)),
+                       C1 = (uint32_t)(pw.cur[3] >> (base & 63));
         const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
         auto site = [&](int j) {
           const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
@@ -937,9 +1018,22 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
           beta[base + j - 1] = make_float4(b0, b1, b2, b3);
         };
         if (base >= 1 && base + kTile - 1 <= (int)S - 1) {
+          // the emission picks and transition rows of the whole tile first
+          // (independent of the recursion), then the recursion alone
+          float4 pk[kTile], tt[kTile];
 #pragma unroll
-          for (int j = kTile - 1; j >= 0; --j)
-            site(j);
+          for (int j = 0; j < kTile; ++j) {
+            const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
+                           c1b = (C1 >> j) & 1u;
+            pk[j] = pick4(erow[j], (a0 << 1) | c0b, (a0 << 1) | c1b, (a1 << 1) | c0b,
+                          (a1 << 1) | c1b);
+            tt[j] = sm.t[buf][j];
+          }
+#pragma unroll
+          for (int j = kTile - 1; j >= 0; --j) {
+            work_bwd_math(b0, b1, b2, b3, pk[j], tt[j]);
+            beta[base + j - 1] = make_float4(b0, b1, b2, b3);
+          }
         } else {
 #pragma unroll 1
           for (int j = kTile - 1; j >= 0; --j)
@@ -954,6 +1048,13 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
   __syncwarp();
   // forward recursion (impute.cpp:416-452): p_m = l_m * beta_m
   float l00 = 0, l01 = 0, l10 = 0, l11 = 0;
+  ParentWords pw;
+  pw.w = 0;
+  if (valid) {
+    load_words(pw.cur, f0, f1, m0, m1, 0);
+    if (wn > 1)
+      load_words(pw.nxt, f0, f1, m0, m1, 1);
+  }
   stage(0, 0, true);
   for (int i = 0; i < ntiles; ++i) {
     const int base = kTile * i, buf = i & 1;
@@ -965,10 +1066,18 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
     __syncwarp();
     if (valid) {
       const uint32_t w = (uint32_t)base >> 6;
-      const uint32_t A0 = (uint32_t)(__ldg(f0 + w) >> (base & 63)),
-                     A1 = (uint32_t)(__ldg(f1 + w) >> (base & 63)),
-                     C0 = (uint32_t)(__ldg(m0 + w) >> (base & 63)),
-                     C1 = (uint32_t)(__ldg(m1 + w) >> (base & 63));
+      if (w != pw.w) {  // entered the next word (upwards): prefetch the one after
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          pw.cur[k] = pw.nxt[k];
+        pw.w = w;
+        if (w + 1 < wn)
+          load_words(pw.nxt, f0, f1, m0, m1, w + 1);
+      }
+      const uint32_t A0 = (uint32_t)(pw.cur[0] >> (base & 63)),
+                     A1 = (uint32_t)(pw.cur[1] >> (base & 63)),
+                     C0 = (uint32_t)(pw.cur[2] >> (base & 63)),
+                     C1 = (uint32_t)(pw.cur[3] >> (base & 63));
       const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
       const float4 *brow = sm.b[buf] + lane * kTileStrideF4;
       auto site = [&](int j) {
@@ -981,9 +1090,22 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
                                      __fmul_rn(l10, bb.z), __fmul_rn(l11, bb.w));
       };
       if (base >= 1 && base + kTile <= (int)S) {
+        float4 pk[kTile], tt[kTile];
 #pragma unroll
-        for (int j = 0; j < kTile; ++j)
-          site(j);
+        for (int j = 0; j < kTile; ++j) {
+          const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
+                         c1b = (C1 >> j) & 1u;
+          pk[j] = pick4(erow[j], (a0 << 1) | c0b, (a0 << 1) | c1b, (a1 << 1) | c0b,
+                        (a1 << 1) | c1b);
+          tt[j] = sm.t[buf][j];
+        }
+#pragma unroll
+        for (int j = 0; j < kTile; ++j) {
+          work_fwd_math(l00, l01, l10, l11, pk[j], tt[j], false);
+          const float4 bb = brow[j];
+          beta[base + j] = make_float4(__fmul_rn(l00, bb.x), __fmul_rn(l01, bb.y),
+                                       __fmul_rn(l10, bb.z), __fmul_rn(l11, bb.w));
+        }
       } else {
 #pragma unroll 1
         for (int j = 0; j < kTile; ++j)
