@@ -48,9 +48,10 @@ namespace glp {
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 // Resident blocks per SM the one-evaluation-per-lane generation kernels are
-// compiled for: a register cap of 168 per thread keeps 12 warps per SM.
+// compiled for: a register cap of 128 per thread keeps 16 warps per SM
+// (faster than 168 registers and 12 warps; at 96 registers the loop spills).
 #ifndef GLP_MIN_BLOCKS
-#define GLP_MIN_BLOCKS 3
+#define GLP_MIN_BLOCKS 4
 #endif
 constexpr int kMinBlocks = GLP_MIN_BLOCKS;
 constexpr uint32_t kNone = 0xffffffffu;
@@ -385,8 +386,9 @@ __device__ __forceinline__ Bits8 window8(const Parents &pw, uint32_t shift) {
 __device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, uint32_t j,
                                               float &s00, float &s01, float &s10,
                                               float &s11) {
-  select4(e, (bw.f0 >> j) & 1u, (bw.f1 >> j) & 1u, (bw.m0 >> j) & 1u, (bw.m1 >> j) & 1u,
-          s00, s01, s10, s11);
+  const uint32_t bit = 1u << j;  // j is a compile-time constant in the unrolled block
+  select4(e, (bw.f0 & bit) != 0u, (bw.f1 & bit) != 0u, (bw.m0 & bit) != 0u,
+          (bw.m1 & bit) != 0u, s00, s01, s10, s11);
 }
 
 // One staged block pair for V quadruples: forward over the 8 sites of slot
