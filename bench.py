@@ -332,6 +332,9 @@ def run_ours(args):
                 "speculative_rounds": rounds,
                 "site_by_site_redos": cnt[3],
                 "lane_occupancy": round(cnt[5] / max(32 * cnt[4], 1), 4),
+                # lane-rounds run per counted evaluation: above 1 by the lanes
+                # of a chain's last round that score past its end
+                "lane_rounds_per_evaluation": round(cnt[5] / max(cnt[0], 1), 4),
                 "useful_fraction": round(N * (C + 1) / max(ev, 1), 4),
                 "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6),
                 "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
@@ -450,6 +453,8 @@ def run_uneven(args):
     clocks.start()
     t_batched = timed(batch.run, args.steps)
     ck = clocks.stop()
+    _, _, lanes_b = dev.stats()
+    cnt_b = dev.counters()
     gen = batch.generation
     batch.close()
     singles = [PreparedBatch(dev, [p], generation=gen) for p in probs]
@@ -462,7 +467,6 @@ def run_uneven(args):
     t_plain = timed(plain, args.steps)
     for s in singles:
         s.close()
-    ev, rounds, lanes = dev.stats()
     v_b = args.steps * upd / t_batched
     v_p = args.steps * upd / t_plain
     line = {
@@ -474,7 +478,11 @@ def run_uneven(args):
                                f"samples U{{100..5000}}, C={C}, own seed/founders/map each",
                    "chunks": len(shapes), "samples_total": int(sum(n for n, _ in shapes)),
                    "updates_per_step": upd, "setup_s": round(setup_s, 1),
-                   "lanes_per_sample": lanes,
+                   "lanes_per_sample": lanes_b,
+                   "accept_rate": round(cnt_b[2] / max(cnt_b[1], 1), 4),
+                   "useful_fraction": round(sum(N for N, _ in shapes) * (C + 1)
+                                            / max(cnt_b[0], 1), 4),
+                   "lane_rounds_per_evaluation": round(cnt_b[5] / max(cnt_b[0], 1), 4),
                    "plain_value": v_p, "plain_ms_per_step": t_plain / args.steps * 1e3,
                    "batched_over_plain": v_b / v_p,
                    "form": "batched = one persistent launch per generation replayed from a "

@@ -337,10 +337,17 @@ double resident_threads(Fn fn, uint32_t P, int sms) {
 }
 
 // Speculation width for N samples at acceptance rate a.  A round of P
-// evaluations keeps (1 - (1-a)^P) / (a P) of them useful; the lanes in use
-// are min(N P, threads resident with P lanes), which shrinks for small P when
-// the staging rings limit the blocks per SM.  The score is the useful
-// fraction times the share of the GPU's lanes in use.
+// evaluations keeps (1 - (1-a)^P) / (a P) of them useful.  A lane-round costs
+// kLaneRoundCost[P] relative to P = 8 when the GPU is full (measured on
+// GB300 at 4,096 sites: narrow groups stage more rows per lane, and below
+// 4 lanes the staging rings cap the resident blocks).  The kernels are
+// issue-bound, so throughput grows sublinearly with the resident warps:
+// with u = min(N P, threads resident with P lanes) / the most resident for any
+// P, lane-rounds run at (1 - e^(-4u)) / (1 - e^-4) of the full rate (4u warps
+// per scheduler; half the warps still give 0.88 of the rate).  The score is
+// useful fraction x rate / cost.
+constexpr double kLaneRoundCost[6] = {6.4, 1.66, 1.34, 1.0, 0.955, 0.953};
+
 template <class FnOf>
 uint32_t pick_lanes(double a, uint64_t N, int sms, FnOf kernel_for, double *cache = nullptr,
                     bool *known = nullptr) {
@@ -362,8 +369,9 @@ uint32_t pick_lanes(double a, uint64_t N, int sms, FnOf kernel_for, double *cach
   for (int i = 0; i < 6; ++i) {
     const uint32_t P = 1u << i;
     const double eff = (1.0 - std::pow(1.0 - a, (double)P)) / (a * P);
-    const double used = std::min((double)N * P, res[i]) / most;
-    const double score = eff * used;
+    const double u = std::min((double)N * P, res[i]) / most;
+    const double rate = (1.0 - std::exp(-4.0 * u)) / (1.0 - std::exp(-4.0));
+    const double score = eff * rate / kLaneRoundCost[i];
     if (score > best_score * 1.02) {
       best_score = score;
       best = P;

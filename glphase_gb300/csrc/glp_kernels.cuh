@@ -138,18 +138,37 @@ constexpr int kGroupF4 = 2 * kRing * kSlotF4;  // forward + backward rings
 // reads of the 8 groups of a warp start 4 banks apart and never conflict.
 constexpr int kGroupStrideF4 = kGroupF4 + 1;
 
-// Copies 8 consecutive float4 from src into dst, shared by the P lanes of a
-// group (lane li takes rows li, li + P, ...); with kWide (P >= 8) lanes 0..7
-// take one row each.
-template <bool kWide>
-__device__ __forceinline__ void stage8(float4 *dst, const float4 *src, uint32_t li, uint32_t P) {
-  if (kWide) {
-    if (li < 8)
-      cp_async16(dst + li, src + li);
+// The rows of an 8-row block that lane li of a P-lane group copies: nr rows
+// from rb.  From P = 8 up lanes 0..7 take one row each; narrower groups take
+// 8/P consecutive rows per lane, so that one copy instruction of the warp
+// writes rows 8/P apart in each group: with the groups' rings 4 banks apart,
+// the 16-byte writes of the two, four or eight groups in a quarter warp then
+// fall in disjoint banks (consecutive rows per instruction would overlap).
+struct StageRows {
+  uint32_t rb, nr;
+};
+template <int kMaxRows>
+__device__ __forceinline__ StageRows stage_rows(uint32_t li, uint32_t P) {
+  StageRows r;
+  if (kMaxRows == 1 || P >= 8) {  // kMaxRows == 1: the kernel's groups never narrow below 8
+    r.rb = li;
+    r.nr = li < 8 ? 1u : 0u;
   } else {
-    for (uint32_t k = li; k < 8; k += P)
-      cp_async16(dst + k, src + k);
+    r.nr = 8u >> (__ffs(P) - 1);  // 8 / P, P a power of two
+    r.rb = li * r.nr;
   }
+  return r;
+}
+
+// Copies 8 consecutive float4 from src into dst: this lane's rows of the
+// block (kMaxRows = 8/P bounds nr for the group size P the kernel starts with;
+// a group only widens later).
+template <int kMaxRows>
+__device__ __forceinline__ void stage8(float4 *dst, const float4 *src, StageRows r) {
+#pragma unroll
+  for (uint32_t k = 0; k < (uint32_t)kMaxRows; ++k)
+    if (k < r.nr)
+      cp_async16(dst + r.rb + k, src + r.rb + k);
 }
 
 // Sites are consumed in blocks of 8 (m0 a multiple of 8): stage(dst, m0, ..)
@@ -162,11 +181,10 @@ struct EmitF32 {
     row = p.emit + (size_t)s * p.S;
   }
   __device__ __forceinline__ float4 get1(uint32_t m) const { return __ldg(row + m); }
-  // copy the emission of sites m0..m0+7 into dst (lane li of P)
-  template <bool kWide>
-  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, uint32_t li,
-                                        uint32_t P) const {
-    stage8<kWide>(dst, row + m0, li, P);
+  // copy this lane's rows of the emission of sites m0..m0+7 into dst
+  template <int kMaxRows>
+  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, StageRows r) const {
+    stage8<kMaxRows>(dst, row + m0, r);
   }
   __device__ __forceinline__ float4 staged(const float4 *src, uint32_t j) const {
     return src[j];
@@ -189,10 +207,9 @@ struct EmitVQ {
     const uint32_t w = __ldg(col + (size_t)(m >> 3) * stride);
     return table[(w >> (28u - 4u * (m & 7u))) & 15u];
   }
-  template <bool kWide>
-  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, uint32_t li,
-                                        uint32_t) const {
-    if (li == 0)
+  template <int kMaxRows>
+  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, StageRows r) const {
+    if (r.rb == 0 && r.nr != 0)  // lane 0 of the group
       cp_async4(dst, col + (size_t)(m0 >> 3) * stride);
   }
   __device__ __forceinline__ float4 staged(const float4 *src, uint32_t j) const {
@@ -487,7 +504,7 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
 // single-word chunk runs like_forward.  All P lanes of the group call this
 // together; gmask names the lanes that synchronise at each block (the group,
 // or the whole warp when every group runs the same loop).
-template <int V, bool kWide, class E>
+template <int V, int kMaxRows, class E>
 __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
                                           const uint4 (&q)[V], float4 *stage, uint32_t li,
                                           uint32_t P, unsigned gmask, double (&out)[V]) {
@@ -534,6 +551,7 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
   }
   const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
   float4 *stF = stage, *stB = stage + kRing * kSlotF4;
+  const StageRows rows = stage_rows<kMaxRows>(li, P);
   // Block pairs t = 8 i + blk: forward sites i*64 + 8*blk .. +7 and
   // backward sites (wb - i)*64 + 8*(7 - blk) .. +7.
   const uint32_t T = nb * 8;
@@ -541,10 +559,10 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
     const uint32_t i = t >> 3, blk = t & 7u;
     const uint32_t m0 = i * 64 + blk * 8, n0 = (wb - i) * 64 + (7 - blk) * 8;
     float4 *sf = stF + (t % kRing) * kSlotF4, *sb = stB + (t % kRing) * kSlotF4;
-    stage8<kWide>(sf, tran4 + m0, li, P);
-    stage8<kWide>(sb, tran4 + n0, li, P);
-    ef.template stage<kWide>(sf + 8, m0, li, P);
-    eb.template stage<kWide>(sb + 8, n0, li, P);
+    stage8<kMaxRows>(sf, tran4 + m0, rows);
+    stage8<kMaxRows>(sb, tran4 + n0, rows);
+    ef.template stage<kMaxRows>(sf + 8, m0, rows);
+    eb.template stage<kMaxRows>(sb + 8, n0, rows);
   };
   if (T > 0)
     issue_pair(0);
@@ -587,8 +605,8 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
   auto issue_fwd = [&](uint32_t t) {
     const uint32_t m0 = (nb + (t >> 3)) * 64 + (t & 7u) * 8;
     float4 *sf = stF + (t % kRing) * kSlotF4;
-    stage8<kWide>(sf, tran4 + m0, li, P);
-    ef.template stage<kWide>(sf + 8, m0, li, P);
+    stage8<kMaxRows>(sf, tran4 + m0, rows);
+    ef.template stage<kMaxRows>(sf + 8, m0, rows);
   };
   if (T2 > 0)
     issue_fwd(0);
@@ -1435,7 +1453,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
       const unsigned gm = (Pc == 32 || warp_lockstep) ? FULL : (((1u << Pc) - 1u) << gbase);
       float4 *ring = glp_stage + ((size_t)warp * G0 + gidx) * kGroupStrideF4;
-      eval_like<V, (P >= 8), E>(p, em, myq, ring, li, Pc, gm, L);
+      eval_like<V, (P >= 8 ? 1 : 8 / P), E>(p, em, myq, ring, li, Pc, gm, L);
 #pragma unroll
       for (int v = 0; v < V; ++v)
         if (li * V + v >= k)
