@@ -1,0 +1,352 @@
+"""Input and output either side of the phasing path.
+
+* genotype likelihoods in the reference's ``.bin`` format
+  (``GLReader::LoadSTBinNames`` / ``LoadSTBinGLs``, src/glReader.cpp:64-82,
+  215-285): a tab-separated text file, optionally gzip-compressed, whose
+  header is ``chr pos allele name1 name2 ...`` and whose rows are
+  ``chrom pos alleles "het homAlt" ...`` (one space-separated pair per
+  sample);
+* genetic maps (``GeneticMap``, src/geneticMap.cpp:4-79): header
+  ``position COMBINED_rate(cM/Mb) Genetic_Map(cM)``, then space-separated
+  rows sorted by position; the genetic location of a site is linearly
+  interpolated between map rows, and the distance between two sites is the
+  difference in Morgans;
+* the phased VCF the reference writes (``Insti::save_vcf``,
+  src/insti.cpp:2098-2167): GT from the allele probabilities of the two
+  haplotypes, GP (genotype) and APP (allele) posteriors Phred-scaled;
+* the non-reference discordance (NRD) its regression tests score a phased
+  VCF by (``VCFNRD``, t/VCFComp.pm:116-131, which reads the ``NRDs`` line of
+  ``bcftools stats``): over the genotypes where truth or call is not
+  homozygous reference, the percentage whose calls differ.
+
+Host code only; the arrays it returns feed ``model.Model`` and ``phase``.
+"""
+from __future__ import annotations
+
+import gzip
+from dataclasses import dataclass, field
+
+import numpy as np
+
+F32 = np.float32
+MAP_HEADER = "position COMBINED_rate(cM/Mb) Genetic_Map(cM)"
+FLT_MAX_10_EXP = 38  # <cfloat>: the Phred value written for probability 0 is 10x this
+
+
+def _open_read(path: str):
+    with open(path, "rb") as f:
+        magic = f.read(2)
+    if magic == b"\x1f\x8b":
+        return gzip.open(path, "rt")
+    return open(path, "rt")
+
+
+def _open_write(path: str):
+    if path.endswith(".gz"):
+        return gzip.open(path, "wt")
+    return open(path, "wt")
+
+
+@dataclass
+class Sites:
+    chrom: list[str] = field(default_factory=list)
+    pos: list[int] = field(default_factory=list)
+    ref: list[str] = field(default_factory=list)
+    alt: list[str] = field(default_factory=list)
+
+    def __len__(self) -> int:
+        return len(self.pos)
+
+    def positions(self) -> np.ndarray:
+        return np.asarray(self.pos, dtype=np.int64)
+
+
+@dataclass
+class BinGLs:
+    names: list[str]
+    sites: Sites
+    gl: np.ndarray          # [N][S][2] (het, homAlt) float32, sample-major
+    not_read: int = 0       # sites past size_limit (GLReader::m_numNotRead)
+
+
+def read_bin(path: str, keep: set[str] | None = None,
+             region: tuple[str, int, int] | None = None, size_limit: int = 0) -> BinGLs:
+    """Read a ``.bin`` file (glReader.cpp:64-82, 215-285).
+
+    ``keep`` restricts the samples (file order is kept), ``region`` =
+    (chrom, first, last) keeps the sites inside it, ``size_limit`` > 0 stops
+    after that many sites and counts the rest.  The file's site-major GLs
+    come back sample-major; the reference keeps (homRef, het, homAlt) with
+    homRef = max(0, 1 - het - homAlt), which ``model.genotype_probs``
+    recomputes from (het, homAlt).  Format errors raise ValueError with the
+    reference's messages.
+    """
+    with _open_read(path) as fd:
+        header = fd.readline().rstrip("\n").split("\t")
+        if len(header) < 4:
+            raise ValueError(f"Input bin file [{path}] does not contain any sample information")
+        names = header[3:]
+        idx = [i for i, n in enumerate(names) if not keep or n in keep]
+        sites = Sites()
+        rows = []
+        not_read = 0
+        for line_num, line in enumerate(fd, start=2):
+            tokens = line.rstrip("\n").split("\t")
+            if len(tokens) != 3 + len(names):
+                raise ValueError(f"Input line {line_num} does not have the correct number of "
+                                 f"columns [{3 + len(names)}]")
+            pos = int(tokens[1])
+            if region is not None:
+                chrom, first, last = region
+                if tokens[0] != chrom or pos < first or pos > last:
+                    continue
+            if size_limit and len(sites) >= size_limit:
+                not_read += 1
+                continue
+            alleles = tokens[2]
+            if len(alleles) > 2:
+                if " " not in alleles:
+                    raise ValueError(f"Could not parse alleles [{alleles}]")
+                ref, alt = alleles.split(" ", 1)
+            else:
+                ref, alt = alleles[0], alleles[1]
+            sites.chrom.append(tokens[0])
+            sites.pos.append(pos)
+            sites.ref.append(ref)
+            sites.alt.append(alt)
+            row = np.empty((len(idx), 2), dtype=F32)
+            for k, i in enumerate(idx):
+                het, hom_alt = tokens[3 + i].split()
+                row[k] = (F32(float(het)), F32(float(hom_alt)))
+            rows.append(row)
+    if rows:
+        gl = np.ascontiguousarray(np.stack(rows, axis=1))
+    else:
+        gl = np.zeros((len(idx), 0, 2), dtype=F32)
+    return BinGLs([names[i] for i in idx], sites, gl, not_read)
+
+
+def write_bin(path: str, data: BinGLs) -> None:
+    """Write GLs in the ``.bin`` layout read_bin parses (values with nine
+    significant digits, which round-trip binary32)."""
+    N, S, _ = data.gl.shape
+    with _open_write(path) as fd:
+        fd.write("\t".join(["chr", "pos", "allele"] + list(data.names)) + "\n")
+        for m in range(S):
+            ref, alt = data.sites.ref[m], data.sites.alt[m]
+            alleles = ref + alt if len(ref) == 1 and len(alt) == 1 else f"{ref} {alt}"
+            cols = [data.sites.chrom[m], str(data.sites.pos[m]), alleles]
+            cols += [f"{float(data.gl[i, m, 0]):.9g} {float(data.gl[i, m, 1]):.9g}"
+                     for i in range(N)]
+            fd.write("\t".join(cols) + "\n")
+
+
+# ---------------------------------------------------------------------------
+# Genetic maps
+
+
+@dataclass
+class GeneticMap:
+    position: np.ndarray    # int64, strictly increasing
+    cm: np.ndarray          # float64 genetic location in cM
+
+    def location(self, pos: int) -> float:
+        """GeneticMap::GeneticLocation (geneticMap.cpp:46-70), in cM."""
+        p = self.position
+        if len(p) == 0:
+            return 0.0
+        if pos < p[0] or pos > p[-1]:
+            raise ValueError(f"Genomic location {pos} is not on genetic map")
+        hi = int(np.searchsorted(p, pos, side="left"))
+        if p[hi] == pos:
+            return float(self.cm[hi])
+        lo = hi - 1
+        diff_gen = float(self.cm[hi]) - float(self.cm[lo])
+        diff_genom = float(p[hi] - p[lo])
+        return float(self.cm[lo]) + (pos - int(p[lo])) / diff_genom * diff_gen
+
+    def distances(self, positions) -> np.ndarray:
+        """r[m] = GeneticDistance(pos[m-1], pos[m]) in Morgans
+        (geneticMap.cpp:72-79); r[0] = 0.  This is the input of
+        ``model.transition_from_distances``."""
+        pos = [int(x) for x in positions]
+        r = np.zeros(len(pos), dtype=np.float64)
+        loc = [self.location(x) for x in pos]
+        for m in range(1, len(pos)):
+            if pos[m - 1] > pos[m]:
+                raise ValueError("first is larger than second")
+            r[m] = (loc[m] - loc[m - 1]) / 100
+        return r
+
+
+def read_genetic_map(path: str) -> GeneticMap:
+    """GeneticMap::GeneticMap (geneticMap.cpp:4-44)."""
+    pos, cm = [], []
+    with _open_read(path) as fd:
+        header = fd.readline().rstrip("\n")
+        if header != MAP_HEADER:
+            raise ValueError("header of genetic map does not look right. Expected "
+                             f"'{MAP_HEADER}', but got '{header}'")
+        for row_num, line in enumerate(fd, start=2):
+            cols = line.rstrip("\n").split(" ")
+            if len(cols) != 3:
+                raise ValueError(f"Could not find three columns in line {row_num}")
+            p = int(cols[0])
+            if pos and p <= pos[-1]:
+                raise ValueError("Genetic map does not appear to be sorted by position at "
+                                 f"line {row_num}")
+            pos.append(p)
+            cm.append(float(cols[2]))
+    if not pos:
+        raise ValueError("Genetic map is empty.")
+    return GeneticMap(np.asarray(pos, dtype=np.int64), np.asarray(cm, dtype=np.float64))
+
+
+# ---------------------------------------------------------------------------
+# VCF
+
+
+def genotype_calls(prob: np.ndarray) -> np.ndarray:
+    """The GT of Insti::save_vcf (insti.cpp:2125-2137) for allele
+    probabilities ``prob`` [S][2N] (p0, p1 of each sample's two haplotypes,
+    Impute::result's layout).  Returns alleles [N][S][2] (int8): the most
+    probable of 0|0, het, 1|1 by (1-p0)(1-p1), (1-p0)p1 + p0(1-p1), p0 p1 in
+    binary32, ties towards 0|0 then het; a het is 1|0 when p0 > p1."""
+    p = np.asarray(prob, dtype=F32)
+    S, hn = p.shape
+    p0 = p[:, 0::2].T
+    p1 = p[:, 1::2].T
+    one = F32(1.0)
+    prr = (one - p0) * (one - p1)
+    pra = (one - p0) * p1 + p0 * (one - p1)
+    paa = p0 * p1
+    rr = (prr >= pra) & (prr >= paa)
+    ra = ~rr & (pra >= prr) & (pra >= paa)
+    aa = ~rr & ~ra
+    gt = np.zeros((hn // 2, S, 2), dtype=np.int8)
+    first_alt = ra & (p0 > p1)
+    gt[..., 0] = (aa | first_alt).astype(np.int8)
+    gt[..., 1] = (aa | (ra & ~first_alt)).astype(np.int8)
+    return gt
+
+
+def _phred(x: np.float32) -> np.float32:
+    if x == 0:
+        return F32(FLT_MAX_10_EXP * 10)
+    if x == 1:
+        return F32(0.0)
+    if x > 1 or x < 0:
+        raise ValueError(f"error: probability {x} is not between 0 and 1")
+    return F32(F32(-10) * np.log10(F32(x)))
+
+
+def _fmt3(x) -> str:
+    """A float the way an ostream with setprecision(3) prints it."""
+    return f"{float(x):.3g}"
+
+
+def write_vcf(path: str, sites: Sites, names: list[str], prob: np.ndarray,
+              command_line: str = "", source: str = "glphase_gb300") -> None:
+    """Phased VCF of Insti::save_vcf (insti.cpp:2098-2167): one record per
+    site with GT:GP:APP per sample, GP = Phred(P(0/0), P(het), P(1/1)) and
+    APP = Phred(p0, p1), values printed to three significant digits."""
+    p = np.asarray(prob, dtype=F32)
+    S, hn = p.shape
+    N = hn // 2
+    if len(sites) != S or len(names) != N:
+        raise ValueError(f"prob is [{S}][{hn}] for {len(sites)} sites and {len(names)} samples")
+    gt = genotype_calls(p)
+    one = F32(1.0)
+    with _open_write(path) as fd:
+        fd.write("##fileformat=VCFv4.2\n")
+        fd.write(f"##source={source}\n")
+        fd.write(f"##phaseAndImputeCall={command_line}\n")
+        fd.write(f"##contig=<ID={sites.chrom[0] if S else '.'}>\n")
+        fd.write('##FORMAT=<ID=GT,Number=1,Type=String,Description="Genotype">\n')
+        fd.write('##FORMAT=<ID=GP,Number=3,Type=Float,Description="Phred-scaled '
+                 'genotype posterior probability">\n')
+        fd.write('##FORMAT=<ID=APP,Number=2,Type=Float,Description="Phred-scaled '
+                 'allelic posterior probability, P(Allele=1|Haplotype)">\n')
+        fd.write("#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO\tFORMAT")
+        for n in names:
+            fd.write("\t" + n)
+        for m in range(S):
+            fd.write(f"\n{sites.chrom[m]}\t{sites.pos[m]}\t.\t{sites.ref[m]}\t{sites.alt[m]}"
+                     "\t100\tPASS\t.\tGT:GP:APP")
+            for i in range(N):
+                p0, p1 = p[m, 2 * i], p[m, 2 * i + 1]
+                prr = (one - p0) * (one - p1)
+                pra = (one - p0) * p1 + p0 * (one - p1)
+                paa = p0 * p1
+                ph = [_phred(F32(v)) for v in (prr, pra, paa, p0, p1)]
+                fd.write(f"\t{gt[i, m, 0]}|{gt[i, m, 1]}:" + ",".join(_fmt3(v) for v in ph[:3])
+                         + ":" + ",".join(_fmt3(v) for v in ph[3:]))
+        fd.write("\n")
+
+
+def read_vcf_gt(path: str):
+    """Sample names, sites and GT alleles [N][S][2] (int8, -1 missing) of a
+    VCF (phased '|' or unphased '/'; haploid and multi-allelic calls are
+    rejected)."""
+    names: list[str] = []
+    sites = Sites()
+    calls = []
+    with _open_read(path) as fd:
+        for line in fd:
+            if line.startswith("##"):
+                continue
+            cols = line.rstrip("\n").split("\t")
+            if line.startswith("#CHROM"):
+                names = cols[9:]
+                continue
+            if not cols or cols == [""]:
+                continue
+            fmt = cols[8].split(":")
+            if "GT" not in fmt:
+                raise ValueError(f"no GT field at {cols[0]}:{cols[1]}")
+            k = fmt.index("GT")
+            sites.chrom.append(cols[0])
+            sites.pos.append(int(cols[1]))
+            sites.ref.append(cols[3])
+            sites.alt.append(cols[4])
+            row = np.full((len(names), 2), -1, dtype=np.int8)
+            for i, field_ in enumerate(cols[9:]):
+                g = field_.split(":")[k].replace("/", "|").split("|")
+                if len(g) != 2:
+                    raise ValueError(f"not a diploid call: {field_}")
+                for j in range(2):
+                    if g[j] != ".":
+                        a = int(g[j])
+                        if a > 1:
+                            raise ValueError(f"multi-allelic call: {field_}")
+                        row[i, j] = a
+            calls.append(row)
+    gt = (np.stack(calls, axis=1) if calls else np.zeros((len(names), 0, 2), np.int8))
+    return names, sites, gt
+
+
+def nrd(truth_gt: np.ndarray, test_gt: np.ndarray) -> float:
+    """Non-reference discordance in percent (the ``NRDs`` value VCFNRD
+    reads from ``bcftools stats``, t/VCFComp.pm:116-131): with genotypes as
+    alt-allele counts, the calls where truth and test differ divided by all
+    calls except those homozygous reference in both; calls missing in either
+    are skipped.  Inputs are GT alleles [N][S][2] over the same samples and
+    sites."""
+    t = np.asarray(truth_gt)
+    q = np.asarray(test_gt)
+    if t.shape != q.shape:
+        raise ValueError(f"genotype arrays differ in shape: {t.shape} vs {q.shape}")
+    ok = (t >= 0).all(axis=-1) & (q >= 0).all(axis=-1)
+    dt = t.sum(axis=-1)[ok]
+    dq = q.sum(axis=-1)[ok]
+    considered = ~((dt == 0) & (dq == 0))
+    total = int(considered.sum())
+    if total == 0:
+        return 0.0
+    return 100.0 * int((dt != dq).sum()) / total
+
+
+def dosages(gt: np.ndarray) -> np.ndarray:
+    """Alt-allele counts [N][S] of GT alleles (-1 where missing)."""
+    g = np.asarray(gt)
+    return np.where((g >= 0).all(axis=-1), g.sum(axis=-1), -1)

@@ -1,0 +1,32 @@
+"""The end-to-end phasing loop of glphase_gb300.phase restated on the CPU
+oracle (test infrastructure): the same generations, penalties, surrogate
+draws, tallies and result, so the device pipeline can be compared with it
+bit for bit and its accuracy checked where no GPU is present."""
+from __future__ import annotations
+
+import numpy as np
+
+from glphase_gb300.batch import anneal_pen
+
+
+def oracle_phase(O, model, haps, opts, nthreads=0):
+    """Returns (prob [S][2N] float32, final haplotypes) like phase.phase."""
+    N, S, Cc = model.N, model.S, opts.cycles
+    H, wn = haps.shape
+    cur = np.ascontiguousarray(haps, dtype=np.uint64)
+    hsum = np.zeros(2 * N * S, np.uint32)
+    tallied_from = opts.sa_burnin + opts.burnin
+    for g in range(opts.generations):
+        assert not opts.knn, "the oracle loop covers the uniform sampler"
+        pb = O.OracleProblem(cur, model.emit, model.t, model.tran, model.pc, Cc)
+        quad, props = O.sample_surrogates(opts.seed, g, N, Cc, 0, H)
+        tr = pb.trace(seed=opts.seed, generation=g)
+        pen = float(anneal_pen(g, opts.sa_burnin))
+        _, cur, _ = O.generation(pb, tr, quad, props, pen, do_work=True, nthreads=nthreads)
+        if g >= tallied_from:
+            flat = np.ascontiguousarray(cur).reshape(-1)
+            for s in range(N):
+                O.lib().glpo_replace(flat, wn, S, s, hsum)
+    prob = np.zeros(2 * N * S, np.float32)
+    O.lib().glpo_result(hsum, N, S, opts.sampling, prob)
+    return prob.reshape(S, 2 * N), cur

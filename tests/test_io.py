@@ -1,0 +1,192 @@
+"""Input/output either side of the path (glphase_gb300.io): the .bin GL
+reader (glReader.cpp:64-82, 215-285), genetic maps (geneticMap.cpp), the
+VCF writer (insti.cpp:2098-2167) and NRD (t/VCFComp.pm:116-131); plus the
+reference's end-to-end phasing test t/90-phase_simulated_gls.t restated on
+the CPU oracle with the reference's own example files."""
+import gzip
+import os
+
+import numpy as np
+import pytest
+
+from glphase_gb300 import io as gio
+
+REF_SAMPLES = "/root/reference/samples/hapGen"
+
+
+def _bin(N=3, S=5, seed=0):
+    rng = np.random.default_rng(seed)
+    gl = rng.random((N, S, 2)).astype(np.float32) * 0.5
+    sites = gio.Sites(["20"] * S, [100 + 7 * m for m in range(S)],
+                      ["A", "C", "AT", "G", "T"][:S], ["G", "T", "A", "GCC", "C"][:S])
+    return gio.BinGLs([f"s{i}" for i in range(N)], sites, gl)
+
+
+@pytest.mark.parametrize("suffix", [".bin", ".bin.gz"])
+def test_bin_round_trip(tmp_path, suffix):
+    d = _bin()
+    path = str(tmp_path / ("x" + suffix))
+    gio.write_bin(path, d)
+    if suffix.endswith(".gz"):
+        with open(path, "rb") as f:
+            assert f.read(2) == b"\x1f\x8b"
+    r = gio.read_bin(path)
+    assert r.names == d.names
+    assert r.sites == d.sites
+    assert np.array_equal(r.gl, d.gl)
+    assert r.gl.dtype == np.float32 and r.gl.shape == (3, 5, 2)
+
+
+def test_bin_keep_region_and_limit(tmp_path):
+    d = _bin()
+    path = str(tmp_path / "x.bin")
+    gio.write_bin(path, d)
+    r = gio.read_bin(path, keep={"s2", "s0"})
+    assert r.names == ["s0", "s2"]
+    assert np.array_equal(r.gl, d.gl[[0, 2]])
+    r = gio.read_bin(path, region=("20", 107, 121))
+    assert r.sites.pos == [107, 114, 121]
+    r = gio.read_bin(path, size_limit=2)
+    assert r.sites.pos == [100, 107] and r.not_read == 3
+    assert r.gl.shape == (3, 2, 2)
+
+
+def test_bin_format_errors(tmp_path):
+    p = tmp_path / "bad.bin"
+    p.write_text("chr\tpos\tallele\n")
+    with pytest.raises(ValueError, match="does not contain any sample information"):
+        gio.read_bin(str(p))
+    p.write_text("chr\tpos\tallele\ta\tb\n20\t5\tAC\t0.1 0.2\n")
+    with pytest.raises(ValueError, match="Input line 2 does not have the correct number"):
+        gio.read_bin(str(p))
+    p.write_text("chr\tpos\tallele\ta\n20\t5\tACG\t0.1 0.2\n")
+    with pytest.raises(ValueError, match="Could not parse alleles"):
+        gio.read_bin(str(p))
+
+
+def test_genetic_map(tmp_path):
+    p = tmp_path / "m.map"
+    p.write_text(gio.MAP_HEADER + "\n100 0 0\n200 0 1.5\n400 0 2.5\n")
+    gm = gio.read_genetic_map(str(p))
+    assert gm.location(100) == 0.0
+    assert gm.location(200) == 1.5
+    assert gm.location(150) == pytest.approx(0.75)
+    assert gm.location(300) == pytest.approx(2.0)
+    r = gm.distances([100, 150, 300, 400])
+    assert r[0] == 0.0
+    assert r[1:] == pytest.approx([0.0075, 0.0125, 0.005])
+    with pytest.raises(ValueError, match="is not on genetic map"):
+        gm.location(401)
+    p.write_text("pos rate cm\n1 0 0\n")
+    with pytest.raises(ValueError, match="header of genetic map"):
+        gio.read_genetic_map(str(p))
+    p.write_text(gio.MAP_HEADER + "\n5 0 0\n5 0 1\n")
+    with pytest.raises(ValueError, match="sorted by position"):
+        gio.read_genetic_map(str(p))
+    p.write_text(gio.MAP_HEADER + "\n5 0\n")
+    with pytest.raises(ValueError, match="three columns"):
+        gio.read_genetic_map(str(p))
+    p.write_text(gio.MAP_HEADER + "\n")
+    with pytest.raises(ValueError, match="empty"):
+        gio.read_genetic_map(str(p))
+
+
+def test_genotype_calls_branches():
+    # columns: samples (p0, p1); one site
+    prob = np.array([[0.0, 0.0, 0.9, 0.1, 0.1, 0.9, 0.9, 0.9, 0.5, 0.5]], np.float32)
+    gt = gio.genotype_calls(prob)
+    assert gt[:, 0].tolist() == [[0, 0], [1, 0], [0, 1], [1, 1], [0, 1]]
+
+
+def test_vcf_record_text(tmp_path):
+    sites = gio.Sites(["20", "20"], [5, 9], ["A", "C"], ["G", "T"])
+    prob = np.array([[1.0, 0.0, 0.5, 0.5],
+                     [0.0, 0.0, 1.0, 1.0]], np.float32)
+    path = str(tmp_path / "o.vcf")
+    gio.write_vcf(path, sites, ["a", "b"], prob, command_line="test")
+    lines = open(path).read().split("\n")
+    assert lines[0] == "##fileformat=VCFv4.2"
+    assert lines[-1] == ""
+    body = [l for l in lines if l and not l.startswith("#")]
+    assert body[0] == ("20\t5\t.\tA\tG\t100\tPASS\t.\tGT:GP:APP\t"
+                       "1|0:380,0,380:0,380\t0|1:6.02,3.01,6.02:3.01,3.01")
+    assert body[1] == ("20\t9\t.\tC\tT\t100\tPASS\t.\tGT:GP:APP\t"
+                       "0|0:0,380,380:380,380\t1|1:380,380,0:0,0")
+    names, s2, gt = gio.read_vcf_gt(path)
+    assert names == ["a", "b"] and s2.pos == [5, 9]
+    assert np.array_equal(gt, gio.genotype_calls(prob))
+    with pytest.raises(ValueError, match="not between 0 and 1"):
+        gio.write_vcf(path, sites, ["a", "b"], prob * 2, command_line="test")
+
+
+def test_vcf_gz_round_trip(tmp_path):
+    rng = np.random.default_rng(4)
+    S, N = 40, 7
+    prob = rng.random((S, 2 * N)).astype(np.float32)
+    sites = gio.Sites(["1"] * S, list(range(10, 10 + S)), ["A"] * S, ["T"] * S)
+    path = str(tmp_path / "o.vcf.gz")
+    gio.write_vcf(path, sites, [f"n{i}" for i in range(N)], prob)
+    with gzip.open(path, "rt") as f:
+        assert f.readline().startswith("##fileformat")
+    _, _, gt = gio.read_vcf_gt(path)
+    assert np.array_equal(gt, gio.genotype_calls(prob))
+
+
+def test_nrd_definition():
+    def g(*d):  # dosages -> alleles
+        a = np.array(d)
+        return np.stack([(a >= 1), (a == 2)], -1).astype(np.int8)[None]
+    t = g(0, 0, 1, 2, 1, 0)
+    assert gio.nrd(t, t) == 0.0
+    # RR/RR pairs are not counted: one discordance among 3 counted calls
+    assert gio.nrd(t, g(0, 0, 1, 2, 2, 0)) == pytest.approx(100 / 3)
+    # a false positive at a truth RR site is counted too: 1 of 4
+    assert gio.nrd(t, g(1, 0, 1, 2, 1, 0)) == pytest.approx(25.0)
+    # phase does not matter, missing calls are skipped
+    q = g(0, 0, 1, 2, 1, 0)
+    q[0, 2] = (1, 0)
+    q[0, 3, 0] = -1
+    assert gio.nrd(t, q) == 0.0
+    assert np.array_equal(gio.dosages(q)[0], [0, 0, 1, -1, 1, 0])
+
+
+needs_samples = pytest.mark.skipif(not os.path.isdir(REF_SAMPLES),
+                                   reason="reference example files not present")
+
+
+@needs_samples
+def test_reads_reference_example_files():
+    d = gio.read_bin(os.path.join(REF_SAMPLES, "ex.bin"))
+    assert len(d.names) == 60 and len(d.sites) == 1000
+    assert d.names[0] == "samp1"
+    assert (d.sites.chrom[0], d.sites.pos[0], d.sites.ref[0], d.sites.alt[0]) == \
+        ("20", 45162, "C", "T")
+    assert tuple(d.gl[0, 0]) == (np.float32(0.008), np.float32(0.0))
+    assert (d.gl >= 0).all() and (d.gl.sum(-1) <= 1.0 + 1e-6).all()
+    gm = gio.read_genetic_map(os.path.join(REF_SAMPLES, "ex.map"))
+    r = gm.distances(d.sites.positions())
+    assert (r >= 0).all() and r[0] == 0
+    names, sites, gt = gio.read_vcf_gt(os.path.join(REF_SAMPLES, "ex.vcf.gz"))
+    assert names == d.names and sites.pos == d.sites.pos
+    assert gt.shape == (60, 1000, 2)
+
+
+@needs_samples
+def test_reference_simulated_gls_nrd(oracle_lib, tmp_path):
+    """t/90-phase_simulated_gls.t:31-37 restated: phase ex.bin with the
+    genetic map at -C100 -m 20 -B5 -i5, write the VCF, and score it against
+    the truth ex.vcf.gz: 0 < NRD < 5.5.  Runs the CPU oracle, which the
+    device pipeline matches bit for bit (tests/test_gpu_phase.py)."""
+    from glphase_gb300 import phase as ph
+    from phase_oracle import oracle_phase
+    d = gio.read_bin(os.path.join(REF_SAMPLES, "ex.bin"))
+    gm = gio.read_genetic_map(os.path.join(REF_SAMPLES, "ex.map"))
+    opts = ph.PhaseOptions(sa_burnin=5, burnin=5, sampling=20, cycles=100, seed=1)
+    m, haps = ph.prepare(d.gl, d.sites.positions(), gm, seed=opts.seed)
+    prob, _ = oracle_phase(oracle_lib, m, haps, opts)
+    out = str(tmp_path / "simulated_gls.bin.vcf.gz")
+    gio.write_vcf(out, d.sites, d.names, prob, command_line="-C100 -m 20 -B5 -i5")
+    _, _, called = gio.read_vcf_gt(out)
+    _, _, truth = gio.read_vcf_gt(os.path.join(REF_SAMPLES, "ex.vcf.gz"))
+    nrd = gio.nrd(truth, called)
+    assert 0 < nrd < 5.5, nrd
