@@ -16,6 +16,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -24,6 +25,7 @@
 #include "glp_knn.cuh"
 #include "glp_launch.h"
 #include "glp_tally.cuh"
+#include "glp_vq.cuh"
 
 namespace glp {
 
@@ -1231,6 +1233,106 @@ int glp_result(glp_ctx *c, const uint32_t *hsum, uint32_t N, uint32_t S, uint32_
   const float norm = (float)(1.0 / sn);
   glp::result_kernel<<<(unsigned)((total + 255) / 256), 256, 0, c->stream>>>(hsum, N, S, norm,
                                                                           prob_out);
+  GLP_CUDA(c, cudaGetLastError());
+  return GLP_OK;
+}
+
+int glp_vq_train(glp_ctx *c, const float *gl, uint64_t P, uint32_t K, float *codebook,
+                 uint64_t seed, uint32_t max_iter, uint32_t *iterations) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!gl || !codebook || P == 0)
+    return fail(c, GLP_ERR_ARG, "gl, codebook and num_gls are required");
+  if (K < 4 || K > (uint32_t)glp::kVQMaxCodes)
+    return fail(c, GLP_ERR_ARG, "codebook_size=%u must be in [4, %d]", K, glp::kVQMaxCodes);
+  const uint64_t nb64 = (P + glp::kVQBlock - 1) / glp::kVQBlock;
+  if (nb64 > 0x7fffffffu)
+    return fail(c, GLP_ERR_ARG, "num_gls=%llu is too large", (unsigned long long)P);
+  const uint32_t nb = (uint32_t)nb64;
+  const size_t smem = glp::vq_assign_smem(K);
+  GLP_CUDA(c, cudaFuncSetAttribute(glp::vq_assign_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  double *d_sums = nullptr, *d_var = nullptr;
+  uint32_t *d_counts = nullptr;
+  float2 *d_cb = nullptr;
+  if (cudaMalloc((void **)&d_sums, (size_t)nb * (2 * K + 1) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void **)&d_counts, (size_t)nb * K * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc((void **)&d_cb, K * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc((void **)&d_var, sizeof(double)) != cudaSuccess) {
+    release(d_sums);
+    release(d_counts);
+    release(d_cb);
+    release(d_var);
+    return fail(c, GLP_ERR_NOMEM, "codebook training scratch");
+  }
+  cudaStream_t st = c->stream;
+  auto assign = [&] {
+    glp::vq_assign_kernel<<<nb, glp::kVQThreads, smem, st>>>(gl, P, d_cb, K, d_sums, d_counts);
+  };
+  // totals of the last assignment: its squared distance, and with `move` the
+  // next entries (iteration `it`)
+  auto totals = [&](uint32_t it, bool move, double *var) -> cudaError_t {
+    glp::vq_update_kernel<<<1, 64, 0, st>>>(gl, P, nb, d_sums, d_counts, K, seed, it,
+                                            move ? d_cb : nullptr, d_var);
+    cudaError_t e = cudaMemcpyAsync(var, d_var, sizeof(double), cudaMemcpyDeviceToHost, st);
+    return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
+  };
+  cudaError_t e = cudaMemcpyAsync(d_cb, codebook, K * sizeof(float2), cudaMemcpyHostToDevice, st);
+  double cur = 0.0, prev = std::numeric_limits<double>::max(), dummy = 0.0;
+  uint32_t it = 0;
+  if (e == cudaSuccess) {
+    assign();
+    e = totals(0, false, &cur);
+  }
+  // GLVQ::BuildCodeBook's loop (glVQ.cpp:78-89)
+  while (e == cudaSuccess && std::fabs(cur - prev) > cur / 100) {
+    if (++it > max_iter) {
+      rc = fail(c, GLP_ERR_NO_CONVERGE,
+                "[GLVQ] Clustering failed to converge within %u iterations", max_iter);
+      break;
+    }
+    prev = cur;
+    e = totals(it, true, &dummy);
+    if (e != cudaSuccess)
+      break;
+    assign();
+    e = totals(it, false, &cur);
+  }
+  if (e == cudaSuccess && rc == GLP_OK)
+    e = cudaMemcpy(codebook, d_cb, K * sizeof(float2), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaGetLastError();
+  release(d_sums);
+  release(d_counts);
+  release(d_cb);
+  release(d_var);
+  if (e != cudaSuccess)
+    return fail(c, GLP_ERR_CUDA, "codebook training: %s", cudaGetErrorString(e));
+  if (iterations)
+    *iterations = std::min(it, max_iter);
+  return rc;
+}
+
+int glp_vq_pack(glp_ctx *c, const float *gl, uint32_t N, uint32_t S, const float *codebook,
+                uint32_t K, uint32_t bits, uint32_t *packed) {
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  if (!gl || !codebook || !packed || N == 0 || S == 0)
+    return fail(c, GLP_ERR_ARG, "gl, codebook, packed_out and sizes are required");
+  if (K < 4 || K > (uint32_t)glp::kVQMaxCodes)
+    return fail(c, GLP_ERR_ARG, "codebook_size=%u must be in [4, %d]", K, glp::kVQMaxCodes);
+  if ((bits != 2 && bits != 4 && bits != 8) || (1u << bits) < K)
+    return fail(c, GLP_ERR_ARG, "bits=%u must be 2, 4 or 8 with 2^bits >= codebook_size=%u",
+                bits, K);
+  glp::VQBook book;
+  for (uint32_t k = 0; k < K; ++k)
+    book.e[k] = make_float2(codebook[2 * k], codebook[2 * k + 1]);
+  const uint32_t per = 32u / bits;
+  const uint64_t total = (uint64_t)((S + per - 1) / per) * N;
+  glp::vq_pack_kernel<<<(unsigned)((total + 255) / 256), 256, 0, c->stream>>>(gl, N, S, book, K,
+                                                                            bits, packed);
   GLP_CUDA(c, cudaGetLastError());
   return GLP_OK;
 }

@@ -18,6 +18,7 @@ GLP_ERR_STATE = 4
 GLP_ERR_INDEX = 5
 GLP_ERR_DEVICE = 6
 GLP_ERR_TOO_LARGE = 7
+GLP_ERR_NO_CONVERGE = 8
 
 GLP_GEN_VQ = 1
 GLP_GEN_NO_WORK = 2
@@ -31,7 +32,8 @@ EXPORTED = [
     "glp_problem_destroy", "glp_problem_set_model", "glp_problem_set_vq", "glp_run_batch",
     "glp_problem_set_model_device", "glp_batch_prepare", "glp_batch_run", "glp_batch_launch",
     "glp_batch_destroy", "glp_run_generation_noalloc", "glp_tally", "glp_result",
-    "glp_set_evals_per_lane", "glp_get_counters", "glp_kernel_times",
+    "glp_set_evals_per_lane", "glp_get_counters", "glp_kernel_times", "glp_vq_train",
+    "glp_vq_pack",
 ]
 
 
@@ -120,6 +122,8 @@ def load(build_if_missing: bool = False):
     L.glp_run_generation_noalloc.argtypes = [C.POINTER(GenerationArgs), vp, vp, vp, vp, vp]
     L.glp_tally.argtypes = [vp, vp, u32, u32, vp]
     L.glp_result.argtypes = [vp, vp, u32, u32, u32, vp]
+    L.glp_vq_train.argtypes = [vp, vp, C.c_uint64, u32, vp, C.c_uint64, u32, vp]
+    L.glp_vq_pack.argtypes = [vp, vp, u32, u32, vp, u32, u32, vp]
     L.glp_run_batch.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs)]
     for name in EXPORTED:
         getattr(L, name)

@@ -44,7 +44,8 @@ typedef enum glp_status {
   GLP_ERR_STATE = 4,    /* a required model input was not set */
   GLP_ERR_INDEX = 5,    /* a haplotype index >= num_haps reached the device */
   GLP_ERR_DEVICE = 6,   /* no usable device */
-  GLP_ERR_TOO_LARGE = 7 /* problem exceeds the fixed scratch of glp_run_generation_noalloc */
+  GLP_ERR_TOO_LARGE = 7, /* problem exceeds the fixed scratch of glp_run_generation_noalloc */
+  GLP_ERR_NO_CONVERGE = 8 /* codebook training did not converge within max_iter iterations */
 } glp_status;
 
 typedef struct glp_ctx glp_ctx;
@@ -269,6 +270,34 @@ int glp_knn_neighbors(glp_ctx *ctx, const uint64_t *haps, uint32_t num_haps, uin
  * asynchronous. */
 int glp_tally(glp_ctx *ctx, const uint64_t *haps, uint32_t num_samples, uint32_t num_sites,
               uint32_t *hsum);
+
+/* GL vector quantisation on the device (GLVQ::BuildCodeBook,
+ * src/glVQ.cpp:26-146; GLPack::GetPackedGLs, src/glPack.cpp:112-165).
+ *
+ * glp_vq_train: Lloyd training of a codebook of K (4 <= K <= 16) (homRef,
+ * het) entries over the num_gls GL triples gl ([num_gls][3] float32, DEVICE
+ * pointer), each normalised by its sum.  codebook ([K][2] float32, HOST) holds
+ * the initial entries on entry (the reference seeds (0,1), (0,0), (1,0),
+ * (1/3,1/3) and random ones) and the trained ones on return.  Iterates until
+ * the total squared distance changes by at most 1 %, as the reference does;
+ * GLP_ERR_NO_CONVERGE after max_iter updates (the reference's limit is
+ * 1000).  A point's entry is the nearest by the reference's comparator
+ * (differences in binary32, squared distance in binary64, first smallest
+ * root); an entry's new value is the binary64 mean of its points in a fixed
+ * summation order, rounded to binary32; an entry without points moves onto
+ * the point SplitMix64 picks from (seed, iteration, entry).  *iterations
+ * (optional) receives the number of updates.  Synchronous. */
+int glp_vq_train(glp_ctx *ctx, const float *gl, uint64_t num_gls, uint32_t codebook_size,
+                 float *codebook, uint64_t seed, uint32_t max_iter, uint32_t *iterations);
+
+/* Codes of gl ([N][S][3] float32, DEVICE) packed 32/bits to a word, first
+ * site in the most significant bits, packed_out [ceil(S/(32/bits))][N]
+ * uint32 (DEVICE); sites past S take the code of the array's first GL
+ * (glPack.cpp:147-149).  bits in {2, 4} with 2^bits >= codebook_size;
+ * codebook [K][2] float32 HOST.  Asynchronous. */
+int glp_vq_pack(glp_ctx *ctx, const float *gl, uint32_t num_samples, uint32_t num_sites,
+                const float *codebook, uint32_t codebook_size, uint32_t bits,
+                uint32_t *packed_out);
 
 /* Allele probabilities from the tallies: prob_out [S][2N] = hsum / sn in
  * binary32.  Replaces Impute::result (src/impute.cpp:599-613).  DEVICE

@@ -42,6 +42,8 @@ def test_null_context_errors(lib):
     assert lib.glp_last_error(None) == b"null context"
     assert lib.glp_run_generation(None, None) == 1
     assert lib.glp_set_tran(None, None, 0) == 1
+    assert lib.glp_vq_train(None, None, 0, 16, None, 0, 10, None) == 1
+    assert lib.glp_vq_pack(None, None, 0, 0, None, 16, 4, None) == 1
 
 
 def test_shim_header_compiles():
