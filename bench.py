@@ -263,6 +263,9 @@ def run_ours(args):
 
     def step(g):
         a = eng.args(None, None, pen_for(g, w.burnin), seed=seed, generation=g, neighbors=nbr)
+        if w.panel_haps and g == 0:
+            # the first generation draws its surrogates from the panel only
+            a.sample_lo, a.sample_hi, a.kick_start = 2 * N, H, 1
         eng.launch(a)
         eng.swap()
 
