@@ -309,17 +309,28 @@ MultiFn multi_kernel(Shape sh, bool vq) {
   return vq ? glp::multi_kernel_vq(sh.P, sh.V) : glp::multi_kernel_f32(sh.P, sh.V);
 }
 
-// hmm_work of a generation: the recursions (one thread per sample), then the
-// sampling (one warp per sample).
+// hmm_work of a generation: the recursions (blocks of two warps over 32
+// samples, backward and forward at once), then the sampling (one warp per
+// sample).  The recursions' staging tiles take more than the default 48 KB
+// of shared memory: allow_chain_smem opts the kernels in on the current
+// device (at context creation, before any launch or graph capture).
+cudaError_t allow_chain_smem() {
+  cudaError_t e = cudaFuncSetAttribute(glp::work_chains_kernel<>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)glp::kChainSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(glp::work_chains_multi_kernel<>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)glp::kChainSmem);
+  return e;
+}
 void launch_work(const glp::GenParams &p, uint64_t samples, cudaStream_t st) {
-  glp::work_chains_kernel<><<<(unsigned)((samples + glp::kWorkThreads - 1) / glp::kWorkThreads),
-                              glp::kWorkThreads, 0, st>>>(p);
+  glp::work_chains_kernel<><<<(unsigned)((samples + 31) / 32), glp::kChainThreads,
+                              glp::kChainSmem, st>>>(p);
   glp::work_sample_kernel<><<<(unsigned)samples, 32, 0, st>>>(p);
 }
 void launch_work(const glp::MultiParams &mp, uint64_t samples, cudaStream_t st) {
-  glp::work_chains_multi_kernel<><<<(unsigned)((samples + glp::kWorkThreads - 1) /
-                                               glp::kWorkThreads),
-                                    glp::kWorkThreads, 0, st>>>(mp);
+  glp::work_chains_multi_kernel<><<<(unsigned)((samples + 31) / 32), glp::kChainThreads,
+                                    glp::kChainSmem, st>>>(mp);
   glp::work_sample_multi_kernel<><<<(unsigned)samples, 32, 0, st>>>(mp);
 }
 
@@ -596,7 +607,8 @@ int glp_create(int device, glp_ctx **out) {
       cudaMalloc((void **)&c->d_counter, sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc((void **)&c->d_stats, glp::kStats * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc((void **)&c->d_error, sizeof(int)) != cudaSuccess ||
-      cudaMemset(c->d_error, 0, sizeof(int)) != cudaSuccess) {
+      cudaMemset(c->d_error, 0, sizeof(int)) != cudaSuccess ||
+      allow_chain_smem() != cudaSuccess) {
     glp_destroy(c);
     return GLP_ERR_CUDA;
   }
@@ -1570,7 +1582,9 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   const size_t smem = glp::stage_bytes((int)P, 1);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, smem) != cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, smem) !=
+          cudaSuccess ||
+      (work && allow_chain_smem() != cudaSuccess))
     return GLP_ERR_CUDA;
   const uint64_t groups = (uint64_t)glp::kThreads / P;
   const uint64_t want = ((uint64_t)N + groups - 1) / groups;

@@ -775,11 +775,13 @@ __device__ __forceinline__ void work_fwd_step(float &l00, float &l01, float &l10
 
 // hmm_work is split in two passes with the reference's arithmetic unchanged.
 // The forward state l_m of impute.cpp:416-447 does not depend on the sampled
-// bits, so (1) one thread per sample runs the two sequential recursions --
-// the backward vectors beta_m (impute.cpp:389-414) and then the forward l_m --
-// and stores p_m = l_m * beta_m (the products of impute.cpp:449-452) in place
-// of beta_m; (2) the sampling of impute.cpp:453-484 then runs for every site
-// in parallel, one warp per sample and 32 sites per instruction.
+// bits, so (1) the two sequential recursions -- the backward vectors beta_m
+// (impute.cpp:389-414) and the forward l_m -- run per sample and leave
+// p_m = l_m * beta_m (the products of impute.cpp:449-452) in the scratch:
+// work_chains_split runs them at the same time on two warps, work_chains one
+// after the other on one thread (chunks mixed within a warp); (2) the
+// sampling of impute.cpp:453-484 then runs for every site in parallel, one
+// warp per sample and 32 sites per instruction.
 
 __device__ __forceinline__ uint32_t clamp_site(int m, uint32_t S) {
   return m < 0 ? 0u : ((uint32_t)m >= S ? S - 1 : (uint32_t)m);
@@ -941,12 +943,11 @@ __device__ __forceinline__ void load_words(uint64_t (&d)[4], const uint64_t *f0,
   d[3] = __ldg(m1 + w);
 }
 
-// Pass 1 for the 32 samples of a warp that share one chunk, with coalesced
-// staging: each 16-site tile of the 32 per-sample rows (emission, and in the
-// forward recursion the backward vectors) is copied into shared memory by the
-// whole warp, one 256-byte row segment per half-warp instruction (cp.async,
-// one tile in flight ahead), so every lane then reads its own row from shared
-// memory.  The recursions and their arithmetic are those of work_chains.
+// Staging of pass 1 for the 32 samples of a warp that share one chunk: each
+// 16-site tile of the 32 per-sample rows (emission, and stored vectors) is
+// copied into shared memory by the whole warp, one 256-byte row segment per
+// half-warp instruction (cp.async, one tile in flight ahead), so every lane
+// then reads its own row from shared memory.
 constexpr int kTile = 16;
 constexpr int kTileStrideF4 = kTile + 1;  // odd number of 16-byte units: no bank conflicts
 
@@ -972,8 +973,22 @@ __device__ __forceinline__ void stage_tile(float4 *dst, const float4 *const *row
   }
 }
 
-__device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s, uint4 q,
-                                                  bool valid, uint32_t lane, ChainTiles &sm) {
+// Pass 1 split over two warps that share the same 32 samples (one thread per
+// sample in each): warp 0 runs the backward recursion from the top site and
+// warp 1 the forward recursion from site 0, at the same time.  Neither
+// depends on the other until p_m = l_m * beta_m, so each runs to the middle
+// site mid storing its vectors -- beta_{m-1} for m >= mid (backward; index
+// mid-1 upwards) and l_m for m <= mid-2 (forward; l_{mid-1} stays in
+// registers) -- then, after a block barrier, each continues through the other
+// half reading what the other stored and writing p there: the backward warp
+// p_m for m <= mid-2 (beta_m fresh, l_m stored), the forward warp p_{mid-1}
+// and p_m for m >= mid (l_m fresh, beta_m stored).  The operations on every
+// vector are those of work_chains, so p is bit-identical; the sequential
+// chain per thread is half as long, which is what bounds the pass when a
+// generation has few samples.  Both warps call this together.
+__device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s, uint4 q,
+                                                  bool valid, uint32_t lane, bool fwd,
+                                                  ChainTiles &sm) {
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tr = p.tran4;
   const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
@@ -981,43 +996,51 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
   float4 *beta = p.beta + (size_t)s * S;
   sm.erow[lane] = valid ? p.emit + (size_t)s * S : nullptr;
   sm.brow[lane] = valid ? beta : nullptr;
-  if (valid)
+  if (!fwd && valid)
     beta[S - 1] = make_float4(1.f, 1.f, 1.f, 1.f);
   __syncwarp();
   const int ntiles = (int)((S + kTile - 1) / kTile);
+  const int top = (int)((S - 1) & ~(uint32_t)(kTile - 1));
+  const int mid = kTile * (ntiles / 2);            // first site of the upper half
+  const int n_hi = (top - mid) / kTile + 1;        // tiles [mid, S)
+  const int n_lo = mid / kTile;                    // tiles [0, mid)
   const float4 *const *erows = sm.erow;
   const float4 *const *brows = sm.brow;
-  auto stage = [&](int buf, int base, bool with_beta) {
+  // emission rows of the tile at base, stored vectors from bbase (with_b)
+  auto stage = [&](int buf, int base, bool with_b, int bbase) {
     stage_tile(sm.e[buf], erows, base, S, lane);
-    if (with_beta)
-      stage_tile(sm.b[buf], brows, base, S, lane);
+    if (with_b)
+      stage_tile(sm.b[buf], brows, bbase, S, lane);
     if (lane < kTile)
       cp_async16(&sm.t[buf][lane], tr + clamp_site(base + (int)lane, S));
     cp_async_commit();
   };
-  // backward recursion (impute.cpp:389-414): sites S-1 .. 1, tiles from the top
-  {
-    float b0 = 1.f, b1 = 1.f, b2 = 1.f, b3 = 1.f;
-    const int top = (int)((S - 1) & ~(uint32_t)(kTile - 1));
-    ParentWords pw;
-    pw.w = (uint32_t)top >> 6;
+  float v0 = 1.f, v1 = 1.f, v2 = 1.f, v3 = 1.f;  // beta (backward) or l (forward)
+  ParentWords pw;
+
+  // backward (impute.cpp:389-414) over n tiles from the tile at first down;
+  // comb: store p_{m-1} = l_{m-1} * beta_{m-1} (l staged one site lower)
+  auto run_bwd = [&](int first, int n, bool comb) {
+    if (n <= 0)
+      return;
+    pw.w = (uint32_t)first >> 6;
     if (valid) {
       load_words(pw.cur, f0, f1, m0, m1, pw.w);
       if (pw.w >= 1)
         load_words(pw.nxt, f0, f1, m0, m1, pw.w - 1);
     }
-    stage(0, top, false);
-    for (int i = 0; i < ntiles; ++i) {
-      const int base = top - kTile * i, buf = i & 1;
-      if (i + 1 < ntiles)
-        stage(buf ^ 1, base - kTile, false);
+    stage(0, first, comb, first - 1);
+    for (int i = 0; i < n; ++i) {
+      const int base = first - kTile * i, buf = i & 1;
+      if (i + 1 < n)
+        stage(buf ^ 1, base - kTile, comb, base - kTile - 1);
       else
         cp_async_commit();
       cp_async_wait<1>();
       __syncwarp();
       if (valid) {
         const uint32_t w = (uint32_t)base >> 6;
-        if (w != pw.w) {  // entered the next word (downwards): prefetch the one after
+        if (w != pw.w) {
 #pragma unroll
           for (int k = 0; k < 4; ++k)
             pw.cur[k] = pw.nxt[k];
@@ -1030,16 +1053,17 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
                        C0 = (uint32_t)(pw.cur[2] >> (base & 63)),
                        C1 = (uint32_t)(pw.cur[3] >> (base & 63));
         const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
-        auto site = [&](int j) {
-          const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
-                         c1b = (C1 >> j) & 1u;
-          work_bwd_step(b0, b1, b2, b3, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
-                        (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b);
-          beta[base + j - 1] = make_float4(b0, b1, b2, b3);
+        const float4 *lrow = sm.b[buf] + lane * kTileStrideF4;
+        auto store = [&](int j) {  // beta_{m-1} (or p_{m-1}) for site m = base + j
+          if (comb) {
+            const float4 l = lrow[j];
+            beta[base + j - 1] = make_float4(__fmul_rn(l.x, v0), __fmul_rn(l.y, v1),
+                                             __fmul_rn(l.z, v2), __fmul_rn(l.w, v3));
+          } else {
+            beta[base + j - 1] = make_float4(v0, v1, v2, v3);
+          }
         };
         if (base >= 1 && base + kTile - 1 <= (int)S - 1) {
-          // the emission picks and transition rows of the whole tile first
-          // (independent of the recursion), then the recursion alone
           float4 pk[kTile], tt[kTile];
 #pragma unroll
           for (int j = 0; j < kTile; ++j) {
@@ -1051,89 +1075,117 @@ __device__ __forceinline__ void work_chains_tiled(const GenParams &p, uint32_t s
           }
 #pragma unroll
           for (int j = kTile - 1; j >= 0; --j) {
-            work_bwd_math(b0, b1, b2, b3, pk[j], tt[j]);
-            beta[base + j - 1] = make_float4(b0, b1, b2, b3);
+            work_bwd_math(v0, v1, v2, v3, pk[j], tt[j]);
+            store(j);
           }
         } else {
 #pragma unroll 1
           for (int j = kTile - 1; j >= 0; --j)
-            if (base + j >= 1 && base + j <= (int)S - 1)
-              site(j);
+            if (base + j >= 1 && base + j <= (int)S - 1) {
+              const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
+                             c1b = (C1 >> j) & 1u;
+              work_bwd_step(v0, v1, v2, v3, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
+                            (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b);
+              store(j);
+            }
         }
       }
       __syncwarp();  // the buffer is refilled next iteration
     }
-  }
-  // every lane's backward vectors are stored before the warp copies them
-  __syncwarp();
-  // forward recursion (impute.cpp:416-452): p_m = l_m * beta_m
-  float l00 = 0, l01 = 0, l10 = 0, l11 = 0;
-  ParentWords pw;
-  pw.w = 0;
-  if (valid) {
-    load_words(pw.cur, f0, f1, m0, m1, 0);
-    if (wn > 1)
-      load_words(pw.nxt, f0, f1, m0, m1, 1);
-  }
-  stage(0, 0, true);
-  for (int i = 0; i < ntiles; ++i) {
-    const int base = kTile * i, buf = i & 1;
-    if (i + 1 < ntiles)
-      stage(buf ^ 1, base + kTile, true);
-    else
-      cp_async_commit();
-    cp_async_wait<1>();
-    __syncwarp();
+  };
+
+  // forward (impute.cpp:416-452) over n tiles from the tile at first up;
+  // comb: store p_m = l_m * beta_m (beta staged), else l_m for m <= mid - 2
+  auto run_fwd = [&](int first, int n, bool comb) {
+    if (n <= 0)
+      return;
+    pw.w = (uint32_t)first >> 6;
     if (valid) {
-      const uint32_t w = (uint32_t)base >> 6;
-      if (w != pw.w) {  // entered the next word (upwards): prefetch the one after
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          pw.cur[k] = pw.nxt[k];
-        pw.w = w;
-        if (w + 1 < wn)
-          load_words(pw.nxt, f0, f1, m0, m1, w + 1);
-      }
-      const uint32_t A0 = (uint32_t)(pw.cur[0] >> (base & 63)),
-                     A1 = (uint32_t)(pw.cur[1] >> (base & 63)),
-                     C0 = (uint32_t)(pw.cur[2] >> (base & 63)),
-                     C1 = (uint32_t)(pw.cur[3] >> (base & 63));
-      const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
-      const float4 *brow = sm.b[buf] + lane * kTileStrideF4;
-      auto site = [&](int j) {
-        const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
-                       c1b = (C1 >> j) & 1u;
-        work_fwd_step(l00, l01, l10, l11, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
-                      (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b, base + j == 0);
-        const float4 bb = brow[j];
-        beta[base + j] = make_float4(__fmul_rn(l00, bb.x), __fmul_rn(l01, bb.y),
-                                     __fmul_rn(l10, bb.z), __fmul_rn(l11, bb.w));
-      };
-      if (base >= 1 && base + kTile <= (int)S) {
-        float4 pk[kTile], tt[kTile];
-#pragma unroll
-        for (int j = 0; j < kTile; ++j) {
-          const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
-                         c1b = (C1 >> j) & 1u;
-          pk[j] = pick4(erow[j], (a0 << 1) | c0b, (a0 << 1) | c1b, (a1 << 1) | c0b,
-                        (a1 << 1) | c1b);
-          tt[j] = sm.t[buf][j];
-        }
-#pragma unroll
-        for (int j = 0; j < kTile; ++j) {
-          work_fwd_math(l00, l01, l10, l11, pk[j], tt[j], false);
-          const float4 bb = brow[j];
-          beta[base + j] = make_float4(__fmul_rn(l00, bb.x), __fmul_rn(l01, bb.y),
-                                       __fmul_rn(l10, bb.z), __fmul_rn(l11, bb.w));
-        }
-      } else {
-#pragma unroll 1
-        for (int j = 0; j < kTile; ++j)
-          if (base + j < (int)S)
-            site(j);
-      }
+      load_words(pw.cur, f0, f1, m0, m1, pw.w);
+      if (pw.w + 1 < wn)
+        load_words(pw.nxt, f0, f1, m0, m1, pw.w + 1);
     }
-    __syncwarp();
+    stage(0, first, comb, first);
+    for (int i = 0; i < n; ++i) {
+      const int base = first + kTile * i, buf = i & 1;
+      if (i + 1 < n)
+        stage(buf ^ 1, base + kTile, comb, base + kTile);
+      else
+        cp_async_commit();
+      cp_async_wait<1>();
+      __syncwarp();
+      if (valid) {
+        const uint32_t w = (uint32_t)base >> 6;
+        if (w != pw.w) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            pw.cur[k] = pw.nxt[k];
+          pw.w = w;
+          if (w + 1 < wn)
+            load_words(pw.nxt, f0, f1, m0, m1, w + 1);
+        }
+        const uint32_t A0 = (uint32_t)(pw.cur[0] >> (base & 63)),
+                       A1 = (uint32_t)(pw.cur[1] >> (base & 63)),
+                       C0 = (uint32_t)(pw.cur[2] >> (base & 63)),
+                       C1 = (uint32_t)(pw.cur[3] >> (base & 63));
+        const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
+        const float4 *brow = sm.b[buf] + lane * kTileStrideF4;
+        auto store = [&](int j) {  // l_m (or p_m) for site m = base + j
+          const int m = base + j;
+          if (comb) {
+            const float4 bb = brow[j];
+            beta[m] = make_float4(__fmul_rn(v0, bb.x), __fmul_rn(v1, bb.y),
+                                  __fmul_rn(v2, bb.z), __fmul_rn(v3, bb.w));
+          } else if (m <= mid - 2) {
+            beta[m] = make_float4(v0, v1, v2, v3);
+          }
+        };
+        if (base >= 1 && base + kTile <= (int)S) {
+          float4 pk[kTile], tt[kTile];
+#pragma unroll
+          for (int j = 0; j < kTile; ++j) {
+            const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
+                           c1b = (C1 >> j) & 1u;
+            pk[j] = pick4(erow[j], (a0 << 1) | c0b, (a0 << 1) | c1b, (a1 << 1) | c0b,
+                          (a1 << 1) | c1b);
+            tt[j] = sm.t[buf][j];
+          }
+#pragma unroll
+          for (int j = 0; j < kTile; ++j) {
+            work_fwd_math(v0, v1, v2, v3, pk[j], tt[j], false);
+            store(j);
+          }
+        } else {
+#pragma unroll 1
+          for (int j = 0; j < kTile; ++j)
+            if (base + j < (int)S) {
+              const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
+                             c1b = (C1 >> j) & 1u;
+              work_fwd_step(v0, v1, v2, v3, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
+                            (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b, base + j == 0);
+              store(j);
+            }
+        }
+      }
+      __syncwarp();
+    }
+  };
+
+  if (fwd)
+    run_fwd(0, n_lo, false);
+  else
+    run_bwd(top, n_hi, false);
+  // both halves' vectors are stored (block barrier: the two warps)
+  __syncthreads();
+  if (fwd) {
+    if (valid && mid >= 1) {  // p_{mid-1}: l_{mid-1} still in registers
+      const float4 bb = beta[mid - 1];
+      beta[mid - 1] = make_float4(__fmul_rn(v0, bb.x), __fmul_rn(v1, bb.y),
+                                  __fmul_rn(v2, bb.z), __fmul_rn(v3, bb.w));
+    }
+    run_fwd(mid, n_hi, true);
+  } else {
+    run_bwd(mid - kTile, n_lo, true);
   }
 }
 
@@ -1573,11 +1625,13 @@ __global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
 }
 
 // hmm_work after the generation kernel, over the published final
-// quadruples.  Pass 1: one thread per sample runs the two recursions (blocks
-// of one warp, so the few hundred warps of a generation spread over every
-// SM).  Pass 2: one warp per sample samples all sites.  Chunks without
-// hmm_work skip both.
+// quadruples.  Pass 1: blocks of two warps over 32 samples, one thread per
+// sample and recursion direction in each warp (work_chains_split), so the
+// few hundred blocks of a generation spread over every SM.  Pass 2: one warp
+// per sample samples all sites.  Chunks without hmm_work skip both.
 constexpr int kWorkThreads = 32;
+constexpr int kChainThreads = 64;
+constexpr size_t kChainSmem = 2 * sizeof(ChainTiles);  // dynamic: one per warp
 
 template <class Src>
 __device__ __forceinline__ uint4 final_quad(const Src &, const GenParams &p, uint32_t s) {
@@ -1588,9 +1642,10 @@ __device__ __forceinline__ uint4 final_quad(const Src &, const GenParams &p, uin
 
 template <class Src>
 __device__ __forceinline__ void chains_body(const Src &src) {
-  __shared__ ChainTiles s_tiles;
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;  // blocks are one warp
+  extern __shared__ __align__(16) unsigned char glp_chain_smem[];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  ChainTiles &s_tiles = reinterpret_cast<ChainTiles *>(glp_chain_smem)[warp];
+  const uint32_t g = blockIdx.x * 32u + lane;  // both warps: the block's 32 samples
   const uint32_t total = src.total();
   uint32_t c = 0, s = 0;
   if (g < total)
@@ -1599,14 +1654,16 @@ __device__ __forceinline__ void chains_body(const Src &src) {
     src.locate(total - 1, c, s);  // idle lanes borrow a valid chunk (they skip the work)
   const GenParams &p = src.chunk(c);
   const bool valid = g < total && p.do_work;
-  // the warp stages rows together when all its lanes share one chunk
+  // the warps stage rows together when all their lanes share one chunk (the
+  // two warps see the same samples, so they take the same branch and either
+  // both or neither reach the barrier in work_chains_split)
   int same = 0;
   __match_all_sync(0xffffffffu, c, &same);
   if (same) {
     if (__any_sync(0xffffffffu, valid))
-      work_chains_tiled(p, s, valid ? final_quad(src, p, s) : make_uint4(0, 0, 0, 0), valid,
-                        lane, s_tiles);
-  } else if (valid) {
+      work_chains_split(p, s, valid ? final_quad(src, p, s) : make_uint4(0, 0, 0, 0), valid,
+                        lane, warp == 1, s_tiles);
+  } else if (valid && warp == 0) {
     work_chains(p, s, final_quad(src, p, s));
   }
 }
@@ -1631,13 +1688,13 @@ __device__ __forceinline__ void sample_body(const Src &src) {
 }
 
 template <int = 0>
-__global__ void __launch_bounds__(kWorkThreads) work_chains_kernel(const GenParams p) {
+__global__ void __launch_bounds__(kChainThreads) work_chains_kernel(const GenParams p) {
   const OneChunk src{p};
   chains_body(src);
 }
 
 template <int = 0>
-__global__ void __launch_bounds__(kWorkThreads) work_chains_multi_kernel(const MultiParams mp) {
+__global__ void __launch_bounds__(kChainThreads) work_chains_multi_kernel(const MultiParams mp) {
   const ManyChunks src{mp};
   chains_body(src);
 }
