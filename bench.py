@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--cycles", type=int, default=100)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per sample (0 = auto)")
     ap.add_argument("--evals", type=int, default=0, help="evaluations per lane (0 = auto)")
+    ap.add_argument("--block-sites", type=int, default=0,
+                    help="sites per normalisation block (8, 4; 0 = auto)")
     ap.add_argument("--vq", action="store_true", help="score with 4-bit VQ GL codes")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -241,7 +243,8 @@ def run_ours(args):
         gp = GLPack(m.t, np.random.default_rng(1))
         packed, codebook = gp.packed_gls(), gp.code_book()
     eng = Engine(m.emit, m.t, m.tran, m.pc, haps, C, device=local, lanes=args.lanes,
-                 packed=packed, codebook=codebook, evals=args.evals)
+                 packed=packed, codebook=codebook, evals=args.evals,
+                 block_sites=args.block_sites)
     dev = torch.device("cuda", local)
     torch.cuda.synchronize()
     # surrogate restriction: the K nearest haplotypes by Hamming distance
@@ -334,6 +337,7 @@ def run_ours(args):
                 "evaluations_per_step": ev,
                 "speculative_rounds": rounds,
                 "site_by_site_redos": cnt[3],
+                "block_sites": eng.dev.block_sites(),
                 "lane_occupancy": round(cnt[5] / max(32 * cnt[4], 1), 4),
                 # lane-rounds run per counted evaluation: above 1 by the lanes
                 # of a chain's last round that score past its end

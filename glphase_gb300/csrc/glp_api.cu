@@ -109,6 +109,11 @@ struct glp_ctx {
   // tuning and statistics
   uint32_t lanes = 0;  // 0 = automatic
   uint32_t evals = 0;  // evaluations per lane and round, 0 = automatic
+  // sites per normalisation block (8 or 4), 0 = automatic: 8 until a
+  // generation recomputes more than 0.1 % of its evaluations site by site,
+  // then 4 for the rest of the context's life
+  uint32_t block_sites = 0;
+  bool short_blocks = false;
   // resident threads per lane width (1 .. 32), per [multi-chunk][VQ] kernel
   double resident[2][2][6] = {};
   bool resident_known[2][2] = {};
@@ -300,12 +305,17 @@ using glp::SingleFn;
 // Speculation shape of a launch: P lanes per sample, V evaluations per lane.
 struct Shape {
   uint32_t P = 1, V = 1;
+  uint32_t sub = 1;  // normalisations per 8-site block (2: every 4 sites)
 };
 
 SingleFn single_kernel(Shape sh, bool vq) {
+  if (sh.sub == 2)
+    return vq ? glp::single_kernel_vq_sub4(sh.P) : glp::single_kernel_f32_sub4(sh.P);
   return vq ? glp::single_kernel_vq(sh.P, sh.V) : glp::single_kernel_f32(sh.P, sh.V);
 }
 MultiFn multi_kernel(Shape sh, bool vq) {
+  if (sh.sub == 2)
+    return vq ? glp::multi_kernel_vq_sub4(sh.P) : glp::multi_kernel_f32_sub4(sh.P);
   return vq ? glp::multi_kernel_vq(sh.P, sh.V) : glp::multi_kernel_f32(sh.P, sh.V);
 }
 
@@ -414,6 +424,10 @@ Shape choose_shape(glp_ctx *c, uint64_t N, bool multi, bool vq) {
   Shape sh;
   sh.P = choose_lanes(c, N, multi, vq);
   sh.V = (c->evals == 2 && (sh.P == 2 || sh.P == 4 || sh.P == 8)) ? 2u : 1u;
+  if (c->block_sites == 4 || (c->block_sites == 0 && c->short_blocks)) {
+    sh.sub = 2;
+    sh.V = 1;
+  }
   return sh;
 }
 
@@ -1021,6 +1035,8 @@ int glp_finish(glp_ctx *c) {
                          cudaMemcpyDeviceToHost));
   if (c->last_chain_cycles)
     c->last_accept = (double)c->last_stats[2] / (double)c->last_chain_cycles;
+  if (c->block_sites == 0 && c->last_stats[0] && c->last_stats[3] * 1000ull > c->last_stats[0])
+    c->short_blocks = true;
   if (h_err) {
     GLP_CUDA(c, cudaMemset(c->d_error, 0, sizeof(int)));
     if (h_err & ~1)
@@ -1179,6 +1195,23 @@ int glp_set_evals_per_lane(glp_ctx *c, uint32_t evals) {
   if (evals > 2)
     return fail(c, GLP_ERR_ARG, "evaluations per lane must be 0, 1 or 2");
   c->evals = evals;
+  return GLP_OK;
+}
+
+int glp_set_block_sites(glp_ctx *c, uint32_t sites) {
+  if (!c)
+    return GLP_ERR_ARG;
+  if (sites != 0 && sites != 4 && sites != 8)
+    return fail(c, GLP_ERR_ARG, "sites per normalisation block must be 0, 4 or 8");
+  c->block_sites = sites;
+  c->short_blocks = false;
+  return GLP_OK;
+}
+
+int glp_get_block_sites(glp_ctx *c, uint32_t *sites) {
+  if (!c || !sites)
+    return GLP_ERR_ARG;
+  *sites = (c->block_sites == 4 || (c->block_sites == 0 && c->short_blocks)) ? 4u : 8u;
   return GLP_OK;
 }
 

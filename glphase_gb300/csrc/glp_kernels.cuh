@@ -410,10 +410,11 @@ __device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, u
 
 // One staged block pair for V quadruples: forward over the 8 sites of slot
 // sf, backward over the 8 sites of slot sb (highest first), then both states
-// normalised; ok[v] turns false when quadruple v may have lost range.  Every
-// staged emission and transition row is read once and used by all V
-// quadruples: 8 V independent FMA chains per lane.
-template <int V, class E>
+// normalised (kSub = 2: also after the first 4 sites of each); eacc[v]
+// collects the range codes.  Every staged emission and transition row is
+// read once and used by all V quadruples: 8 V independent FMA chains per
+// lane.
+template <int V, class E, int kSub = 1>
 __device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], const E &ef,
                                              const E &eb, const float4 *sf, const float4 *sb,
                                              const Bits8 (&wf)[V], const Bits8 (&wb)[V],
@@ -430,13 +431,18 @@ __device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], con
       fwd_fast(f[v], tx, s00, s01, s10, s11);
       bwd_fast(b[v], ty, r00, r01, r10, r11);
     }
+    if (kSub == 2 && j == 3) {
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        eacc[v] |= fwd_norm(f[v]) | bwd_norm(b[v]);
+    }
   }
 #pragma unroll
   for (int v = 0; v < V; ++v)
     eacc[v] |= fwd_norm(f[v]) | bwd_norm(b[v]);
 }
 
-template <int V, class E>
+template <int V, class E, int kSub = 1>
 __device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const float4 *sf,
                                             const Bits8 (&wf)[V], uint32_t (&eacc)[V]) {
 #pragma unroll
@@ -447,6 +453,11 @@ __device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const f
       float s00, s01, s10, s11;
       site_emission(ex, wf[v], j, s00, s01, s10, s11);
       fwd_fast(f[v], tx, s00, s01, s10, s11);
+    }
+    if (kSub == 2 && j == 3) {
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        eacc[v] |= fwd_norm(f[v]);
     }
   }
 #pragma unroll
@@ -504,7 +515,7 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
 // single-word chunk runs like_forward.  All P lanes of the group call this
 // together; gmask names the lanes that synchronise at each block (the group,
 // or the whole warp when every group runs the same loop).
-template <int V, int kMaxRows, class E>
+template <int V, int kMaxRows, class E, int kSub = 1>
 __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
                                           const uint4 (&q)[V], float4 *stage, uint32_t li,
                                           uint32_t P, unsigned gmask, double (&out)[V]) {
@@ -597,7 +608,7 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
     cp_async_wait<2>();
     __syncwarp(gmask);
     const uint32_t slot = (t % kRing) * kSlotF4;
-    both_staged8<V>(f, b, ef, eb, stF + slot, stB + slot, xf, xb, eacc);
+    both_staged8<V, E, kSub>(f, b, ef, eb, stF + slot, stB + slot, xf, xb, eacc);
     __syncwarp(gmask);
   }
   // forward-only words [nb, wf) (wn odd, or a ragged last word)
@@ -631,7 +642,7 @@ __device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
       xf[v] = window8(pf[v], blk * 8);
     cp_async_wait<2>();
     __syncwarp(gmask);
-    fwd_staged8<V>(f, ef, stF + (t % kRing) * kSlotF4, xf, eacc);
+    fwd_staged8<V, E, kSub>(f, ef, stF + (t % kRing) * kSlotF4, xf, eacc);
     __syncwarp(gmask);
   }
 #pragma unroll
@@ -1347,7 +1358,7 @@ __device__ __forceinline__ LaneGroups regroup(uint32_t lane, uint32_t na) {
   return g;
 }
 
-template <int P, int V, class E, class Src>
+template <int P, int V, class E, class Src, int kSub = 1>
 __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counter,
                                                 unsigned long long *stats, int *error,
                                                 const float4 *vq_smem) {
@@ -1505,7 +1516,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
       const unsigned gm = (Pc == 32 || warp_lockstep) ? FULL : (((1u << Pc) - 1u) << gbase);
       float4 *ring = glp_stage + ((size_t)warp * G0 + gidx) * kGroupStrideF4;
-      eval_like<V, (P >= 8 ? 1 : 8 / P), E>(p, em, myq, ring, li, Pc, gm, L);
+      eval_like<V, (P >= 8 ? 1 : 8 / P), E, kSub>(p, em, myq, ring, li, Pc, gm, L);
 #pragma unroll
       for (int v = 0; v < V; ++v)
         if (li * V + v >= k)
@@ -1603,8 +1614,10 @@ __host__ __device__ constexpr size_t stage_bytes(int P, int /*V*/) {
 }
 
 // One chunk per launch (the reference's RunHMMOnDevice granularity).  P lanes
-// per sample, V evaluations per lane and round.
-template <int P, int V, class E>
+// per sample, V evaluations per lane and round; kSub = 2 normalises every 4
+// sites instead of every 8 (for GLs confident enough that 8-site blocks
+// often leave the normalisation range).
+template <int P, int V, class E, int kSub = 1>
 __global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
     generation_kernel(const GenParams p) {
   __shared__ float4 s_vq[16];
@@ -1612,16 +1625,16 @@ __global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
     s_vq[threadIdx.x] = p.vq_table[threadIdx.x];
   __syncthreads();
   const OneChunk src{p};
-  generation_body<P, V, E>(src, p.counter, p.stats, p.error, s_vq);
+  generation_body<P, V, E, OneChunk, kSub>(src, p.counter, p.stats, p.error, s_vq);
 }
 
 // Many chunks of uneven size in one persistent launch: one queue over all
 // samples of all chunks.
-template <int P, int V, class E>
+template <int P, int V, class E, int kSub = 1>
 __global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
     generation_multi_kernel(const MultiParams mp) {
   const ManyChunks src{mp};
-  generation_body<P, V, E>(src, mp.counter, mp.stats, mp.error, nullptr);
+  generation_body<P, V, E, ManyChunks, kSub>(src, mp.counter, mp.stats, mp.error, nullptr);
 }
 
 // hmm_work after the generation kernel, over the published final

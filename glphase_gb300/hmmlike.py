@@ -101,6 +101,16 @@ class HMMLikeCUDA:
     def set_evals_per_lane(self, evals: int) -> None:
         self._c(self.L.glp_set_evals_per_lane(self.ctx, evals))
 
+    def set_block_sites(self, sites: int) -> None:
+        """Sites per normalisation block: 8, 4, or 0 = automatic."""
+        self._c(self.L.glp_set_block_sites(self.ctx, sites))
+
+    def block_sites(self) -> int:
+        """The normalisation block size the next launch uses."""
+        v = C.c_uint32(0)
+        self._c(self.L.glp_get_block_sites(self.ctx, C.byref(v)))
+        return int(v.value)
+
     def counters(self) -> list[int]:
         """[evaluations, rounds, accepts, site-by-site redos, warp rounds,
         active lanes over warp rounds] of the last generation."""
@@ -201,7 +211,7 @@ class Engine:
     def __init__(self, emit: np.ndarray, prob: np.ndarray, tran: np.ndarray, pc: np.ndarray,
                  haps: np.ndarray, num_cycles: int, device: int = 0, lanes: int = 0,
                  packed: np.ndarray | None = None, codebook: np.ndarray | None = None,
-                 evals: int = 0):
+                 evals: int = 0, block_sites: int = 0):
         import torch
         self.torch = torch
         self.dev = HMMLikeCUDA(device)
@@ -218,6 +228,7 @@ class Engine:
             self.dev.copy_packed_gls_to_device(packed)
         self.dev.set_lanes_per_sample(lanes)
         self.dev.set_evals_per_lane(evals)
+        self.dev.set_block_sites(block_sites)
         h = torch.from_numpy(np.ascontiguousarray(haps).view(np.int64))
         self.haps = h.to(self.device)
         self.hnew = self.haps.clone()

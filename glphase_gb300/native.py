@@ -33,7 +33,7 @@ EXPORTED = [
     "glp_problem_set_model_device", "glp_batch_prepare", "glp_batch_run", "glp_batch_launch",
     "glp_batch_destroy", "glp_run_generation_noalloc", "glp_tally", "glp_result",
     "glp_set_evals_per_lane", "glp_get_counters", "glp_kernel_times", "glp_vq_train",
-    "glp_vq_pack",
+    "glp_vq_pack", "glp_set_block_sites", "glp_get_block_sites",
 ]
 
 
@@ -124,6 +124,8 @@ def load(build_if_missing: bool = False):
     L.glp_result.argtypes = [vp, vp, u32, u32, u32, vp]
     L.glp_vq_train.argtypes = [vp, vp, C.c_uint64, u32, vp, C.c_uint64, u32, vp]
     L.glp_vq_pack.argtypes = [vp, vp, u32, u32, vp, u32, u32, vp]
+    L.glp_set_block_sites.argtypes = [vp, u32]
+    L.glp_get_block_sites.argtypes = [vp, vp]
     L.glp_run_batch.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs)]
     for name in EXPORTED:
         getattr(L, name)

@@ -177,6 +177,18 @@ int glp_set_lanes_per_sample(glp_ctx *ctx, uint32_t lanes);
  * speculative scheme). */
 int glp_set_evals_per_lane(glp_ctx *ctx, uint32_t evals);
 
+/* Sites per normalisation block of the likelihood (no counterpart in the
+ * reference, which rescales site by site): 8 or 4, or 0 = automatic (8 until
+ * a generation finished by glp_finish recomputed more than 0.1 % of its
+ * evaluations site by site, then 4 for the rest of the context's life).
+ * Very confident GLs can shrink an 8-site block beyond the range one
+ * normalisation covers; such evaluations are recomputed site by site
+ * (counters[3] of glp_get_counters), which 4-site blocks almost never need,
+ * at about 4 % more arithmetic.  Results are the same either way.
+ * glp_get_block_sites reports the size the next launch uses. */
+int glp_set_block_sites(glp_ctx *ctx, uint32_t sites);
+int glp_get_block_sites(glp_ctx *ctx, uint32_t *sites);
+
 /* Evaluations (scored quadruples, speculative ones included) and speculative
  * rounds of the most recent generation (after glp_finish). */
 int glp_get_stats(glp_ctx *ctx, uint64_t *evaluations, uint64_t *rounds,

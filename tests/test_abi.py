@@ -36,6 +36,8 @@ def test_library_exports_every_declared_symbol(lib):
 def test_null_context_errors(lib):
     assert lib.glp_set_lanes_per_sample(None, 4) == 1
     assert lib.glp_set_evals_per_lane(None, 2) == 1
+    assert lib.glp_set_block_sites(None, 4) == 1
+    assert lib.glp_get_block_sites(None, None) == 1
     assert lib.glp_get_counters(None, None, 0) == 1
     assert lib.glp_kernel_times(None, 0, None, None) == 1
     assert lib.glp_get_stats(None, None, None, None) == 1

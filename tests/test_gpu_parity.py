@@ -175,9 +175,58 @@ def test_tiny_emissions_take_the_site_by_site_path(dev, oracle_lib, S):
     m.emit = m.emit.copy()
     m.emit[:, 200:240] *= np.float32(1e-7)        # forward half
     m.emit[::2, S - 100:S - 80] *= np.float32(1e-9)  # backward half
-    out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
-    assert dev.counters()[3] > 0  # some evaluations took the site-by-site path
+    dev.set_block_sites(8)
+    try:
+        out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
+        assert dev.counters()[3] > 0  # some evaluations took the site-by-site path
+    finally:
+        dev.set_block_sites(0)
     check_against_oracle(oracle_lib, m, haps, quad, props, 1.0, out, 7, 1)
+
+
+def confident_problem():
+    """Sites 100..159 of every sample scaled by 1e-6: an 8-site block there
+    shrinks the state by about 2^-170, beyond one normalisation's 2^-124; a
+    4-site block by about 2^-85."""
+    m, haps, quad, props = make_problem(N=16, S=700, C=12, seed=13)
+    m.emit = m.emit.copy()
+    m.emit[:, 100:160] *= np.float32(1e-6)
+    return m, haps, quad, props
+
+
+@pytest.mark.parametrize("sites", [8, 4])
+def test_block_sites_match_oracle(dev, oracle_lib, sites):
+    m, haps, quad, props = confident_problem()
+    dev.set_block_sites(sites)
+    try:
+        assert dev.block_sites() == sites
+        out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
+        ev, redo = dev.counters()[0], dev.counters()[3]
+    finally:
+        dev.set_block_sites(0)
+    if sites == 8:
+        assert redo > 0
+    else:
+        assert redo == 0
+    check_against_oracle(oracle_lib, m, haps, quad, props, 1.0, out, 7, 1)
+
+
+def test_block_sites_switch_automatically(dev):
+    m, haps, quad, props = confident_problem()
+    dev.set_block_sites(0)
+    assert dev.block_sites() == 8
+    try:
+        run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
+        ev, redo = dev.counters()[0], dev.counters()[3]
+        assert redo * 1000 > ev
+        assert dev.block_sites() == 4    # the next launch normalises every 4 sites
+        run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=2)
+        assert dev.counters()[3] == 0
+    finally:
+        dev.set_block_sites(0)
+    assert dev.block_sites() == 8
+    with pytest.raises(nat.GlpError):
+        dev.set_block_sites(5)
 
 
 def test_counters_describe_the_generation(dev):
