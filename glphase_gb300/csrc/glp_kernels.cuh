@@ -1557,29 +1557,74 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
     const double La = __shfl_sync(FULL, Lw, srcl);
     const uint32_t sla = __shfl_sync(FULL, slw, srcl);
     const uint32_t pha = __shfl_sync(FULL, phw, srcl);
+    // The positions after the first acceptance that replace the same slot
+    // scored exactly the quadruple the sequential chain builds there (it
+    // differs from the round's start only in that slot), so the chain goes on
+    // through them -- each tested against the likelihood accepted last --
+    // up to the first position that replaces another slot.
+    uint32_t last = first_acc, hap = pha;
+    uint64_t more = 0;  // accepted positions after first_acc
+    double cur = La;
+    bool go = active && abal != 0;
+    for (uint32_t d = 1; d < 32u * V; ++d) {
+      const uint32_t r = first_acc + d;
+      go = go && r < k;
+      const uint32_t rr = go ? r : 0u, src = gbase + rr / V, vr = rr % V;
+      uint32_t sl_r = __shfl_sync(FULL, slot[0], src);
+#pragma unroll
+      for (int v = 1; v < V; ++v) {
+        const uint32_t t = __shfl_sync(FULL, slot[v], src);
+        if ((uint32_t)v == vr)
+          sl_r = t;
+      }
+      go = go && sl_r == sla;
+      if (!__any_sync(FULL, go))
+        break;
+      double L_r = __shfl_sync(FULL, L[0], src), u_r = __shfl_sync(FULL, u[0], src);
+      uint32_t ph_r = __shfl_sync(FULL, phap[0], src);
+#pragma unroll
+      for (int v = 1; v < V; ++v) {
+        const double tl = __shfl_sync(FULL, L[v], src), tu = __shfl_sync(FULL, u[v], src);
+        const uint32_t tp = __shfl_sync(FULL, phap[v], src);
+        if ((uint32_t)v == vr) {
+          L_r = tl;
+          u_r = tu;
+          ph_r = tp;
+        }
+      }
+      if (go) {
+        last = r;
+        if (L_r >= cur || u_r < exp((L_r - cur) * (double)p.pen)) {
+          cur = L_r;
+          hap = ph_r;
+          more |= 1ull << r;
+        }
+      }
+    }
     if (active) {
       curr = curr0;
       if (abal) {
-        set_slot(q, sla, pha);
-        curr = La;
+        set_slot(q, sla, hap);
+        curr = cur;
       }
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       const uint32_t r = li * V + v, ev = e + r;
-      if (r < k && r <= first_acc) {
+      if (r < k && r <= last) {
         if (p.eval_trace)
           p.eval_trace[(size_t)s * (C + 1) + ev] = L[v];
         if (ev > 0 && p.accept_trace)
-          p.accept_trace[(size_t)s * C + ev - 1] = (uint8_t)(r == first_acc);
+          p.accept_trace[(size_t)s * C + ev - 1] =
+              (uint8_t)(r == first_acc || ((more >> r) & 1ull));
       }
     }
     if (active) {
-      e = (first_acc < PV) ? e + first_acc + 1 : e + k;
+      e = (first_acc < PV) ? e + last + 1 : e + k;
       if (li == 0) {
         n_evals += k;
         ++n_rounds;
-        n_acc += first_acc < PV ? 1u : 0u;
+        n_acc += first_acc < PV ? 1u + (uint32_t)__popcll(more) : 0u;
       }
     }
 
