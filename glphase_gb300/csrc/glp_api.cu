@@ -119,6 +119,10 @@ struct glp_ctx {
   bool resident_known[2][2] = {};
   uint32_t lanes_used = 4;
   double last_accept = -1.0;  // acceptance rate of the last generation
+  // annealing penalty of the last launch, and of the generation last_accept
+  // was measured on: the acceptance rate only predicts a generation run at
+  // the same penalty (it falls several-fold while the penalty ramps up)
+  float launch_pen = -1.0f, accept_pen = -2.0f;
   uint64_t last_chain_cycles = 0;
   unsigned long long last_stats[glp::kStats] = {};
   // device-time record of the last kTimed generations launched from the host
@@ -369,7 +373,7 @@ double resident_threads(Fn fn, uint32_t P, int sms) {
 // rate(u) = u (1 + h) / (u + h), h = 0.08 (measured: 0.93 of the full rate at
 // half the warps, 0.87 between u = 0.21 and 0.41 on 2,000 samples x 8,192
 // sites).  The score is useful fraction x rate / cost.
-constexpr double kLaneRoundCost[6] = {6.4, 1.66, 1.34, 1.0, 0.955, 0.953};
+constexpr double kLaneRoundCost[6] = {6.4, 2.44, 1.34, 1.0, 0.955, 0.953};
 
 template <class FnOf>
 uint32_t pick_lanes(double a, uint64_t N, int sms, FnOf kernel_for, double *cache = nullptr,
@@ -404,10 +408,12 @@ uint32_t pick_lanes(double a, uint64_t N, int sms, FnOf kernel_for, double *cach
   return best;
 }
 
-uint32_t choose_lanes(glp_ctx *c, uint64_t N, bool multi, bool vq) {
+uint32_t choose_lanes(glp_ctx *c, uint64_t N, bool multi, bool vq, float pen) {
   if (c->lanes)
     return c->lanes;
-  const double a = c->last_accept < 0 ? 0.12 : std::max(c->last_accept, 1e-3);
+  const double a = (c->last_accept < 0 || pen != c->accept_pen)
+                       ? 0.12
+                       : std::max(c->last_accept, 1e-3);
   return pick_lanes(
       a, N, c->sms,
       [&](uint32_t P) {
@@ -420,9 +426,10 @@ uint32_t choose_lanes(glp_ctx *c, uint64_t N, bool multi, bool vq) {
 
 // Lanes from choose_lanes; two evaluations per lane only on request
 // (glp_set_evals_per_lane), and only where that kernel exists (P = 2, 4, 8).
-Shape choose_shape(glp_ctx *c, uint64_t N, bool multi, bool vq) {
+Shape choose_shape(glp_ctx *c, uint64_t N, bool multi, bool vq, float pen) {
   Shape sh;
-  sh.P = choose_lanes(c, N, multi, vq);
+  sh.P = choose_lanes(c, N, multi, vq, pen);
+  c->launch_pen = pen;
   sh.V = (c->evals == 2 && (sh.P == 2 || sh.P == 4 || sh.P == 8)) ? 2u : 1u;
   if (c->block_sites == 4 || (c->block_sites == 0 && c->short_blocks)) {
     sh.sub = 2;
@@ -550,7 +557,7 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
   if (rc)
     return rc;
   const bool vq = (a->flags & GLP_GEN_VQ) != 0;
-  const Shape sh = choose_shape(c, a->num_samples, false, vq);
+  const Shape sh = choose_shape(c, a->num_samples, false, vq, a->pen);
   const uint32_t P = sh.P;
   SingleFn fn = single_kernel(sh, vq);
   const unsigned grid = grid_for(c, fn, a->num_samples, P, sh.V, &rc);
@@ -844,7 +851,7 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   mp.counter = c->d_counter;
   mp.stats = c->d_stats;
   mp.error = c->d_error;
-  const Shape sh = choose_shape(c, total, true, vq);
+  const Shape sh = choose_shape(c, total, true, vq, c->h_table[0].pen);
   const uint32_t P = sh.P;
   MultiFn fn = multi_kernel(sh, vq);
   const unsigned grid = grid_for(c, fn, total, P, sh.V, &rc);
@@ -972,7 +979,7 @@ int glp_batch_prepare(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   b->mp.counter = c->d_counter;
   b->mp.stats = c->d_stats;
   b->mp.error = c->d_error;
-  const Shape sh = choose_shape(c, total, true, vq);
+  const Shape sh = choose_shape(c, total, true, vq, table[0].pen);
   b->P = sh.P;
   b->V = sh.V;
   b->fn = multi_kernel(sh, vq);
@@ -1033,8 +1040,10 @@ int glp_finish(glp_ctx *c) {
   GLP_CUDA(c, cudaMemcpy(&h_err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost));
   GLP_CUDA(c, cudaMemcpy(c->last_stats, c->d_stats, sizeof(c->last_stats),
                          cudaMemcpyDeviceToHost));
-  if (c->last_chain_cycles)
+  if (c->last_chain_cycles) {
     c->last_accept = (double)c->last_stats[2] / (double)c->last_chain_cycles;
+    c->accept_pen = c->launch_pen;
+  }
   if (c->block_sites == 0 && c->last_stats[0] && c->last_stats[3] * 1000ull > c->last_stats[0])
     c->short_blocks = true;
   if (h_err) {
