@@ -85,7 +85,7 @@ def workload(args, rank):
 # the batched workload at S = 1,024 (N = 10,000, C = 100, 8 lanes, float
 # emission); the traffic grows in proportion to S (emission rows per scored
 # site), so the full-size figure is this one scaled by S / 1,024.
-NCU_TRAFFIC_S1024 = 1.285192e9 + 0.003168e9
+NCU_TRAFFIC_S1024 = 1.426213e9 + 0.003265e9
 
 
 def traffic_per_launch(N, S, C, args):
