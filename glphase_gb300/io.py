@@ -6,6 +6,9 @@
   header is ``chr pos allele name1 name2 ...`` and whose rows are
   ``chrom pos alleles "het homAlt" ...`` (one space-separated pair per
   sample);
+* genotype likelihoods in a VCF's GL (log10) or PL (Phred) field
+  (``GLReader::LoadBCFGLs``, src/glReader.cpp:100-200; text VCF, optionally
+  gzip-compressed, without htslib);
 * genetic maps (``GeneticMap``, src/geneticMap.cpp:4-79): header
   ``position COMBINED_rate(cM/Mb) Genetic_Map(cM)``, then space-separated
   rows sorted by position; the genetic location of a site is linearly
@@ -29,6 +32,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 F32 = np.float32
+FLT_MIN_10_EXP = -37  # <cfloat>
 MAP_HEADER = "position COMBINED_rate(cM/Mb) Genetic_Map(cM)"
 FLT_MAX_10_EXP = 38  # <cfloat>: the Phred value written for probability 0 is 10x this
 
@@ -69,6 +73,30 @@ class BinGLs:
     not_read: int = 0       # sites past size_limit (GLReader::m_numNotRead)
 
 
+def gl_pair(hom_ref, het, hom_alt) -> tuple[np.float32, np.float32]:
+    """What the reference keeps of a GL trio (drop_first_aware_add_gl_trio
+    with ST_DROP_FIRST, glReader.cpp:202-213, insti.cpp:219): het / sum and
+    homAlt / sum, sum = (homRef + het) + homAlt, all binary32."""
+    hr, h, a = F32(hom_ref), F32(het), F32(hom_alt)
+    s = F32(F32(hr + h) + a)
+    return F32(h / s), F32(a / s)
+
+
+def gl2prob(val) -> np.float32:
+    """Bio::gl2prob (bio.hpp:154-161): 10^val in binary32, clamped to [0, 1]."""
+    with np.errstate(over="ignore"):
+        t = np.power(F32(10), F32(val))
+    return F32(min(max(t, F32(0)), F32(1)))
+
+
+def phred2prob(phred: int) -> np.float32:
+    """Bio::phred2prob (bio.hpp:163-170): 0 beyond the binary32 range, else
+    10^(-phred/10) with the exponent in binary32 and the power in binary64."""
+    if phred > FLT_MIN_10_EXP * -10:
+        return F32(0)
+    return F32(10.0 ** float(F32(-F32(phred)) / F32(10)))
+
+
 def read_bin(path: str, keep: set[str] | None = None,
              region: tuple[str, int, int] | None = None, size_limit: int = 0) -> BinGLs:
     """Read a ``.bin`` file (glReader.cpp:64-82, 215-285).
@@ -76,10 +104,9 @@ def read_bin(path: str, keep: set[str] | None = None,
     ``keep`` restricts the samples (file order is kept), ``region`` =
     (chrom, first, last) keeps the sites inside it, ``size_limit`` > 0 stops
     after that many sites and counts the rest.  The file's site-major GLs
-    come back sample-major; the reference keeps (homRef, het, homAlt) with
-    homRef = max(0, 1 - het - homAlt), which ``model.genotype_probs``
-    recomputes from (het, homAlt).  Format errors raise ValueError with the
-    reference's messages.
+    come back sample-major as the reference keeps them: the trio
+    (max(0, 1 - het - homAlt), het, homAlt) through ``gl_pair``.  Format
+    errors raise ValueError with the reference's messages.
     """
     with _open_read(path) as fd:
         header = fd.readline().rstrip("\n").split("\t")
@@ -115,9 +142,86 @@ def read_bin(path: str, keep: set[str] | None = None,
             sites.ref.append(ref)
             sites.alt.append(alt)
             row = np.empty((len(idx), 2), dtype=F32)
+            one, zero = F32(1), F32(0)
             for k, i in enumerate(idx):
                 het, hom_alt = tokens[3 + i].split()
-                row[k] = (F32(float(het)), F32(float(hom_alt)))
+                h, a = F32(float(het)), F32(float(hom_alt))
+                row[k] = gl_pair(max(zero, F32(F32(one - h) - a)), h, a)
+            rows.append(row)
+    if rows:
+        gl = np.ascontiguousarray(np.stack(rows, axis=1))
+    else:
+        gl = np.zeros((len(idx), 0, 2), dtype=F32)
+    return BinGLs([names[i] for i in idx], sites, gl, not_read)
+
+
+def read_vcf_gls(path: str, tags=("GL", "PL"), keep: set[str] | None = None,
+                 region: tuple[str, int, int] | None = None, size_limit: int = 0) -> BinGLs:
+    """GLs from a VCF (GLReader::LoadBCFGLs, glReader.cpp:100-200): the first
+    of ``tags`` the header declares as a FORMAT field; GL values through
+    ``gl2prob``, PL through ``phred2prob``, each trio through ``gl_pair``.
+    Biallelic records only.  A missing value (".") is read as a flat
+    likelihood (the reference would carry a NaN).  Returns the .bin reader's
+    structure."""
+    declared: set[str] = set()
+    names: list[str] = []
+    idx: list[int] = []
+    tag = None
+    sites = Sites()
+    rows = []
+    not_read = 0
+    with _open_read(path) as fd:
+        for line in fd:
+            if line.startswith("##"):
+                if line.startswith("##FORMAT=<ID="):
+                    declared.add(line[len("##FORMAT=<ID="):].split(",", 1)[0])
+                continue
+            cols = line.rstrip("\n").split("\t")
+            if line.startswith("#CHROM"):
+                names = cols[9:]
+                idx = [i for i, n in enumerate(names) if not keep or n in keep]
+                tag = next((t for t in tags if t in ("GL", "PL") and t in declared), None)
+                if tag is None:
+                    raise ValueError("[GLReader] Could not find a known tag")
+                continue
+            if len(cols) < 9:
+                continue
+            pos = int(cols[1])
+            if region is not None:
+                chrom, first, last = region
+                if cols[0] != chrom or pos < first or pos > last:
+                    continue
+            if size_limit and len(sites) >= size_limit:
+                not_read += 1
+                continue
+            alts = [] if cols[4] == "." else cols[4].split(",")
+            if len(alts) < 1:
+                raise ValueError("Too few alleles in BCF record")
+            if len(alts) > 1:
+                raise ValueError("More than two alleles per record are not supported. Please "
+                                 "break BCF into biallelics using bcftools norm -m -")
+            fmt = cols[8].split(":")
+            if tag not in fmt:
+                raise ValueError(f"no {tag} value at {cols[0]}:{cols[1]}")
+            k = fmt.index(tag)
+            row = np.empty((len(idx), 2), dtype=F32)
+            for j, i in enumerate(idx):
+                fields = cols[9 + i].split(":")
+                vals = fields[k].split(",") if k < len(fields) else ["."]
+                if len(vals) != 3:
+                    if vals == ["."]:
+                        vals = [".", ".", "."]
+                    else:
+                        raise ValueError(f"Returned number of values is not correct: {len(vals)}")
+                if tag == "GL":
+                    trio = [gl2prob(0.0 if v == "." else float(v)) for v in vals]
+                else:
+                    trio = [phred2prob(0 if v == "." else int(v)) for v in vals]
+                row[j] = gl_pair(*trio)
+            sites.chrom.append(cols[0])
+            sites.pos.append(pos)
+            sites.ref.append(cols[3])
+            sites.alt.append(alts[0])
             rows.append(row)
     if rows:
         gl = np.ascontiguousarray(np.stack(rows, axis=1))

@@ -96,11 +96,16 @@ def prepare(gl_het_alt: np.ndarray, positions: np.ndarray,
 def phase_bin(bin_path: str, vcf_path: str | None = None, map_path: str | None = None,
               opts: PhaseOptions | None = None, keep: set[str] | None = None,
               command_line: str = ""):
-    """Phase the samples of a ``.bin`` GL file and (optionally) write the
-    phased VCF: ``insti -g map -C.. -B.. -i.. -m.. file.bin`` on one GPU.
-    Returns (prob [S][2N], the parsed input)."""
+    """Phase the samples of a GL file and (optionally) write the phased VCF:
+    ``insti -g map -C.. -B.. -i.. -m.. file.bin`` (or ``-Fbcf file.vcf.gz``)
+    on one GPU.  ``.vcf`` / ``.vcf.gz`` files are read for their GL or PL
+    field, anything else as ``.bin``.  Returns (prob [S][2N], the parsed
+    input)."""
     opts = opts or PhaseOptions()
-    data = gio.read_bin(bin_path, keep=keep)
+    if bin_path.endswith((".vcf", ".vcf.gz")):
+        data = gio.read_vcf_gls(bin_path, keep=keep)
+    else:
+        data = gio.read_bin(bin_path, keep=keep)
     gmap = gio.read_genetic_map(map_path) if map_path else None
     m, haps = prepare(data.gl, data.sites.positions(), gmap, seed=opts.seed)
     prob, _ = phase(m, haps, opts)

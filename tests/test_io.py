@@ -33,7 +33,11 @@ def test_bin_round_trip(tmp_path, suffix):
     r = gio.read_bin(path)
     assert r.names == d.names
     assert r.sites == d.sites
-    assert np.array_equal(r.gl, d.gl)
+    one = np.float32(1)
+    want = np.array([[gio.gl_pair(max(np.float32(0), (one - h) - a), h, a) for h, a in row]
+                     for row in d.gl], dtype=np.float32)
+    assert np.array_equal(r.gl, want)
+    assert np.allclose(r.gl, d.gl, rtol=1e-6, atol=0)
     assert r.gl.dtype == np.float32 and r.gl.shape == (3, 5, 2)
 
 
@@ -43,7 +47,7 @@ def test_bin_keep_region_and_limit(tmp_path):
     gio.write_bin(path, d)
     r = gio.read_bin(path, keep={"s2", "s0"})
     assert r.names == ["s0", "s2"]
-    assert np.array_equal(r.gl, d.gl[[0, 2]])
+    assert np.array_equal(r.gl, gio.read_bin(path).gl[[0, 2]])
     r = gio.read_bin(path, region=("20", 107, 121))
     assert r.sites.pos == [107, 114, 121]
     r = gio.read_bin(path, size_limit=2)
@@ -62,6 +66,53 @@ def test_bin_format_errors(tmp_path):
     p.write_text("chr\tpos\tallele\ta\n20\t5\tACG\t0.1 0.2\n")
     with pytest.raises(ValueError, match="Could not parse alleles"):
         gio.read_bin(str(p))
+
+
+def test_gl_conversions():
+    """Bio::gl2prob / Bio::phred2prob (bio.hpp:154-170) and the GL trio the
+    reference keeps (glReader.cpp:202-213)."""
+    assert gio.gl2prob(0.0) == 1.0 and gio.gl2prob(2.0) == 1.0
+    assert gio.gl2prob(-1.0) == np.float32(np.power(np.float32(10), np.float32(-1)))
+    assert gio.phred2prob(0) == 1.0
+    assert gio.phred2prob(10) == np.float32(0.1)
+    assert gio.phred2prob(370) == np.float32(1e-37) and gio.phred2prob(371) == 0.0
+    h, a = gio.gl_pair(np.float32(0.992), np.float32(0.008), np.float32(0))
+    s = np.float32(np.float32(0.992) + np.float32(0.008))
+    assert (h, a) == (np.float32(np.float32(0.008) / s), np.float32(0))
+    assert gio.gl_pair(1, 1, 1) == (np.float32(1 / 3), np.float32(1 / 3))
+
+
+VCF_HEAD = """##fileformat=VCFv4.2
+##FORMAT=<ID=GT,Number=1,Type=String,Description="Genotype">
+##FORMAT=<ID={tag},Number=G,Type={kind},Description="likelihoods">
+#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO\tFORMAT\ta\tb
+"""
+
+
+def test_vcf_gl_and_pl(tmp_path):
+    p = tmp_path / "g.vcf"
+    p.write_text(VCF_HEAD.format(tag="GL", kind="Float") +
+                 "1\t10\t.\tA\tG\t.\t.\t.\tGT:GL\t0/0:0,-1,-2\t./.:.\n"
+                 "1\t20\t.\tAC\tA\t.\t.\t.\tGL\t-2,0,-2\t-3,-1,0\n")
+    r = gio.read_vcf_gls(str(p))
+    assert r.names == ["a", "b"] and r.sites.pos == [10, 20] and r.sites.alt == ["G", "A"]
+    t = [gio.gl2prob(v) for v in (0.0, -1.0, -2.0)]
+    assert tuple(r.gl[0, 0]) == gio.gl_pair(*t)
+    assert tuple(r.gl[1, 0]) == gio.gl_pair(1, 1, 1)      # missing: flat
+    p.write_text(VCF_HEAD.format(tag="PL", kind="Integer") +
+                 "1\t10\t.\tA\tG\t.\t.\t.\tPL\t0,10,20\t400,0,30\n")
+    r = gio.read_vcf_gls(str(p))
+    assert tuple(r.gl[0, 0]) == gio.gl_pair(*[gio.phred2prob(v) for v in (0, 10, 20)])
+    assert gio.phred2prob(400) == 0.0
+    assert tuple(r.gl[1, 0]) == gio.gl_pair(*[gio.phred2prob(v) for v in (400, 0, 30)])
+    assert r.gl[1, 0, 0] > 0.99
+    p.write_text(VCF_HEAD.format(tag="PL", kind="Integer") +
+                 "1\t10\t.\tA\tG,T\t.\t.\t.\tPL\t0,1,2,3,4,5\t0,1,2,3,4,5\n")
+    with pytest.raises(ValueError, match="More than two alleles"):
+        gio.read_vcf_gls(str(p))
+    p.write_text(VCF_HEAD.format(tag="DS", kind="Float"))
+    with pytest.raises(ValueError, match="Could not find a known tag"):
+        gio.read_vcf_gls(str(p))
 
 
 def test_genetic_map(tmp_path):
@@ -169,17 +220,23 @@ def test_reads_reference_example_files():
     names, sites, gt = gio.read_vcf_gt(os.path.join(REF_SAMPLES, "ex.vcf.gz"))
     assert names == d.names and sites.pos == d.sites.pos
     assert gt.shape == (60, 1000, 2)
+    v = gio.read_vcf_gls(os.path.join(REF_SAMPLES, "ex.gls.vcf.gz"))
+    assert v.names == d.names and v.sites.pos == d.sites.pos and v.gl.shape == (60, 1000, 2)
+    assert (v.gl >= 0).all() and (v.gl.sum(-1) <= 1.0 + 1e-6).all()
 
 
 @needs_samples
-def test_reference_simulated_gls_nrd(oracle_lib, tmp_path):
-    """t/90-phase_simulated_gls.t:31-37 restated: phase ex.bin with the
-    genetic map at -C100 -m 20 -B5 -i5, write the VCF, and score it against
-    the truth ex.vcf.gz: 0 < NRD < 5.5.  Runs the CPU oracle, which the
-    device pipeline matches bit for bit (tests/test_gpu_phase.py)."""
+@pytest.mark.parametrize("source", ["ex.bin", "ex.gls.vcf.gz"])
+def test_reference_simulated_gls_nrd(oracle_lib, tmp_path, source):
+    """t/90-phase_simulated_gls.t:31-50 restated: phase ex.bin (and the same
+    samples' GLs from ex.gls.vcf.gz) with the genetic map at -C100 -m 20 -B5
+    -i5, write the VCF, and score it against the truth ex.vcf.gz:
+    0 < NRD < 5.5.  Runs the CPU oracle, which the device pipeline matches
+    bit for bit (tests/test_gpu_phase.py)."""
     from glphase_gb300 import phase as ph
     from phase_oracle import oracle_phase
-    d = gio.read_bin(os.path.join(REF_SAMPLES, "ex.bin"))
+    path = os.path.join(REF_SAMPLES, source)
+    d = gio.read_bin(path) if source.endswith(".bin") else gio.read_vcf_gls(path)
     gm = gio.read_genetic_map(os.path.join(REF_SAMPLES, "ex.map"))
     opts = ph.PhaseOptions(sa_burnin=5, burnin=5, sampling=20, cycles=100, seed=1)
     m, haps = ph.prepare(d.gl, d.sites.positions(), gm, seed=opts.seed)
