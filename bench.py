@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the untimed full-schedule phasing accuracy run")
     ap.add_argument("--uniform", action="store_true",
                     help="uniform surrogates instead of the configuration's kNN restriction")
     ap.add_argument("--chunks", type=int, default=64, help="uneven workload: chunk count")
@@ -78,7 +80,30 @@ def workload(args, rank):
     rp = replicas.plan(w.seed, rank=rank, world=max(rank + 1, dist_env()[0]))
     ds = synth.generate(w, N=N, S=S, seed=rp.data_seed)
     m, haps = synth.initial_state(ds, seed=7 + rank)
+    workload.dataset = ds
     return w, m, haps
+
+
+def accuracy(w, m, haps, ds, seed, device):
+    """Phasing accuracy of the workload's full schedule (burn-in + sampling
+    generations, the configuration's surrogate sampler, device tallies and
+    result; glphase_gb300.phase): NRD of the called genotypes against the
+    synthetic truth, beside the NRD of calling each genotype from its GLs
+    alone.  Not timed."""
+    from glphase_gb300 import io as gio, phase as ph
+    N = m.N
+    opts = ph.PhaseOptions(sa_burnin=w.burnin, burnin=0, sampling=w.sampling, cycles=w.cycles,
+                           seed=seed, knn=w.knn, cluster_start=0,
+                           kick_start=bool(w.panel_haps), device=device)
+    prob, _ = ph.phase(m, haps, opts)
+    truth = np.stack([ds.truth[0:2 * N:2], ds.truth[1:2 * N:2]], axis=-1).astype(np.int8)
+    call = np.argmax(m.t, axis=-1)
+    gl_only = np.stack([call >= 1, call == 2], axis=-1).astype(np.int8)
+    return {"nrd_percent": round(gio.nrd(truth, gio.genotype_calls(prob)), 3),
+            "nrd_gl_only_percent": round(gio.nrd(truth, gl_only), 3),
+            "generations": opts.generations,
+            "sampler": f"kNN K={w.knn}" if w.knn else "uniform",
+            "truth": "synthetic haplotypes the GLs were simulated from"}
 
 
 # DRAM bytes (read + write) of one generation_kernel launch measured by ncu on
@@ -362,6 +387,8 @@ def run_ours(args):
             line["e2e"] = e2e
         if base:
             line["cpu_baseline"] = base
+        if not args.no_accuracy:
+            line["accuracy"] = accuracy(w, m, haps, workload.dataset, seed, local)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

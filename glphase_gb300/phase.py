@@ -16,7 +16,9 @@ the final probabilities and haplotypes come back.
 The surrogate sampler is uniform over all other haplotypes
 (``UnifSampler``), or, from generation ``cluster_start`` on, the K nearest
 haplotypes by Hamming distance built on the device from the haplotypes of
-that generation (``KNN``, kNN.cpp:99-206).
+that generation (``KNN``, kNN.cpp:99-206).  With reference-panel rows after
+the 2N sample haplotypes, ``kick_start`` draws generation 0's surrogates
+from the panel only.
 """
 from __future__ import annotations
 
@@ -40,6 +42,7 @@ class PhaseOptions:
     knn: int = 0              # K nearest-neighbour surrogates (0: uniform)
     cluster_start: int = 0    # generation from which the kNN sampler is used
     lanes: int = 0            # speculation width (0: chosen per generation)
+    kick_start: bool = False  # generation 0 draws its surrogates from the panel rows only
     device: int = 0
 
     @property
@@ -67,7 +70,10 @@ def phase(model: mdl.Model, haps: np.ndarray, opts: PhaseOptions):
         if opts.knn and nbr is None and g >= opts.cluster_start:
             nbr = eng.knn(opts.knn)
         pen = float(anneal_pen(g, opts.sa_burnin))
-        eng.launch(eng.args(None, None, pen, opts.seed, g, neighbors=nbr))
+        a = eng.args(None, None, pen, opts.seed, g, neighbors=nbr)
+        if opts.kick_start and g == 0 and eng.H > 2 * N:
+            a.sample_lo, a.sample_hi, a.kick_start = 2 * N, eng.H, 1
+        eng.launch(a)
         eng.swap()
         if g >= tallied_from:
             dev._c(L.glp_tally(dev.ctx, eng.haps.data_ptr(), N, S, hsum.data_ptr()))
