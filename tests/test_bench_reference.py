@@ -1,0 +1,43 @@
+"""bench.py's reference arm (the CPU path of the reference, timed on the
+host cores) runs without a GPU: one JSON line with the benchmark contract's
+keys on rank 0, nothing on the other ranks."""
+import json
+import os
+import subprocess
+import sys
+
+from conftest import ROOT
+
+ARGS = ["--impl", "reference", "--steps", "2", "--warmup", "1", "--samples", "64",
+        "--sites", "256", "--cpu-seconds", "1"]
+
+
+def run(env_extra=None):
+    env = dict(os.environ)
+    env.update(env_extra or {})
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + ARGS, env=env,
+                          capture_output=True, text=True, timeout=600, cwd=ROOT)
+
+
+def test_reference_arm_line():
+    out = run()
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 2
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert {"value", "unit", "sample"} <= set(cb)
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0
+    assert e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_other_ranks_are_silent():
+    out = run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert not [l for l in out.stdout.splitlines() if l.startswith("{")]
