@@ -202,9 +202,16 @@ def cpu_baseline(m, haps, quad, props, C, pen, seconds, seed=1, gen=0):
     O.generation(pb, tr, quad, props, pen, 0, n2, True, nthreads=threads)
     dt = time.perf_counter() - t0
     ups = n2 * (C + 1) * m.S / dt
+    # the same on one thread, over as many samples as there are threads
+    n1 = min(m.N, threads)
+    t0 = time.perf_counter()
+    O.generation(pb, tr, quad, props, pen, 0, n1, True, nthreads=1)
+    dt1 = time.perf_counter() - t0
     return {"value": ups, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{n2} of {m.N} samples of one generation (C={C}, S={m.S}), "
-                      f"{dt:.1f} s on {threads} host threads"}, dt
+                      f"{dt:.1f} s on {threads} host threads",
+            "single_thread_value": n1 * (C + 1) * m.S / dt1,
+            "single_thread_sample": f"{n1} samples, {dt1:.1f} s on 1 thread"}, dt
 
 
 def run_reference(args):
@@ -241,7 +248,9 @@ def run_reference(args):
                    "samples": m.N, "sites": m.S, "cycles": C,
                    "sampler": "uniform over all other haplotypes"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} of {m.N} samples per step, {args.steps} steps"},
+                         "sample": f"{n} of {m.N} samples per step, {args.steps} steps",
+                         "single_thread_value": base["single_thread_value"],
+                         "single_thread_sample": base["single_thread_sample"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

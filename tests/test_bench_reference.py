@@ -32,6 +32,7 @@ def test_reference_arm_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert {"value", "unit", "sample"} <= set(cb)
+    assert cb["single_thread_value"] > 0
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0
     assert e2e["d2h_bytes_per_step"] == 0
