@@ -202,8 +202,8 @@ def cpu_baseline(m, haps, quad, props, C, pen, seconds, seed=1, gen=0):
     O.generation(pb, tr, quad, props, pen, 0, n2, True, nthreads=threads)
     dt = time.perf_counter() - t0
     ups = n2 * (C + 1) * m.S / dt
-    # the same on one thread, over as many samples as there are threads
-    n1 = min(m.N, threads)
+    # the same on one thread, over about one second's worth of samples
+    n1 = int(min(m.N, max(1, n2 / max(dt * threads, 1e-9))))
     t0 = time.perf_counter()
     O.generation(pb, tr, quad, props, pen, 0, n1, True, nthreads=1)
     dt1 = time.perf_counter() - t0
