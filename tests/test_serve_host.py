@@ -50,6 +50,7 @@ class FakeProblem:
         self.chunk, self.seed = chunk, seed
         self.haps, self.hnew = "a", "b"
         self.like = None
+        self.pb = None  # the C problem handle the mixed launch passes
         self.closed = False
 
     def args(self, generation):
