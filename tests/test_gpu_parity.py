@@ -114,7 +114,7 @@ def check_against_oracle(O, m, haps, quad, props, pen, out, seed, gen, trace=Non
     return worst, worst64
 
 
-@pytest.mark.parametrize("S", [1, 63, 64, 65, 130, 300, 1024])
+@pytest.mark.parametrize("S", [1, 2, 16, 17, 33, 63, 64, 65, 130, 300, 1024])
 def test_generation_matches_oracle_sites(dev, oracle_lib, S):
     m, haps, quad, props = make_problem(N=16, S=S, C=12)
     out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
