@@ -119,6 +119,32 @@ def traffic_per_launch(N, S, C, args):
     return NCU_TRAFFIC_S1024 * S / 1024
 
 
+def hbm_roofline(N, S, H, wn, kernel_ms, traffic, args):
+    """The same kernel against the measured HBM copy bandwidth: compulsory
+    bytes of one generation kernel launch (every sample's emission rows read
+    once, 16 B a site, and the haplotype panel, H x wn words) over its time.
+    The kernel re-reads a sample's emission every speculative round, mostly
+    from L2; `traffic` is what reached DRAM."""
+    peak = None
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            peak = float(json.load(open(path))["hbm_gbs"])
+        except (ValueError, KeyError):
+            peak = None
+    if peak is None:
+        peak = 6800.0
+        src = "fallback"
+    else:
+        src = "measured"
+    algo = N * S * 16 + H * wn * 8
+    achieved = algo / (kernel_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "note": f"compulsory bytes {algo} per launch; peak = {src} HBM copy bandwidth; "
+                    "far below it: the kernel is bound by FP32 issue (roofline)"}
+
+
 def pen_for(gen, burnin):
     """Annealing penalty of generation gen (insti.cpp:1670-1671), binary32."""
     from glphase_gb300.batch import anneal_pen
@@ -386,6 +412,8 @@ def run_ours(args):
                                  "FMA rate on this GPU (glp_measure_fp32_peak); traffic = "
                                  "DRAM bytes per launch from one ncu capture at S=1024 scaled "
                                  "by S (profiles/generation_kernel_10000x1024_full.md)"},
+            "roofline_hbm": hbm_roofline(N, S, H, wn, kernel_ms, traffic_per_launch(N, S, C, args),
+                                         args),
             "clocks": ck,
             "gpu_launches": 3 * args.steps,
             "step_ms": step_ms,
