@@ -94,7 +94,8 @@ def accuracy(w, m, haps, ds, seed, device):
     N = m.N
     opts = ph.PhaseOptions(sa_burnin=w.burnin, burnin=0, sampling=w.sampling, cycles=w.cycles,
                            seed=seed, knn=w.knn, cluster_start=0,
-                           kick_start=bool(w.panel_haps), device=device)
+                           kick_start=bool(w.panel_haps), kick_first=bool(w.panel_haps),
+                           device=device)
     prob, _ = ph.phase(m, haps, opts)
     truth = np.stack([ds.truth[0:2 * N:2], ds.truth[1:2 * N:2]], axis=-1).astype(np.int8)
     call = np.argmax(m.t, axis=-1)

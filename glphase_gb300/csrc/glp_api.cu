@@ -461,6 +461,10 @@ int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
       return fail(c, GLP_ERR_ARG, "surrogate range [%u, %u) must hold 3+ of %u haplotypes",
                   lo, hi, H);
   }
+  const bool kick_first = (a->flags & GLP_GEN_KICK_FIRST) != 0;
+  if (kick_first && draws && C && H < 2 * N + 1)
+    return fail(c, GLP_ERR_ARG,
+                "GLP_GEN_KICK_FIRST needs panel haplotypes after the 2*num_samples=%u rows", 2 * N);
   if (work && !a->hnew)
     return fail(c, GLP_ERR_ARG, "hnew is required unless GLP_GEN_NO_WORK is set");
   if (!pb->d_tran4 || pb->S != S)
@@ -529,6 +533,7 @@ int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
   p->do_work = work ? 1u : 0u;
   p->burnin = a->burnin;
   p->kick = a->kick_start ? 1u : 0u;
+  p->kick_first = kick_first ? 1u : 0u;
   return GLP_OK;
 }
 
@@ -1605,6 +1610,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   p.klen = a->neighbors_per_sample;
   p.samp_lo = lo;
   p.samp_hi = hi;
+  p.kick_first = ((a->flags & GLP_GEN_KICK_FIRST) && H > 2 * N) ? 1u : 0u;
   std::memcpy(p.pc, pc16, sizeof(p.pc));
   p.pen = a->pen;
   p.seed = a->seed;

@@ -89,6 +89,7 @@ struct GenParams {
   uint32_t klen, samp_lo, samp_hi;   // uniform surrogates over [samp_lo, samp_hi)
   uint32_t burnin;                   // >0: advance_kernel sets pen = min((g+1)/burnin,1)^2
   uint32_t kick;                     // 1: surrogates from [samp_lo, H) in generation 0 only
+  uint32_t kick_first;               // 1: every chain's first proposal from the panel rows
   float pc[16];
   float pen;
   uint64_t seed;
@@ -1489,8 +1490,11 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
           glp_mh_draw(p.seed, p.generation, s, cyc, &slot[v], &u[v]);
         }
         phap[v] = p.props ? __ldg(p.props + (size_t)cyc * N + s)
-                          : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP,
-                                          p.samp_lo, p.samp_hi, p.nbr, p.klen);
+                  : (p.kick_first && cyc == 0)
+                      ? glp_surrogate_ref(p.seed, p.generation, s, cyc, GLP_TAG_PROP, 2u * N,
+                                          H, p.nbr, p.klen)
+                      : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP, p.samp_lo,
+                                      p.samp_hi, p.nbr, p.klen);
         if (phap[v] >= H) {
           atomicOr(error, 1);
           phap[v] = 0;

@@ -139,6 +139,35 @@ GLP_HD uint32_t glp_surrogate(uint64_t seed, uint32_t generation, uint32_t s,
   return glp_uniform_hap(x, s, lo, hi);
 }
 
+/* The proposal of a chain's first cycle under kick-start (insti.cpp:1505-1511
+ * with --kickstart; Sampler::SampleHap(I, true), sampler.cpp:12-27): a
+ * reference-panel haplotype, index >= ref_lo.  The reference redraws from its
+ * sampler until the index is one; here the draw is uniform over the
+ * neighbour list's panel entries (in list order) when a list is given and
+ * holds any, else uniform over [ref_lo, hi) (where the reference would loop
+ * forever on a list without panel entries). */
+GLP_HD uint32_t glp_surrogate_ref(uint64_t seed, uint32_t generation, uint32_t s,
+                                  uint32_t index, uint32_t tag, uint32_t ref_lo, uint32_t hi,
+                                  const uint32_t *nbr, uint32_t klen) {
+  const glp_u32x4 x = glp_draw(seed, generation, s, index, tag);
+  if (nbr) {
+    const uint32_t *row = nbr + (size_t)s * klen;
+    uint32_t c = 0;
+    for (uint32_t k = 0; k < klen; ++k)
+      c += row[k] >= ref_lo ? 1u : 0u;
+    if (c) {
+      uint32_t j = glp_below(x.v[2], x.v[3], c);
+      for (uint32_t k = 0; k < klen; ++k)
+        if (row[k] >= ref_lo) {
+          if (j == 0)
+            return row[k];
+          --j;
+        }
+    }
+  }
+  return glp_uniform_hap(x, s, ref_lo, hi);
+}
+
 /* hmm_work uniform for one site. */
 GLP_HD float glp_work_uniform(uint64_t seed, uint32_t generation,
                               uint32_t sample, uint32_t site) {

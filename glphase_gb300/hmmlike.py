@@ -252,9 +252,12 @@ class Engine:
         return self.nbr
 
     def args(self, quad_in, props, pen: float, seed: int, generation: int, work: bool = True,
-             eval_trace=None, accept_trace=None, neighbors=None) -> nat.GenerationArgs:
+             eval_trace=None, accept_trace=None, neighbors=None,
+             kick_first: bool = False) -> nat.GenerationArgs:
         """quad_in / props None: drawn in the kernel (from `neighbors` when
-        given, else uniformly over all other haplotypes)."""
+        given, else uniformly over all other haplotypes); kick_first: every
+        chain's first proposal from the panel rows (the reference's
+        --kickstart)."""
         a = nat.GenerationArgs()
         a.num_samples, a.num_sites, a.num_cycles, a.num_haps = self.N, self.S, self.C, self.H
         a.haps = self.haps.data_ptr()
@@ -267,7 +270,8 @@ class Engine:
         a.pen = pen
         a.seed = seed
         a.generation = generation
-        a.flags = (nat.GLP_GEN_VQ if self.vq else 0) | (0 if work else nat.GLP_GEN_NO_WORK)
+        a.flags = ((nat.GLP_GEN_VQ if self.vq else 0) | (0 if work else nat.GLP_GEN_NO_WORK) |
+                   (nat.GLP_GEN_KICK_FIRST if kick_first else 0))
         a.like_out = self.like.data_ptr()
         a.eval_trace = None if eval_trace is None else eval_trace.data_ptr()
         a.accept_trace = None if accept_trace is None else accept_trace.data_ptr()

@@ -22,6 +22,7 @@ GLP_ERR_NO_CONVERGE = 8
 
 GLP_GEN_VQ = 1
 GLP_GEN_NO_WORK = 2
+GLP_GEN_KICK_FIRST = 4
 
 EXPORTED = [
     "glp_check_device", "glp_create", "glp_destroy", "glp_last_error", "glp_set_stream",

@@ -18,7 +18,9 @@ The surrogate sampler is uniform over all other haplotypes
 haplotypes by Hamming distance built on the device from the haplotypes of
 that generation (``KNN``, kNN.cpp:99-206).  With reference-panel rows after
 the 2N sample haplotypes, ``kick_start`` draws generation 0's surrogates
-from the panel only.
+from the panel only (the README's kick-start) and ``kick_first`` every
+chain's first proposal in every generation (the code's ``--kickstart``,
+insti.cpp:1505-1511).
 """
 from __future__ import annotations
 
@@ -43,6 +45,7 @@ class PhaseOptions:
     cluster_start: int = 0    # generation from which the kNN sampler is used
     lanes: int = 0            # speculation width (0: chosen per generation)
     kick_start: bool = False  # generation 0 draws its surrogates from the panel rows only
+    kick_first: bool = False  # every chain's first proposal from the panel (--kickstart)
     device: int = 0
 
     @property
@@ -70,7 +73,8 @@ def phase(model: mdl.Model, haps: np.ndarray, opts: PhaseOptions):
         if opts.knn and nbr is None and g >= opts.cluster_start:
             nbr = eng.knn(opts.knn)
         pen = float(anneal_pen(g, opts.sa_burnin))
-        a = eng.args(None, None, pen, opts.seed, g, neighbors=nbr)
+        a = eng.args(None, None, pen, opts.seed, g, neighbors=nbr,
+                     kick_first=opts.kick_first and eng.H > 2 * N)
         if opts.kick_start and g == 0 and eng.H > 2 * N:
             a.sample_lo, a.sample_hi, a.kick_start = 2 * N, eng.H, 1
         eng.launch(a)

@@ -57,6 +57,9 @@ typedef struct glp_ctx glp_ctx;
 /* glp_generation_args.flags */
 #define GLP_GEN_VQ 1u      /* score with the VQ codes (else float emit) */
 #define GLP_GEN_NO_WORK 2u /* skip the fused hmm_work (hnew untouched) */
+/* draw every chain's first proposal from the panel rows [2N, H) (the
+ * reference's --kickstart, src/insti.cpp:1505-1511); in-kernel draws only */
+#define GLP_GEN_KICK_FIRST 4u
 
 /* One MH generation over all N samples. */
 typedef struct glp_generation_args {

@@ -445,16 +445,38 @@ void glpo_work_uniforms(uint64_t seed, uint32_t generation, uint32_t sample, uin
     u[m] = glp_work_uniform(seed, generation, sample, m);
 }
 
+/* Insti::solve's kick-start (insti.cpp:1505-1511): the first proposal comes
+ * from Sampler::SampleHap(I, true) (sampler.cpp:12-27), which redraws until
+ * the index is a panel haplotype (>= 2N).  With counter-based draws: a
+ * uniform pick among the neighbour list's panel entries, in list order, or
+ * uniform over [2N, H) without a list or panel entries. */
+static uint32_t kick_proposal(uint64_t seed, uint32_t generation, uint32_t s, uint32_t N,
+                              uint32_t H, const uint32_t *nbr, uint32_t klen) {
+  const glp_u32x4 x = glp_draw(seed, generation, s, 0, GLP_TAG_PROP);
+  const uint32_t ref_lo = 2 * N;
+  if (nbr) {
+    uint32_t panel[1024], n = 0;
+    for (uint32_t k = 0; k < klen && n < 1024; ++k)
+      if (nbr[(size_t)s * klen + k] >= ref_lo)
+        panel[n++] = nbr[(size_t)s * klen + k];
+    if (n)
+      return panel[glp_below(x.v[2], x.v[3], n)];
+  }
+  return glp_uniform_hap(x, s, ref_lo, H);
+}
+
 void glpo_sample_surrogates(uint64_t seed, uint32_t generation, uint32_t N, uint32_t C,
                             uint32_t lo, uint32_t hi, const uint32_t *nbr, uint32_t klen,
-                            uint32_t *quad, uint32_t *props) {
+                            int kick_first, uint32_t H, uint32_t *quad, uint32_t *props) {
   for (uint32_t s = 0; s < N; ++s) {
     for (uint32_t j = 0; j < 4; ++j)
       quad[(size_t)j * N + s] =
           glp_surrogate(seed, generation, s, j, GLP_TAG_INIT, lo, hi, nbr, klen);
     for (uint32_t c = 0; c < C; ++c)
       props[(size_t)c * N + s] =
-          glp_surrogate(seed, generation, s, c, GLP_TAG_PROP, lo, hi, nbr, klen);
+          (kick_first && c == 0)
+              ? kick_proposal(seed, generation, s, N, H, nbr, klen)
+              : glp_surrogate(seed, generation, s, c, GLP_TAG_PROP, lo, hi, nbr, klen);
   }
 }
 

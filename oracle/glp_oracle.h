@@ -149,7 +149,7 @@ void glpo_work_uniforms(uint64_t seed, uint32_t generation, uint32_t sample, uin
  * NULL for uniform over [lo, hi) minus the sample's own pair. */
 void glpo_sample_surrogates(uint64_t seed, uint32_t generation, uint32_t N, uint32_t C,
                             uint32_t lo, uint32_t hi, const uint32_t *nbr, uint32_t klen,
-                            uint32_t *quad, uint32_t *props);
+                            int kick_first, uint32_t H, uint32_t *quad, uint32_t *props);
 
 /* KNN::CalculateVarAfs + CutDownHaps (kNN.cpp:216-257): bit m of mask is
  * set when site m's alt-allele frequency over all H haplotypes (or its minor

@@ -90,7 +90,7 @@ def lib():
         L.glpo_work_uniforms.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
         L.glpo_sample_surrogates.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                              C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32,
-                                             _u32p, _u32p]
+                                             C.c_int, C.c_uint32, _u32p, _u32p]
         L.glpo_common_sites.argtypes = [_u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double,
                                         C.c_double, C.c_int, _u64p]
         L.glpo_knn.restype = C.c_int
@@ -246,9 +246,11 @@ def work_uniforms(seed, generation, sample, S):
     return u
 
 
-def sample_surrogates(seed, generation, N, C_cycles, lo, hi, nbr=None):
+def sample_surrogates(seed, generation, N, C_cycles, lo, hi, nbr=None, kick_first=False,
+                      H=None):
     """The surrogates a generation draws on the device, materialised:
-    (quad [4][N], props [C][N])."""
+    (quad [4][N], props [C][N]).  kick_first: the first proposal of every
+    chain from the panel rows [2N, H) (H defaults to hi)."""
     quad = np.zeros((4, N), np.uint32)
     props = np.zeros((max(C_cycles, 1), N), np.uint32)
     if nbr is not None:
@@ -256,7 +258,8 @@ def sample_surrogates(seed, generation, N, C_cycles, lo, hi, nbr=None):
         ptr, klen = nb.ctypes.data, nb.shape[1]
     else:
         nb, ptr, klen = None, None, 0
-    lib().glpo_sample_surrogates(seed, generation, N, C_cycles, lo, hi, ptr, klen, quad, props)
+    lib().glpo_sample_surrogates(seed, generation, N, C_cycles, lo, hi, ptr, klen,
+                                 int(kick_first), hi if H is None else H, quad, props)
     return quad, props[:C_cycles]
 
 

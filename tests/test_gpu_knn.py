@@ -73,7 +73,8 @@ def test_device_surrogates_match_oracle(dev, oracle_lib):
     m, haps, _, _ = make_problem(N=24, S=400, C=20, panel=40, seed=6)
     H = haps.shape[0]
     nbr = O.knn(haps, m.S, 10)[:m.N]
-    for lo, hi, table in ((0, 0, None), (48, H, None), (0, 0, nbr)):
+    for lo, hi, table, kick in ((0, 0, None, False), (48, H, None, False), (0, 0, nbr, False),
+                                (0, 0, None, True), (0, 0, nbr, True)):
         seed, gen = 31, 5
         dev.copy_tran_to_device(m.tran)
         dev.copy_mutation_mat_to_device(m.pc)
@@ -91,12 +92,15 @@ def test_device_surrogates_match_oracle(dev, oracle_lib):
         a.like_out, a.eval_trace, a.accept_trace = like.ctypes.data, evals.ctypes.data, \
             acc.ctypes.data
         a.sample_lo, a.sample_hi = lo, hi
+        a.flags = nat.GLP_GEN_KICK_FIRST if kick else 0
         if table is not None:
             tb = np.ascontiguousarray(table)
             a.neighbors, a.neighbors_per_sample = tb.ctypes.data, tb.shape[1]
         rc = dev.L.glp_run_generation_host(dev.ctx, C.byref(a))
         assert rc == 0, dev.L.glp_last_error(dev.ctx)
         quad, props = O.sample_surrogates(seed, gen, m.N, 20, lo, hi if hi else H,
-                                          nbr=table)
+                                          nbr=table, kick_first=kick, H=H)
+        if kick:
+            assert props[0].min() >= 2 * m.N
         out = dict(quad=qo, hnew=hnew, like=like, evals=evals, acc=acc)
         check_against_oracle(O, m, haps, quad, props, 0.7, out, seed, gen)

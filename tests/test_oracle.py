@@ -257,3 +257,23 @@ def test_device_surrogate_streams(oracle_lib):
     q, p = O.sample_surrogates(9, 3, 50, 100, 0, 0, nbr=nbr)
     assert p.min() >= 60 and p.max() < 67
     assert len(np.unique(p)) == 7
+
+
+def test_kick_start_first_proposal(oracle_lib):
+    """--kickstart (insti.cpp:1505-1511): every chain's first proposal is a
+    panel haplotype (index >= 2N), the other draws are unchanged."""
+    O = oracle_lib
+    N, H = 50, 160                      # panel rows 100..159
+    q0, p0 = O.sample_surrogates(9, 3, N, 40, 0, H)
+    q1, p1 = O.sample_surrogates(9, 3, N, 40, 0, H, kick_first=True)
+    assert np.array_equal(q0, q1) and np.array_equal(p0[1:], p1[1:])
+    assert p1[0].min() >= 2 * N and p1[0].max() < H
+    # with a neighbour list: its panel entries only, in any of them
+    nbr = np.tile(np.array([3, 120, 7, 140, 9], np.uint32)[None, :], (N, 1))
+    q1, p1 = O.sample_surrogates(9, 3, N, 40, 0, 0, nbr=nbr, kick_first=True, H=H)
+    assert set(p1[0].tolist()) == {120, 140}
+    assert set(np.unique(p1[1:]).tolist()) <= {3, 120, 7, 140, 9}
+    # a list without panel entries falls back to a uniform panel draw
+    nbr = np.tile(np.array([3, 7, 9], np.uint32)[None, :], (N, 1))
+    _, p1 = O.sample_surrogates(9, 3, N, 40, 0, 0, nbr=nbr, kick_first=True, H=H)
+    assert p1[0].min() >= 2 * N and p1[0].max() < H
