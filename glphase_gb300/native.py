@@ -24,6 +24,10 @@ GLP_GEN_VQ = 1
 GLP_GEN_NO_WORK = 2
 GLP_GEN_KICK_FIRST = 4
 
+GLP_REQ_QUEUED = 0
+GLP_REQ_RESIDENT = 1
+GLP_REQ_DONE = 2
+
 EXPORTED = [
     "glp_check_device", "glp_create", "glp_destroy", "glp_last_error", "glp_set_stream",
     "glp_set_tran", "glp_set_mutation_mat", "glp_set_codebook", "glp_set_packed_gls",
@@ -34,7 +38,9 @@ EXPORTED = [
     "glp_problem_set_model_device", "glp_batch_prepare", "glp_batch_run", "glp_batch_launch",
     "glp_batch_destroy", "glp_run_generation_noalloc", "glp_tally", "glp_result",
     "glp_set_evals_per_lane", "glp_get_counters", "glp_kernel_times", "glp_vq_train",
-    "glp_vq_pack", "glp_set_block_sites", "glp_get_block_sites",
+    "glp_vq_pack", "glp_set_block_sites", "glp_get_block_sites", "glp_server_create",
+    "glp_server_submit", "glp_server_tick", "glp_server_poll", "glp_server_stats",
+    "glp_server_destroy",
 ]
 
 
@@ -128,6 +134,13 @@ def load(build_if_missing: bool = False):
     L.glp_set_block_sites.argtypes = [vp, u32]
     L.glp_get_block_sites.argtypes = [vp, vp]
     L.glp_run_batch.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs)]
+    L.glp_server_create.argtypes = [vp, u64, i32, C.POINTER(vp)]
+    L.glp_server_submit.argtypes = [vp, vp, C.POINTER(GenerationArgs), u32, C.POINTER(u64)]
+    L.glp_server_tick.argtypes = [vp, C.POINTER(u32), C.POINTER(u32)]
+    L.glp_server_poll.argtypes = [vp, u64, C.POINTER(i32), C.POINTER(u32), C.POINTER(vp)]
+    L.glp_server_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
+    L.glp_server_destroy.argtypes = [vp]
+    L.glp_server_destroy.restype = None
     for name in EXPORTED:
         getattr(L, name)
     _lib = L

@@ -15,6 +15,10 @@ sample's chain depends only on its own chunk, so a request's result is the
 same alone and in any mix (tests/test_gpu_serve.py checks it bit for bit).
 
 The plain form runs the same ticks with one launch per resident request.
+
+``NativeServer`` runs the same loop inside the library (glp_server_*): the
+queue, admission, per-request generation arguments and retirement are C++,
+and Python only submits, ticks and polls.
 """
 from __future__ import annotations
 
@@ -165,3 +169,79 @@ class Server:
                 self.stats.latencies.append(r.finished - r.arrival)
         self.stats.wall_s = time.perf_counter() - t_start
         return self.stats
+
+
+class NativeServer(Server):
+    """The serving loop of the C ABI (glp_server_create / submit / tick /
+    poll): the same admission, generation arguments and retirement as
+    ``Server``, run by the library.  A request's device problem is created
+    when it is submitted (its model inputs are already on the device)."""
+
+    def __init__(self, dev, budget_bytes: int, plain: bool = False):
+        import ctypes as C
+        super().__init__(dev, budget_bytes, plain)
+        self.srv = C.c_void_p()
+        dev._c(dev.L.glp_server_create(dev.ctx, budget_bytes, int(plain), C.byref(self.srv)))
+        self._ids: dict[int, int] = {}
+
+    def submit(self, req: Request) -> None:
+        import ctypes as C
+        from . import native as nat
+        L = self.dev.L
+        req.problem = DeviceProblem(self.dev, req.chunk, req.cycles, req.seed, req.burnin)
+        a = req.problem.args(0)
+        rid = C.c_uint64()
+        rc = L.glp_server_submit(self.srv, req.problem.pb, C.byref(a), req.generations,
+                                 C.byref(rid))
+        if rc == nat.GLP_ERR_ARG:
+            msg = L.glp_last_error(self.dev.ctx).decode()
+            req.problem.close()
+            raise ValueError(f"request {req.rid}: {msg}")
+        self.dev._c(rc)
+        self._ids[req.rid] = rid.value
+        self.queue.append(req)
+
+    def _poll(self, req: Request):
+        import ctypes as C
+        state, done, ptr = C.c_int(), C.c_uint32(), C.c_void_p()
+        self.dev._c(self.dev.L.glp_server_poll(self.srv, self._ids[req.rid], C.byref(state),
+                                               C.byref(done), C.byref(ptr)))
+        return state.value, done.value, ptr.value
+
+    def tick(self, now: float) -> list[Request]:
+        import ctypes as C
+        from . import native as nat
+        L = self.dev.L
+        resident, finished = C.c_uint32(), C.c_uint32()
+        t0 = time.perf_counter()
+        self.dev._c(L.glp_server_tick(self.srv, C.byref(resident), C.byref(finished)))
+        if resident.value:
+            self.stats.busy_s += time.perf_counter() - t0
+        for r in list(self.queue):
+            if self._poll(r)[0] != nat.GLP_REQ_QUEUED:
+                self.queue.remove(r)
+                r.admitted = now
+                self.active.append(r)
+        self.stats.peak_resident = max(self.stats.peak_resident, len(self.active))
+        self.stats.peak_bytes = max(self.stats.peak_bytes,
+                                    sum(r.footprint() for r in self.active))
+        done = []
+        for r in list(self.active):
+            state, r.gen, ptr = self._poll(r)
+            if state == nat.GLP_REQ_DONE:
+                self.active.remove(r)
+                p = r.problem
+                r.result_haps = p.haps if ptr == p.haps.data_ptr() else p.hnew
+                r.result_like = p.like
+                p.close()
+                done.append(r)
+        ticks, updates, used = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.dev._c(L.glp_server_stats(self.srv, C.byref(ticks), C.byref(updates),
+                                       C.byref(used)))
+        self.stats.ticks, self.stats.updates, self.used = ticks.value, updates.value, used.value
+        return done
+
+    def close(self) -> None:
+        if self.srv:
+            self.dev.L.glp_server_destroy(self.srv)
+            self.srv = None

@@ -265,6 +265,48 @@ int glp_batch_run(glp_batch *batch);
 int glp_batch_launch(glp_batch *batch);
 void glp_batch_destroy(glp_batch *batch);
 
+/* ---- Request server: continuous batching (no reference counterpart: the
+ * reference phases one chunk per process, src/insti.cpp:1557-1728). ----
+ * A request is a problem, a generation template and a generation count G.
+ * Requests wait in arrival order; each glp_server_tick admits the waiting
+ * requests whose device footprint, N*S*44 + 2*H*ceil(S/64)*8 bytes
+ * (emission, genotype probabilities, hmm_work scratch, both haplotype
+ * buffers), fits what is left of budget_bytes, runs one generation of every
+ * resident request -- all in one glp_run_batch launch, or one glp_run_batch
+ * launch per request when `plain` -- waits for it, and retires the requests
+ * that have run G generations.  Generation g of a request takes the
+ * template with generation = g; pen = min((g+1)/burnin, 1)^2 in binary32
+ * when burnin > 0 (src/insti.cpp:1670-1671), else the template's pen; haps
+ * and hnew exchanged on odd g (generation g writes hnew on even g, haps on
+ * odd g); the kick-start range in g = 0 only when kick_start = 1.  Every
+ * draw is keyed by the template's seed and g, so a request's result does not
+ * depend on the other requests it shared launches with.  The template's
+ * device buffers stay owned by the caller and alive until the request is
+ * done.  The ticks are synchronous on the context stream. */
+typedef struct glp_server glp_server;
+
+#define GLP_REQ_QUEUED 0   /* waiting for device memory */
+#define GLP_REQ_RESIDENT 1 /* admitted, generations in progress */
+#define GLP_REQ_DONE 2     /* all generations done */
+
+int glp_server_create(glp_ctx *ctx, uint64_t budget_bytes, int plain, glp_server **out);
+/* GLP_ERR_ARG when the footprint exceeds the whole budget, the problem
+ * belongs to another context, hnew is NULL or GLP_GEN_NO_WORK is set. */
+int glp_server_submit(glp_server *server, glp_problem *problem,
+                      const glp_generation_args *args, uint32_t generations,
+                      uint64_t *request_id);
+/* resident: requests run this tick; finished: requests that finished. */
+int glp_server_tick(glp_server *server, uint32_t *resident, uint32_t *finished);
+/* State, generations done and the buffer holding the current haplotypes:
+ * the template's hnew after an odd number of generations, else its haps. */
+int glp_server_poll(glp_server *server, uint64_t request_id, int *state,
+                    uint32_t *generations_done, const uint64_t **haps);
+/* Ticks run, site updates done (N*(C+1)*S per request generation), bytes
+ * held by resident requests. */
+int glp_server_stats(glp_server *server, uint64_t *ticks, uint64_t *updates,
+                     uint64_t *used_bytes);
+void glp_server_destroy(glp_server *server);
+
 /* kNN surrogate restriction on the device: for each of the H/2 samples,
  * the ceil(K/2) haplotypes nearest (Hamming distance over the sites whose
  * alt-allele frequency, or MAF when use_maf, lies in [freq_lb, freq_ub]) to

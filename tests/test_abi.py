@@ -46,6 +46,12 @@ def test_null_context_errors(lib):
     assert lib.glp_set_tran(None, None, 0) == 1
     assert lib.glp_vq_train(None, None, 0, 16, None, 0, 10, None) == 1
     assert lib.glp_vq_pack(None, None, 0, 0, None, 16, 4, None) == 1
+    assert lib.glp_server_create(None, 1 << 30, 0, None) == 1
+    assert lib.glp_server_submit(None, None, None, 1, None) == 1
+    assert lib.glp_server_tick(None, None, None) == 1
+    assert lib.glp_server_poll(None, 1, None, None, None) == 1
+    assert lib.glp_server_stats(None, None, None, None) == 1
+    lib.glp_server_destroy(None)
 
 
 def test_shim_header_compiles():

@@ -1,11 +1,13 @@
 """Serving loop with continuous batching: a request's result is the same
 alone and in a mix of requests that arrive while it is on the GPU; the HBM
-budget bounds what is resident."""
+budget bounds what is resident.  The library's own serving loop
+(glp_server_*, through NativeServer) gives the Python loop's results bit for
+bit, batched and plain."""
 import pytest
 
 from glphase_gb300 import synth, synth_device as sd
 from glphase_gb300.hmmlike import HMMLikeCUDA
-from glphase_gb300.serve import Request, Server
+from glphase_gb300.serve import NativeServer, Request, Server
 
 pytestmark = pytest.mark.gpu
 
@@ -59,3 +61,46 @@ def test_oversized_request_is_rejected(dev):
     srv = Server(dev, budget_bytes=r.footprint() - 1)
     with pytest.raises(ValueError):
         srv.serve([r])
+
+
+SPECS = [(0, 60, 700, 6), (1, 25, 130, 9), (2, 80, 1024, 4), (3, 7, 64, 7), (4, 33, 65, 1)]
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_native_server_matches_python_server(dev, plain):
+    import torch
+    py = [make(i, N, S, G) for i, N, S, G in SPECS]
+    ref = Server(dev, budget_bytes=1 << 34).serve(py)
+    nat = [make(i, N, S, G) for i, N, S, G in SPECS]
+    srv = NativeServer(dev, budget_bytes=1 << 34, plain=plain)
+    st = srv.serve(nat)
+    srv.close()
+    assert st.ticks == ref.ticks == max(G for *_, G in SPECS)
+    assert st.updates == ref.updates and st.peak_resident == len(SPECS)
+    for a, b in zip(py, nat):
+        assert b.gen == a.gen == a.generations
+        assert torch.equal(a.result_haps, b.result_haps), a.rid
+        assert torch.equal(a.result_like, b.result_like), a.rid
+
+
+def test_native_server_budget_and_mix(dev):
+    import torch
+    alone = [make(i, 30, 300, 3) for i in range(4)]
+    for r in alone:
+        s = NativeServer(dev, budget_bytes=1 << 34)
+        s.serve([r])
+        s.close()
+    reqs = [make(i, 30, 300, 3) for i in range(4)]
+    one = reqs[0].footprint()
+    srv = NativeServer(dev, budget_bytes=int(one * 2.5))
+    st = srv.serve(reqs)
+    assert st.peak_resident == 2 and st.peak_bytes <= int(one * 2.5)
+    assert len(st.latencies) == 4 and srv.used == 0
+    for a, b in zip(alone, reqs):
+        assert torch.equal(a.result_haps, b.result_haps)
+        assert torch.equal(a.result_like, b.result_like)
+    srv.close()
+    small = NativeServer(dev, budget_bytes=one - 1)
+    with pytest.raises(ValueError, match="more than the budget"):
+        small.submit(make(8, 30, 300, 2))
+    small.close()
