@@ -14,10 +14,16 @@
   rows sorted by position; the genetic location of a site is linearly
   interpolated between map rows, and the distance between two sites is the
   difference in Morgans;
+* a reference panel in IMPUTE2 legend + hap form (``Insti::OpenLegend``,
+  ``OpenHap``, ``FilterSites``, ``LoadHaps``, src/insti.cpp:855-1184): the
+  legend's sites ``id position a0 a1`` and one row of 0/1 alleles per site,
+  kept where chrom:pos:ref:alt matches a GL site and packed to the rows that
+  follow the 2N sample haplotypes;
 * the phased VCF the reference writes (``Insti::save_vcf``,
   src/insti.cpp:2098-2167): GT from the allele probabilities of the two
   haplotypes, GP (genotype) and APP (allele) posteriors Phred-scaled;
-* the non-reference discordance (NRD) its regression tests score a phased
+* the haplotype match (up to each sample's orientation) and the
+  non-reference discordance (NRD) its regression tests score a phased
   VCF by (``VCFNRD``, t/VCFComp.pm:116-131, which reads the ``NRDs`` line of
   ``bcftools stats``): over the genotypes where truth or call is not
   homozygous reference, the percentage whose calls differ.
@@ -307,6 +313,89 @@ def read_genetic_map(path: str) -> GeneticMap:
 
 
 # ---------------------------------------------------------------------------
+# Reference panel (legend + hap)
+
+LEGEND_HEADER = ("id", "position", "a0", "a1")
+
+
+def read_legend(path: str, chrom: str) -> Sites:
+    """Insti::OpenLegend (insti.cpp:1031-1078): the header must start with
+    ``id position a0 a1``; every row gives (position, a0, a1) of a site on
+    ``chrom`` (the GL sites' chromosome); empty lines are errors."""
+    sites = Sites()
+    with _open_read(path) as fd:
+        for line_num, line in enumerate(fd, start=1):
+            line = line.rstrip("\n")
+            if not line:
+                raise ValueError(f"Error in legend file {path}: empty lines detected.")
+            tokens = line.split()
+            if line_num == 1:
+                if tuple(tokens[:4]) != LEGEND_HEADER:
+                    raise ValueError(f"Error in legend file {path}: header start does not "
+                                     f"match: {' '.join(LEGEND_HEADER)}")
+                continue
+            sites.chrom.append(chrom)
+            sites.pos.append(int(tokens[1]))
+            sites.ref.append(tokens[2])
+            sites.alt.append(tokens[3])
+    return sites
+
+
+def read_hap(path: str) -> np.ndarray:
+    """Insti::OpenHap (insti.cpp:1080-1137): one row per site, one 0/1
+    column per haplotype, the same column count on every row.  Returns uint8
+    [sites][haplotypes]."""
+    rows = []
+    width = None
+    with _open_read(path) as fd:
+        for line_num, line in enumerate(fd):
+            tokens = line.split()
+            if width is None:
+                width = len(tokens)
+            if len(tokens) != width:
+                raise ValueError("Every row of hap file must have the same number of columns")
+            vals = [int(t) for t in tokens]
+            if any(v not in (0, 1) for v in vals):
+                raise ValueError(f"All alleles are not 0 or 1 In haplotypes file {path} at "
+                                 f"line number {line_num} (0-based)")
+            rows.append(vals)
+    if not width:
+        raise ValueError("num haps is 0.  Haps file empty?")
+    return np.asarray(rows, dtype=np.uint8)
+
+
+def load_reference_panel(legend_path: str, hap_path: str, sites: Sites) -> np.ndarray:
+    """The reference panel for the GL sites ``sites``
+    (``Insti::LoadHapLegSamp`` with ``InstiPanelType::REFERENCE``,
+    insti.cpp:1139-1184): legend rows whose chrom:pos:ref:alt is a GL site
+    are kept in legend order (``FilterSites``, insti.cpp:855-925) and every
+    GL site must be found exactly once; the kept rows are bit-packed per
+    haplotype (``HapPanel::Char2BitVec``, hapPanel.cpp:41-64).  Returns
+    uint64 [panel haplotypes][ceil(S/64)], the rows appended after the 2N
+    sample haplotypes (insti.cpp:1398)."""
+    from .model import pack_haplotypes
+    chrom = sites.chrom[0] if len(sites) else ""
+    legend = read_legend(legend_path, chrom)
+    haps = read_hap(hap_path)
+    if len(legend) != haps.shape[0]:
+        raise ValueError("legend and hap files have different numbers of sites")
+    if len(sites) > len(legend):
+        raise ValueError("the reference panel has fewer sites than the GLs")
+    gl_keys = {f"{c}:{p}:{r}:{a}" for c, p, r, a in zip(sites.chrom, sites.pos, sites.ref,
+                                                        sites.alt)}
+    keep = [i for i, (p, r, a) in enumerate(zip(legend.pos, legend.ref, legend.alt))
+            if f"{chrom}:{p}:{r}:{a}" in gl_keys]
+    if not keep:
+        raise ValueError("Error: No sites in loaded panel matched already loaded sites. Is "
+                         "your input file sorted?")
+    if len(keep) > len(sites):
+        raise ValueError("[insti] too many matching sites found")
+    if len(keep) != len(sites):
+        raise ValueError("[insti] Could not find all GL sites in loaded haplotype panel")
+    return pack_haplotypes(haps[keep].T)
+
+
+# ---------------------------------------------------------------------------
 # VCF
 
 
@@ -448,6 +537,34 @@ def nrd(truth_gt: np.ndarray, test_gt: np.ndarray) -> float:
     if total == 0:
         return 0.0
     return 100.0 * int((dt != dq).sum()) / total
+
+
+def hap_match(test_gt: np.ndarray, expected_gt: np.ndarray) -> str | None:
+    """The haplotype comparison of the reference's regression tests
+    (``VCFHapMatch`` / ``HapEq``, t/VCFComp.pm:48-114): site by site, each
+    sample's two haplotypes must equal the expected ones, or the expected
+    ones swapped; a sample is swapped for good at its first mismatch on its
+    first haplotype, and any other mismatch fails.  Inputs are GT alleles
+    [N][S][2].  Returns None on a match, else the reason."""
+    t = np.asarray(test_gt)
+    e = np.asarray(expected_gt)
+    if t.shape[1] != e.shape[1]:
+        return "hap files have different lengths"
+    if t.shape[0] != e.shape[0]:
+        return "hap files have differing number of haps"
+    if t.shape[0] == 0:
+        return "hap files have 0 haplotypes"
+    flipped = [False] * t.shape[0]
+    for m in range(t.shape[1]):
+        for i in range(t.shape[0]):
+            for j in range(2):
+                while t[i, m, j] != e[i, m, (1 - j) if flipped[i] else j]:
+                    if not flipped[i] and j == 0:
+                        flipped[i] = True
+                        continue
+                    return (f"Haplotypes do not match at line {m + 1}, at Allele number "
+                            f"{2 * i + j + 1}")
+    return None
 
 
 def dosages(gt: np.ndarray) -> np.ndarray:

@@ -105,19 +105,27 @@ def prepare(gl_het_alt: np.ndarray, positions: np.ndarray,
 
 def phase_bin(bin_path: str, vcf_path: str | None = None, map_path: str | None = None,
               opts: PhaseOptions | None = None, keep: set[str] | None = None,
-              command_line: str = ""):
+              command_line: str = "", region: tuple[str, int, int] | None = None,
+              ref_legend: str | None = None, ref_hap: str | None = None):
     """Phase the samples of a GL file and (optionally) write the phased VCF:
-    ``insti -g map -C.. -B.. -i.. -m.. file.bin`` (or ``-Fbcf file.vcf.gz``)
-    on one GPU.  ``.vcf`` / ``.vcf.gz`` files are read for their GL or PL
-    field, anything else as ``.bin``.  Returns (prob [S][2N], the parsed
-    input)."""
+    ``insti -g map -C.. -B.. -i.. -m.. [--region chr:a-b] [-h hap -l legend]
+    file.bin`` (or ``-Fbcf file.vcf.gz``) on one GPU.  ``.vcf`` / ``.vcf.gz``
+    files are read for their GL or PL field, anything else as ``.bin``;
+    ``region`` = (chrom, first, last) keeps the sites inside it; a reference
+    panel (legend + hap) becomes the haplotype rows after the 2N sample
+    rows.  Returns (prob [S][2N], the parsed input)."""
     opts = opts or PhaseOptions()
     if bin_path.endswith((".vcf", ".vcf.gz")):
-        data = gio.read_vcf_gls(bin_path, keep=keep)
+        data = gio.read_vcf_gls(bin_path, keep=keep, region=region)
     else:
-        data = gio.read_bin(bin_path, keep=keep)
+        data = gio.read_bin(bin_path, keep=keep, region=region)
     gmap = gio.read_genetic_map(map_path) if map_path else None
     m, haps = prepare(data.gl, data.sites.positions(), gmap, seed=opts.seed)
+    if ref_legend or ref_hap:
+        if not (ref_legend and ref_hap):
+            raise ValueError("a reference panel needs both a legend and a hap file")
+        panel = gio.load_reference_panel(ref_legend, ref_hap, data.sites)
+        haps = np.concatenate([haps, panel])
     prob, _ = phase(m, haps, opts)
     if vcf_path:
         gio.write_vcf(vcf_path, data.sites, data.names, prob, command_line=command_line)

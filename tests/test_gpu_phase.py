@@ -83,3 +83,19 @@ def test_knn_sampler_phasing():
     nrd = gio.nrd(truth, gio.genotype_calls(prob))
     base = gio.nrd(truth, gl_only_calls(m.t))
     assert nrd < 0.5 * base, (nrd, base)
+
+
+@pytest.mark.parametrize("case", ["map", "nomap", "region"])
+def test_simple_gls_on_device(oracle_lib, case):
+    """t/10-phase_simple_gls.t:32-68 through the device pipeline: the same
+    allele probabilities as the oracle loop, and the reference's expected
+    haplotypes up to each sample's orientation."""
+    from phase_oracle import oracle_phase
+    from simple_gls_cases import simple_case
+    for seed in (1, 2):
+        m, haps, opts, expected = simple_case(case, seed)
+        prob, final = ph.phase(m, haps, opts)
+        want_prob, want_haps = oracle_phase(oracle_lib, m, haps, opts)
+        assert np.array_equal(prob, want_prob) and np.array_equal(final, want_haps)
+        if seed == 1:
+            assert gio.hap_match(gio.genotype_calls(prob), expected) is None

@@ -1,0 +1,145 @@
+"""The reference's own loading and regression cases, restated:
+
+* t/10-phase_simple_gls.t:32-68 -- simple GLs phased with and without the
+  genetic map and on a region, haplotypes compared up to each sample's
+  orientation (VCFHapMatch / HapEq, t/VCFComp.pm:48-114), on the CPU oracle
+  from the committed fixture (tests/golden/phase_cases.npz);
+* src/testing/insti_unittests.cpp:85-184 (Insti.loadGLs) -- sites, GLs
+  before and after Insti::initialize, and the reference panel of the
+  onlyThree sample files, read from the reference tree when it is present.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from glphase_gb300 import io as gio
+from glphase_gb300 import model as mdl
+
+REF = "/root/reference"
+SAMPLES = os.path.join(REF, "samples")
+ONLY_THREE = os.path.join(SAMPLES, "20_011976121_012173018.bin.onlyThree")
+needs_ref = pytest.mark.skipif(not os.path.isdir(SAMPLES),
+                               reason="reference sample files not present")
+
+
+def test_hap_match_rules():
+    e = np.array([[[0, 1], [1, 1], [1, 0]]], np.int8)
+    assert gio.hap_match(e, e) is None
+    assert gio.hap_match(e[:, :, ::-1], e) is None               # whole sample swapped
+    assert gio.hap_match(np.array([[[1, 0], [1, 1], [1, 0]]], np.int8), e) is not None
+    assert "Allele number 2" in gio.hap_match(np.array([[[0, 0], [1, 1], [1, 0]]], np.int8), e)
+    assert gio.hap_match(e[:, :2], e) == "hap files have different lengths"
+    two = np.concatenate([e, e[:, :, ::-1]])
+    assert gio.hap_match(two, np.concatenate([e, e])) is None    # per-sample orientation
+
+
+@pytest.mark.parametrize("case", ["map", "nomap", "region"])
+def test_simple_gls_phase_like_the_reference(oracle_lib, case):
+    """The expected haplotypes for every seed tried with the full schedule,
+    and for most seeds on the region, whose 5 sampling generations leave
+    sample 3's two hets in the wrong phase now and then, as the reference's
+    own run can."""
+    from phase_oracle import oracle_phase
+    from simple_gls_cases import simple_case
+    matches = 0
+    for seed in range(1, 9):
+        m, haps, opts, expected = simple_case(case, seed)
+        prob, _ = oracle_phase(oracle_lib, m, haps, opts)
+        matches += gio.hap_match(gio.genotype_calls(prob), expected) is None
+    assert matches >= (6 if case == "region" else 8), matches
+
+
+@needs_ref
+def test_phase_cases_fixture_matches_reference_files(tmp_path, monkeypatch):
+    import importlib.util
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location(
+        "make_phase_cases", os.path.join(here, "golden", "make_phase_cases.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    monkeypatch.setattr(mod, "OUT", str(tmp_path / "cases.npz"))
+    mod.main(REF)
+    new = np.load(tmp_path / "cases.npz")
+    old = np.load(os.path.join(here, "golden", "phase_cases.npz"))
+    assert sorted(new.files) == sorted(old.files)
+    for k in new.files:
+        assert np.array_equal(new[k], old[k]), k
+
+
+@needs_ref
+@pytest.mark.parametrize("suffix", [".bin", ".vcf.gz"])
+def test_load_gls_known_answers(suffix):
+    """insti_unittests.cpp:85-172: 3 samples, 1,024 sites on chromosome 20;
+    the (het, homAlt) pairs as loaded and the (homRef, het, homAlt) trios
+    after Insti::initialize (insti.cpp:1345-1350)."""
+    path = ONLY_THREE + suffix
+    d = gio.read_bin(path) if suffix == ".bin" else gio.read_vcf_gls(path)
+    assert len(d.names) == 3 and len(d.sites) == 1024
+    assert set(d.sites.chrom) == {"20"}
+    assert [d.sites.pos[i] for i in (0, 5, 1023)] == [11976121, 11977230, 12173018]
+    assert [(d.sites.ref[i], d.sites.alt[i]) for i in (0, 5, 1023)] == \
+        [("T", "C"), ("A", "G"), ("G", "T")]
+    gl = d.gl  # [N][S][2]; the reference's pre-initialize prob is [S][N][2]
+    assert gl[0, 0, 0] == 0 and gl[0, 0, 1] == 1
+    assert gl[1, 0, 0] == pytest.approx(0.2, rel=4 * 2 ** -23) and gl[1, 0, 1] == 0
+    assert (gl[2, 0] == 0).all() and gl[0, 1, 1] == 1 and gl[1, 1, 1] == 0
+    assert gl[1, 2, 0] == 1                                      # prob[in*6 - 4]
+    t = mdl.genotype_probs(gl)
+    assert tuple(t[0, 0]) == (0, 0, 1)
+    assert t[1, 0, 0] == pytest.approx(0.8, rel=4 * 2 ** -23)
+    assert t[1, 0, 1] == pytest.approx(0.2, rel=4 * 2 ** -23) and t[1, 0, 2] == 0
+    assert tuple(t[2, 0]) == (1, 0, 0)
+    assert t[0, 1, 1] == 0 and t[0, 1, 2] == 1
+
+
+@needs_ref
+def test_reference_panel_known_answers():
+    """insti_unittests.cpp:174-184: after LoadHapLegSamp(legend, hap)
+    haplotypes 0 and 2 carry the reference allele and haplotype 3 the
+    alternative at sites 0-600; from site 601 haplotypes 0 and 3 carry the
+    alternative, 1 and 2 the reference."""
+    d = gio.read_bin(ONLY_THREE + ".bin")
+    panel = gio.load_reference_panel(ONLY_THREE + ".legend", ONLY_THREE + ".hap", d.sites)
+    assert panel.shape == (4, 16)
+    bits = mdl.unpack_haplotypes(panel, 1024)
+    assert (bits[0, :601] == 0).all() and (bits[2, :601] == 0).all()
+    assert (bits[3, :601] == 1).all()
+    assert (bits[0, 601:] == 1).all() and (bits[1, 601:] == 0).all()
+    assert (bits[2, 601:] == 0).all() and (bits[3, 601:] == 1).all()
+
+
+def _panel_files(tmp_path, legend_rows, hap_rows, header="id position a0 a1"):
+    leg, hap = tmp_path / "p.legend", tmp_path / "p.hap"
+    leg.write_text(header + "\n" + "".join(r + "\n" for r in legend_rows))
+    hap.write_text("".join(r + "\n" for r in hap_rows))
+    return str(leg), str(hap)
+
+
+def test_reference_panel_rules(tmp_path):
+    sites = gio.Sites(["5"] * 3, [100, 200, 300], ["A", "C", "G"], ["T", "G", "A"])
+    rows = ["x 50 A C", "x 100 A T", "x 150 C C", "x 200 C G", "x 300 G A"]
+    haps = ["1 1", "0 1", "1 0", "1 1", "0 0"]
+    leg, hap = _panel_files(tmp_path, rows, haps)
+    p = gio.load_reference_panel(leg, hap, sites)
+    assert mdl.unpack_haplotypes(p, 3).tolist() == [[0, 1, 0], [1, 1, 0]]
+    # a GL site the panel lacks (alleles must match too)
+    leg, hap = _panel_files(tmp_path, rows[:4] + ["x 300 G C"], haps)
+    with pytest.raises(ValueError, match="Could not find all GL sites"):
+        gio.load_reference_panel(leg, hap, sites)
+    # a GL site twice
+    leg, hap = _panel_files(tmp_path, rows + ["x 300 G A"], haps + ["1 1"])
+    with pytest.raises(ValueError, match="too many matching sites"):
+        gio.load_reference_panel(leg, hap, sites)
+    leg, hap = _panel_files(tmp_path, rows, haps, header="id pos a0 a1")
+    with pytest.raises(ValueError, match="header start"):
+        gio.load_reference_panel(leg, hap, sites)
+    leg, hap = _panel_files(tmp_path, rows, haps[:4] + ["0 0 1"])
+    with pytest.raises(ValueError, match="same number of columns"):
+        gio.load_reference_panel(leg, hap, sites)
+    leg, hap = _panel_files(tmp_path, rows, haps[:4] + ["0 2"])
+    with pytest.raises(ValueError, match="not 0 or 1"):
+        gio.load_reference_panel(leg, hap, sites)
+    leg, hap = _panel_files(tmp_path, rows[:2] + [""] + rows[2:], haps)
+    with pytest.raises(ValueError, match="empty lines"):
+        gio.load_reference_panel(leg, hap, sites)
