@@ -64,8 +64,29 @@ class Sites:
     ref: list[str] = field(default_factory=list)
     alt: list[str] = field(default_factory=list)
 
+    _keys: set = field(default_factory=set, repr=False, compare=False)
+
     def __len__(self) -> int:
         return len(self.pos)
+
+    def push_ordered(self, chrom: str, pos: int, ref: str, alt: str) -> None:
+        """Append a site as ``Bio::snp_storage_ordered::push_back``
+        (bio.cpp:47-75) does for the GL readers: positions never decrease,
+        one chromosome, and no chrom:pos:ref:alt twice (multi-allelic sites
+        come as biallelic records at the same position)."""
+        if self.pos and pos < self.pos[-1]:
+            raise ValueError(f"Tried to insert position [{pos}] that was less than last "
+                             f"position [{self.pos[-1]}]")
+        if self.chrom and chrom != self.chrom[0]:
+            raise ValueError(f"Input snp is wrong chromosome [{chrom}]")
+        key = f"{chrom}:{pos}:{ref}:{alt}"
+        if key in self._keys:
+            raise ValueError(f"Cannot push SNP, it already exists: [{key}]")
+        self._keys.add(key)
+        self.chrom.append(chrom)
+        self.pos.append(pos)
+        self.ref.append(ref)
+        self.alt.append(alt)
 
     def positions(self) -> np.ndarray:
         return np.asarray(self.pos, dtype=np.int64)
@@ -143,10 +164,7 @@ def read_bin(path: str, keep: set[str] | None = None,
                 ref, alt = alleles.split(" ", 1)
             else:
                 ref, alt = alleles[0], alleles[1]
-            sites.chrom.append(tokens[0])
-            sites.pos.append(pos)
-            sites.ref.append(ref)
-            sites.alt.append(alt)
+            sites.push_ordered(tokens[0], pos, ref, alt)
             row = np.empty((len(idx), 2), dtype=F32)
             one, zero = F32(1), F32(0)
             for k, i in enumerate(idx):
@@ -224,10 +242,7 @@ def read_vcf_gls(path: str, tags=("GL", "PL"), keep: set[str] | None = None,
                 else:
                     trio = [phred2prob(0 if v == "." else int(v)) for v in vals]
                 row[j] = gl_pair(*trio)
-            sites.chrom.append(cols[0])
-            sites.pos.append(pos)
-            sites.ref.append(cols[3])
-            sites.alt.append(alts[0])
+            sites.push_ordered(cols[0], pos, cols[3], alts[0])
             rows.append(row)
     if rows:
         gl = np.ascontiguousarray(np.stack(rows, axis=1))

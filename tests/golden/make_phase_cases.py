@@ -9,8 +9,11 @@ Run in a checkout where the reference tree exists:
 Stored: the GLs, positions and genetic-map distances of simple.gls.v1.bin
 (3 samples x 3 sites), the expected phased genotypes of the whole file and
 of the region 20:101363- (simple.gls.v1.expected.bin.vcf,
-simple.gls.v1.region.expected.bin.vcf), so the device pipeline can be run
-on them without the reference tree.
+simple.gls.v1.region.expected.bin.vcf), and the same for
+simple.gls.v1.samePos.bin (three biallelic records at one position,
+t/15-phase_simple_gls_multiallelic.t, compared with the same expected
+haplotypes), so the device pipeline can be run on them without the
+reference tree.
 """
 from __future__ import annotations
 
@@ -38,8 +41,12 @@ def main(ref_root: str) -> None:
     _, rsites, region_gt = gio.read_vcf_gt(
         os.path.join(simple, "simple.gls.v1.region.expected.bin.vcf"))
     pos = d.sites.positions()
+    same = gio.read_bin(os.path.join(simple, "simple.gls.v1.samePos.bin"))
+    same_pos = same.sites.positions()
     np.savez_compressed(
         OUT,
+        same_gl=same.gl, same_pos=same_pos, same_r=gmap.distances(same_pos),
+        same_alt=np.array(same.sites.alt),
         simple_gl=d.gl, simple_pos=pos, simple_r=gmap.distances(pos),
         simple_ref=np.array(d.sites.ref), simple_alt=np.array(d.sites.alt),
         simple_names=np.array(d.names), simple_expected_gt=exp_gt,

@@ -1,8 +1,10 @@
-"""The reference's simple-GL regression cases (t/10-phase_simple_gls.t:32-68)
-on the committed fixture tests/golden/phase_cases.npz: 3 samples x 3 sites
-phased with -C100 -B0 -i10 -m100 with and without the genetic map, and the
-region 20:101363- with -C100 -B0 -i5 -m5; the phased haplotypes must match
-the expected VCF up to each sample's orientation (VCFHapMatch)."""
+"""The reference's simple-GL regression cases (t/10-phase_simple_gls.t:32-68,
+t/15-phase_simple_gls_multiallelic.t:27-50) on the committed fixture
+tests/golden/phase_cases.npz: 3 samples x 3 sites phased with -C100 -B0
+-i10 -m100 with and without the genetic map, the same with the three sites
+at one position (biallelic records of a multi-allelic site), and the region
+20:101363- with -C100 -B0 -i5 -m5; the phased haplotypes must match the
+expected VCF up to each sample's orientation (VCFHapMatch)."""
 from __future__ import annotations
 
 import os
@@ -12,7 +14,7 @@ import numpy as np
 from glphase_gb300 import phase as ph
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "phase_cases.npz")
-CASES = ["map", "nomap", "region"]
+CASES = ["map", "nomap", "region", "same_map", "same_nomap"]
 
 
 class _MapDistances:
@@ -38,6 +40,9 @@ def simple_case(name: str, seed: int = 1):
     else:
         expected = z["simple_expected_gt"]
         opts = ph.PhaseOptions(sa_burnin=0, burnin=10, sampling=100, cycles=100, seed=seed)
-    gmap = _MapDistances(z["simple_r"]) if name == "map" else None
+    r = z["simple_r"]
+    if name.startswith("same"):
+        gl, pos, r = z["same_gl"], z["same_pos"], z["same_r"]
+    gmap = _MapDistances(r) if name.endswith("map") and "nomap" not in name else None
     m, haps = ph.prepare(np.ascontiguousarray(gl), pos, gmap, seed=seed)
     return m, haps, opts, expected

@@ -85,9 +85,10 @@ def test_knn_sampler_phasing():
     assert nrd < 0.5 * base, (nrd, base)
 
 
-@pytest.mark.parametrize("case", ["map", "nomap", "region"])
+@pytest.mark.parametrize("case", ["map", "nomap", "region", "same_map", "same_nomap"])
 def test_simple_gls_on_device(oracle_lib, case):
-    """t/10-phase_simple_gls.t:32-68 through the device pipeline: the same
+    """t/10-phase_simple_gls.t:32-68 and t/15-phase_simple_gls_multiallelic.t
+    through the device pipeline: the same
     allele probabilities as the oracle loop, and the reference's expected
     haplotypes up to each sample's orientation."""
     from phase_oracle import oracle_phase

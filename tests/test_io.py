@@ -66,6 +66,16 @@ def test_bin_format_errors(tmp_path):
     p.write_text("chr\tpos\tallele\ta\n20\t5\tACG\t0.1 0.2\n")
     with pytest.raises(ValueError, match="Could not parse alleles"):
         gio.read_bin(str(p))
+    # Bio::snp_storage_ordered (bio.cpp:47-75): order, one chromosome, no repeats
+    head = "chr\tpos\tallele\ta\n"
+    p.write_text(head + "20\t5\tAC\t0.1 0.2\n20\t5\tAG\t0.1 0.2\n")
+    assert gio.read_bin(str(p)).sites.alt == ["C", "G"]
+    for rows, msg in ((["20\t5\tAC", "20\t5\tAC"], "already exists"),
+                      (["20\t6\tAC", "20\t5\tAC"], "less than last position"),
+                      (["20\t5\tAC", "21\t6\tAC"], "wrong chromosome")):
+        p.write_text(head + "".join(r + "\t0.1 0.2\n" for r in rows))
+        with pytest.raises(ValueError, match=msg):
+            gio.read_bin(str(p))
 
 
 def test_gl_conversions():

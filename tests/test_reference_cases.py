@@ -1,9 +1,11 @@
 """The reference's own loading and regression cases, restated:
 
-* t/10-phase_simple_gls.t:32-68 -- simple GLs phased with and without the
-  genetic map and on a region, haplotypes compared up to each sample's
+* t/10-phase_simple_gls.t:32-68 and t/15-phase_simple_gls_multiallelic.t --
+  simple GLs phased with and without the genetic map, on a region, and with
+  all sites at one position, haplotypes compared up to each sample's
   orientation (VCFHapMatch / HapEq, t/VCFComp.pm:48-114), on the CPU oracle
-  from the committed fixture (tests/golden/phase_cases.npz);
+  from the committed fixture (tests/golden/phase_cases.npz); the broken
+  input of t/15 (a site twice) is rejected;
 * src/testing/insti_unittests.cpp:85-184 (Insti.loadGLs) -- sites, GLs
   before and after Insti::initialize, and the reference panel of the
   onlyThree sample files, read from the reference tree when it is present.
@@ -34,7 +36,7 @@ def test_hap_match_rules():
     assert gio.hap_match(two, np.concatenate([e, e])) is None    # per-sample orientation
 
 
-@pytest.mark.parametrize("case", ["map", "nomap", "region"])
+@pytest.mark.parametrize("case", ["map", "nomap", "region", "same_map", "same_nomap"])
 def test_simple_gls_phase_like_the_reference(oracle_lib, case):
     """The expected haplotypes for every seed tried with the full schedule,
     and for most seeds on the region, whose 5 sampling generations leave
@@ -143,3 +145,11 @@ def test_reference_panel_rules(tmp_path):
     leg, hap = _panel_files(tmp_path, rows[:2] + [""] + rows[2:], haps)
     with pytest.raises(ValueError, match="empty lines"):
         gio.load_reference_panel(leg, hap, sites)
+
+
+@needs_ref
+def test_duplicate_site_input_is_rejected():
+    """t/15-phase_simple_gls_multiallelic.t:52-53: insti fails on
+    simple.gls.v2.samePos.err.bin, whose last record repeats a site."""
+    with pytest.raises(ValueError, match="already exists"):
+        gio.read_bin(os.path.join(SAMPLES, "simple_gls", "simple.gls.v2.samePos.err.bin"))
