@@ -19,7 +19,10 @@ def oracle_phase(O, model, haps, opts, nthreads=0):
     for g in range(opts.generations):
         assert not opts.knn, "the oracle loop covers the uniform sampler"
         pb = O.OracleProblem(cur, model.emit, model.t, model.tran, model.pc, Cc)
-        quad, props = O.sample_surrogates(opts.seed, g, N, Cc, 0, H)
+        panel = H > 2 * N
+        lo, hi = (2 * N, H) if (opts.kick_start and panel and g == 0) else (0, H)
+        quad, props = O.sample_surrogates(opts.seed, g, N, Cc, lo, hi,
+                                          kick_first=opts.kick_first and panel, H=H)
         tr = pb.trace(seed=opts.seed, generation=g)
         pen = float(anneal_pen(g, opts.sa_burnin))
         _, cur, _ = O.generation(pb, tr, quad, props, pen, do_work=True, nthreads=nthreads)

@@ -100,3 +100,23 @@ def test_simple_gls_on_device(oracle_lib, case):
         assert np.array_equal(prob, want_prob) and np.array_equal(final, want_haps)
         if seed == 1:
             assert gio.hap_match(gio.genotype_calls(prob), expected) is None
+
+
+@pytest.mark.parametrize("kick", ["first", "start"])
+def test_panel_phasing_matches_oracle(oracle_lib, kick):
+    """Phasing with reference-panel rows after the 2N sample rows: every
+    chain's first proposal from the panel (--kickstart as the reference code
+    does it, insti.cpp:1505-1511), or the first generation drawing from the
+    panel only; device and oracle loops identical bit for bit."""
+    from phase_oracle import oracle_phase
+    w = synth.Workload("panel-e2e", N=24, S=300, founders=10, depth=3.0, burnin=2,
+                       sampling=4, panel_haps=40, seed=17)
+    ds = synth.generate(w)
+    m, haps = synth.initial_state(ds, seed=4)
+    assert haps.shape[0] == 2 * 24 + 40
+    opts = ph.PhaseOptions(sa_burnin=2, burnin=1, sampling=4, cycles=30, seed=6,
+                           kick_first=kick == "first", kick_start=kick == "start")
+    prob, final = ph.phase(m, haps, opts)
+    want_prob, want_haps = oracle_phase(oracle_lib, m, haps, opts)
+    assert np.array_equal(final, want_haps)
+    assert np.array_equal(prob, want_prob)

@@ -6,6 +6,9 @@
   orientation (VCFHapMatch / HapEq, t/VCFComp.pm:48-114), on the CPU oracle
   from the committed fixture (tests/golden/phase_cases.npz); the broken
   input of t/15 (a site twice) is rejected;
+* t/91-phase_simulated_gls_with_scaffold.t (reference panel, --kickstart)
+  and t/905-phase_simulated_gls_multi.t (split multi-allelic records) on the
+  reference's simulated example, scored by NRD against its truth VCF;
 * src/testing/insti_unittests.cpp:85-184 (Insti.loadGLs) -- sites, GLs
   before and after Insti::initialize, and the reference panel of the
   onlyThree sample files, read from the reference tree when it is present.
@@ -20,6 +23,7 @@ from glphase_gb300 import model as mdl
 
 REF = "/root/reference"
 SAMPLES = os.path.join(REF, "samples")
+HAPGEN = os.path.join(SAMPLES, "hapGen")
 ONLY_THREE = os.path.join(SAMPLES, "20_011976121_012173018.bin.onlyThree")
 needs_ref = pytest.mark.skipif(not os.path.isdir(SAMPLES),
                                reason="reference sample files not present")
@@ -153,3 +157,53 @@ def test_duplicate_site_input_is_rejected():
     simple.gls.v2.samePos.err.bin, whose last record repeats a site."""
     with pytest.raises(ValueError, match="already exists"):
         gio.read_bin(os.path.join(SAMPLES, "simple_gls", "simple.gls.v2.samePos.err.bin"))
+
+
+def _read_gls(path):
+    return gio.read_bin(path) if path.endswith(".bin") else gio.read_vcf_gls(path)
+
+
+@needs_ref
+@pytest.mark.parametrize("source", ["ex.bin", "ex.gls.vcf.gz"])
+def test_reference_panel_kickstart_nrd(oracle_lib, source):
+    """t/91-phase_simulated_gls_with_scaffold.t:31-58: ``-g ex.map -C100
+    -m10 -B0 -i3 -H ex.haps.gz -L ex.leg -k``: the 120 panel haplotypes
+    after the 120 sample rows, every chain's first proposal from the panel;
+    NRD against ex.vcf.gz below 5 (2.09 and 3.14 here; seeds 2-4: 2.18-2.43
+    and 3.05-3.20)."""
+    from glphase_gb300 import phase as ph
+    from phase_oracle import oracle_phase
+    d = _read_gls(os.path.join(HAPGEN, source))
+    gm = gio.read_genetic_map(os.path.join(HAPGEN, "ex.map"))
+    opts = ph.PhaseOptions(sa_burnin=0, burnin=3, sampling=10, cycles=100, seed=1,
+                           kick_first=True)
+    m, haps = ph.prepare(d.gl, d.sites.positions(), gm, seed=opts.seed)
+    panel = gio.load_reference_panel(os.path.join(HAPGEN, "ex.leg"),
+                                     os.path.join(HAPGEN, "ex.haps.gz"), d.sites)
+    assert panel.shape == (120, 16)
+    prob, _ = oracle_phase(oracle_lib, m, np.concatenate([haps, panel]), opts)
+    _, _, truth = gio.read_vcf_gt(os.path.join(HAPGEN, "ex.vcf.gz"))
+    nrd = gio.nrd(truth, gio.genotype_calls(prob))
+    assert 0 < nrd < 5, nrd
+
+
+@needs_ref
+@pytest.mark.parametrize("source,truth", [("ex.gls.multi.vcf.gz", "ex.multi.vcf.gz"),
+                                          ("ex.gls.almost_multi.vcf.gz",
+                                           "ex.almost_multi.vcf.gz")])
+def test_multiallelic_simulated_gls_nrd(oracle_lib, source, truth):
+    """t/905-phase_simulated_gls_multi.t:29-51: ``-C100 -m20 -B5 -i5 -Fbcf``
+    without a map on GLs whose multi-allelic sites are split into biallelic
+    records at one position (and on the version with neighbouring
+    positions); 0 < NRD < 5.5 (4.93 and 5.08 here; seeds 2-4: 5.03-5.09 and
+    5.00-5.07)."""
+    from glphase_gb300 import phase as ph
+    from phase_oracle import oracle_phase
+    d = gio.read_vcf_gls(os.path.join(HAPGEN, source))
+    opts = ph.PhaseOptions(sa_burnin=5, burnin=5, sampling=20, cycles=100, seed=1)
+    m, haps = ph.prepare(d.gl, d.sites.positions(), None, seed=opts.seed)
+    prob, _ = oracle_phase(oracle_lib, m, haps, opts)
+    _, sites, want = gio.read_vcf_gt(os.path.join(HAPGEN, truth))
+    assert sites.pos == d.sites.pos and sites.alt == d.sites.alt
+    nrd = gio.nrd(want, gio.genotype_calls(prob))
+    assert 0 < nrd < 5.5, nrd
