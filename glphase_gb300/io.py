@@ -109,6 +109,35 @@ def gl_pair(hom_ref, het, hom_alt) -> tuple[np.float32, np.float32]:
     return F32(h / s), F32(a / s)
 
 
+def strtof(tokens) -> np.ndarray:
+    """Decimal strings to binary32 as ``std::stof`` (strtof) rounds them:
+    straight from the decimal value to the nearest binary32, ties to even.
+    Parsing to binary64 first and rounding that is the same except where the
+    binary64 value lands exactly on a binary32 midpoint without the decimal
+    being there; those few are settled against the exact decimal."""
+    from decimal import Decimal
+    toks = list(tokens)
+    d = np.array(toks, dtype=np.float64) if toks else np.zeros(0)
+    with np.errstate(over="ignore"):
+        f = d.astype(F32)
+    toward = np.where(d > f.astype(np.float64), np.inf, -np.inf).astype(F32)
+    g = np.nextafter(f, toward)
+    mid = (f.astype(np.float64) + g.astype(np.float64)) / 2
+    tie = (d == mid) & (d != f.astype(np.float64)) & np.isfinite(d)
+    for i in np.flatnonzero(tie):
+        x, m = Decimal(toks[i].strip()), Decimal(float(mid[i]))
+        if x != m:  # the decimal is off the midpoint: round toward its side
+            f[i] = g[i] if (x > m) == (g[i] > f[i]) else f[i]
+    return f
+
+
+def gl_pairs(hom_ref: np.ndarray, het: np.ndarray, hom_alt: np.ndarray):
+    """``gl_pair`` over arrays (the same binary32 operations elementwise)."""
+    hr, h, a = (np.asarray(x, dtype=F32) for x in (hom_ref, het, hom_alt))
+    s = (hr + h) + a
+    return h / s, a / s
+
+
 def gl2prob(val) -> np.float32:
     """Bio::gl2prob (bio.hpp:154-161): 10^val in binary32, clamped to [0, 1]."""
     with np.errstate(over="ignore"):
@@ -142,7 +171,8 @@ def read_bin(path: str, keep: set[str] | None = None,
         names = header[3:]
         idx = [i for i, n in enumerate(names) if not keep or n in keep]
         sites = Sites()
-        rows = []
+        het_tok: list[str] = []
+        alt_tok: list[str] = []
         not_read = 0
         for line_num, line in enumerate(fd, start=2):
             tokens = line.rstrip("\n").split("\t")
@@ -165,17 +195,21 @@ def read_bin(path: str, keep: set[str] | None = None,
             else:
                 ref, alt = alleles[0], alleles[1]
             sites.push_ordered(tokens[0], pos, ref, alt)
-            row = np.empty((len(idx), 2), dtype=F32)
-            one, zero = F32(1), F32(0)
-            for k, i in enumerate(idx):
-                het, hom_alt = tokens[3 + i].split()
-                h, a = F32(float(het)), F32(float(hom_alt))
-                row[k] = gl_pair(max(zero, F32(F32(one - h) - a)), h, a)
-            rows.append(row)
-    if rows:
-        gl = np.ascontiguousarray(np.stack(rows, axis=1))
-    else:
-        gl = np.zeros((len(idx), 0, 2), dtype=F32)
+            for i in idx:
+                pair = tokens[3 + i].split()
+                if len(pair) < 2:
+                    raise ValueError(f"Input line {line_num}: could not parse the GL pair "
+                                     f"[{tokens[3 + i]}]")
+                het_tok.append(pair[0])
+                alt_tok.append(pair[1])
+    S, n = len(sites), len(idx)
+    # stof of each value, then the trio (max(0, 1 - het - homAlt), het, homAlt)
+    # kept as gl_pair keeps it (glReader.cpp:272-283), all in binary32
+    h = strtof(het_tok).reshape(S, n)
+    a = strtof(alt_tok).reshape(S, n)
+    hr = np.maximum((F32(1) - h) - a, F32(0))
+    ph, pa = gl_pairs(hr, h, a)
+    gl = np.ascontiguousarray(np.stack([ph, pa], axis=-1).transpose(1, 0, 2))
     return BinGLs([names[i] for i in idx], sites, gl, not_read)
 
 
@@ -580,6 +614,25 @@ def hap_match(test_gt: np.ndarray, expected_gt: np.ndarray) -> str | None:
                     return (f"Haplotypes do not match at line {m + 1}, at Allele number "
                             f"{2 * i + j + 1}")
     return None
+
+
+def nrd_matched(truth_names, truth_sites: Sites, truth_gt: np.ndarray,
+                test_names, test_sites: Sites, test_gt: np.ndarray) -> tuple[float, int, int]:
+    """``nrd`` over what two call sets share, as ``bcftools stats A B -s
+    <A's samples>`` pairs them: samples by name, sites by chrom, position,
+    ref and alt.  Returns (NRD percent, shared samples, shared sites)."""
+    ti = {n: i for i, n in enumerate(test_names)}
+    si = {k: i for i, k in enumerate(zip(test_sites.chrom, test_sites.pos, test_sites.ref,
+                                         test_sites.alt))}
+    sites = [(j, si[k]) for j, k in enumerate(zip(truth_sites.chrom, truth_sites.pos,
+                                                   truth_sites.ref, truth_sites.alt))
+             if k in si]
+    samples = [(i, ti[n]) for i, n in enumerate(truth_names) if n in ti]
+    if not sites or not samples:
+        return 0.0, len(samples), len(sites)
+    tr = np.asarray(truth_gt)[np.ix_([a for a, _ in samples], [a for a, _ in sites])]
+    te = np.asarray(test_gt)[np.ix_([b for _, b in samples], [b for _, b in sites])]
+    return nrd(tr, te), len(samples), len(sites)
 
 
 def dosages(gt: np.ndarray) -> np.ndarray:

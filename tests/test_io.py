@@ -78,6 +78,36 @@ def test_bin_format_errors(tmp_path):
             gio.read_bin(str(p))
 
 
+def test_strtof_rounds_the_decimal_once():
+    """std::stof rounds the decimal straight to binary32; a decimal just off
+    a binary32 midpoint whose nearest binary64 IS the midpoint must still go
+    to its own side (binary64 first, then binary32 would tie to even)."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 60
+    one, up = np.float32(1), np.nextafter(np.float32(1), np.float32(2))
+    m = Decimal(1) + Decimal(2) ** -24                # midpoint of 1 and 1 + 2^-23
+    eps = Decimal(2) ** -80
+    got = gio.strtof([str(m + eps), str(m - eps), str(m), "0.2", "1e-3", " 0.5", "0"])
+    assert got[0] == up and got[1] == one and got[2] == one   # exact tie: to even
+    assert np.float32(float(str(m + eps))) == one             # the binary64 route differs
+    m3 = Decimal(1) + 3 * Decimal(2) ** -24               # tie between odd and even
+    assert gio.strtof([str(m3)])[0] == np.nextafter(up, np.float32(2))
+    assert gio.strtof([str(m3 - eps)])[0] == up
+    assert list(got[3:]) == [np.float32(0.2), np.float32(1e-3), np.float32(0.5), 0]
+
+
+def test_nrd_matched_pairs_samples_and_sites_by_name():
+    ts = gio.Sites(["1"] * 3, [10, 20, 30], ["A", "C", "G"], ["T", "G", "A"])
+    qs = gio.Sites(["1"] * 3, [10, 30, 30], ["A", "G", "G"], ["T", "C", "A"])
+    truth = np.array([[[0, 1], [1, 1], [0, 0]], [[1, 1], [0, 0], [0, 1]]], np.int8)
+    test = np.array([[[0, 0], [0, 0], [0, 1]], [[1, 0], [0, 0], [0, 0]]], np.int8)
+    # test samples in the other order; sites 10 and 30:G>A are shared
+    nrd, ns, nsite = gio.nrd_matched(["a", "b"], ts, truth, ["b", "a"], qs, test)
+    assert (ns, nsite) == (2, 2)
+    # a: 0|1 vs 1|0 agree, 0|0 vs 0|0 not counted; b: 1|1 vs 0|0 differ, 0|1 vs 0|1 -> 1 of 3
+    assert nrd == pytest.approx(100 / 3)
+
+
 def test_gl_conversions():
     """Bio::gl2prob / Bio::phred2prob (bio.hpp:154-170) and the GL trio the
     reference keeps (glReader.cpp:202-213)."""

@@ -9,6 +9,9 @@
 * t/91-phase_simulated_gls_with_scaffold.t (reference panel, --kickstart)
   and t/905-phase_simulated_gls_multi.t (split multi-allelic records) on the
   reference's simulated example, scored by NRD against its truth VCF;
+* t/92-phase_real_gls_with_pre_haps_multi.t's real GLs (2,495 samples,
+  1,024 sites with split multi-allelic records) phased from the .bin without
+  pre-existing haplotypes and scored against the chip genotypes;
 * src/testing/insti_unittests.cpp:85-184 (Insti.loadGLs) -- sites, GLs
   before and after Insti::initialize, and the reference panel of the
   onlyThree sample files, read from the reference tree when it is present.
@@ -207,3 +210,29 @@ def test_multiallelic_simulated_gls_nrd(oracle_lib, source, truth):
     assert sites.pos == d.sites.pos and sites.alt == d.sites.alt
     nrd = gio.nrd(want, gio.genotype_calls(prob))
     assert 0 < nrd < 5.5, nrd
+
+
+@needs_ref
+def test_real_gls_nrd(oracle_lib):
+    """t/92-phase_real_gls_with_pre_haps_multi.t:59-100 without the
+    pre-existing haplotypes (a scaffold is outside this path) and from the
+    .bin (the tree holds no BCF of these GLs): ``-R20:5335724-5861377 -g
+    map -C100 -m10 -B0 -i5``, NRD against the Omni chip genotypes of the
+    shared samples and sites below 15 (11.1 here)."""
+    from glphase_gb300 import phase as ph
+    from phase_oracle import oracle_phase
+    src = os.path.join(SAMPLES, "multi_gls")
+    d = gio.read_bin(os.path.join(src, "chr20.5335724-5861377.1024_site_subset.HRC.r1.AC5."
+                                       "TGPP3_samples.likelihoods.winniFilter.bin"),
+                     region=("20", 5335724, 5861377))
+    assert len(d.names) == 2495 and len(d.sites) == 1024
+    gm = gio.read_genetic_map(os.path.join(SAMPLES, "geneticMap",
+                                           "genetic_map_chr20_combined_b37.txt.gz"))
+    opts = ph.PhaseOptions(sa_burnin=0, burnin=5, sampling=10, cycles=100, seed=1)
+    m, haps = ph.prepare(d.gl, d.sites.positions(), gm, seed=opts.seed)
+    prob, _ = oracle_phase(oracle_lib, m, haps, opts)
+    tn, ts, tg = gio.read_vcf_gt(os.path.join(
+        src, "20.5335724-5861377.chip.omni_broad_sanger_combined.20140818.snps.genotypes.vcf.gz"))
+    nrd, ns, nsite = gio.nrd_matched(tn, ts, tg, d.names, d.sites, gio.genotype_calls(prob))
+    assert ns > 300 and nsite > 300
+    assert 0 < nrd < 15, nrd
