@@ -33,7 +33,7 @@ class DeviceProblem:
     and new haplotype buffers, outputs."""
 
     def __init__(self, dev: HMMLikeCUDA, chunk, cycles: int, seed: int, burnin: int,
-                 kick_start: bool = False):
+                 kick_start: bool = False, vq=None):
         import torch
         self.dev = dev
         self.chunk = chunk
@@ -47,6 +47,15 @@ class DeviceProblem:
         dev._c(dev.L.glp_problem_set_model_device(self.pb, tran.ctypes.data, pc.ctypes.data,
                                                   chunk.emit.data_ptr(), chunk.prob.data_ptr(),
                                                   self.N, self.S))
+        # vq = (packed [ceil(S/8)][N] uint32, codebook [16][2] float32): the
+        # 4-bit GL codes replace the float emission (GLP_GEN_VQ)
+        self.flags = 0
+        if vq is not None:
+            packed = np.ascontiguousarray(vq[0], dtype=np.uint32)
+            cb = np.ascontiguousarray(vq[1], dtype=np.float32)
+            dev._c(dev.L.glp_problem_set_vq(self.pb, packed.ctypes.data, packed.size,
+                                            cb.ctypes.data))
+            self.flags = nat.GLP_GEN_VQ
         self.haps = chunk.haps
         self.hnew = chunk.haps.clone()
         self.quad = torch.zeros((4, self.N), dtype=torch.int32, device=chunk.haps.device)
@@ -59,6 +68,7 @@ class DeviceProblem:
         a.hap_idxs_out, a.like_out = self.quad.data_ptr(), self.like.data_ptr()
         a.pen = float(anneal_pen(generation, self.burnin))
         a.seed, a.generation, a.burnin = self.seed, generation, self.burnin
+        a.flags = self.flags
         if self.kick_start and generation == 0:
             a.sample_lo, a.sample_hi, a.kick_start = 2 * self.N, self.H, 1
         return a

@@ -1246,8 +1246,9 @@ int glp_get_stats(glp_ctx *c, uint64_t *evaluations, uint64_t *rounds, uint32_t 
 // problem, a generation template, a generation count) wait in a FIFO queue;
 // each tick admits the queued requests whose device footprint fits the
 // remaining budget, runs one generation of every resident request -- one
-// persistent launch for all of them (glp_run_batch), or one such launch per
-// request in the plain form -- waits for it, and retires the requests that have done
+// persistent launch for all of them (glp_run_batch; two when both emission
+// sources are resident), or one such launch per request in the plain form --
+// waits for it, and retires the requests that have done
 // their generations.  A request's generation g runs with the annealing
 // penalty of Insti::estimate (insti.cpp:1670-1671) for the template's
 // burn-in, reads the template's haps buffer on even generations and its hnew
@@ -1378,7 +1379,18 @@ int glp_server_tick(glp_server *s, uint32_t *resident, uint32_t *finished) {
     for (size_t i = 0; i < n && !rc; ++i)
       rc = glp_run_batch(c, 1, &pbs[i], &args[i]);
   } else {
-    rc = glp_run_batch(c, (uint32_t)n, pbs.data(), args.data());
+    // one launch per emission source present (a launch holds one kind)
+    for (uint32_t vq = 0; vq < 2 && !rc; ++vq) {
+      std::vector<glp_generation_args> ga;
+      std::vector<glp_problem *> gp;
+      for (size_t i = 0; i < n; ++i)
+        if (((args[i].flags & GLP_GEN_VQ) != 0) == (vq == 1)) {
+          ga.push_back(args[i]);
+          gp.push_back(pbs[i]);
+        }
+      if (!gp.empty())
+        rc = glp_run_batch(c, (uint32_t)gp.size(), gp.data(), ga.data());
+    }
   }
   if (rc)
     return rc;

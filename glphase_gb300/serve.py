@@ -43,6 +43,7 @@ class Request:
     finished: float = -1.0
     problem: DeviceProblem | None = None
     gen: int = 0
+    vq: tuple | None = None  # (packed codes, codebook): VQ emissions instead of float
 
     @property
     def updates(self) -> int:
@@ -98,7 +99,7 @@ class Server:
             if self.used + need > self.budget:
                 break
             self.queue.pop(0)
-            r.problem = DeviceProblem(self.dev, r.chunk, r.cycles, r.seed, r.burnin)
+            r.problem = DeviceProblem(self.dev, r.chunk, r.cycles, r.seed, r.burnin, vq=r.vq)
             r.admitted = now
             self.used += need
             self.active.append(r)
@@ -188,7 +189,8 @@ class NativeServer(Server):
         import ctypes as C
         from . import native as nat
         L = self.dev.L
-        req.problem = DeviceProblem(self.dev, req.chunk, req.cycles, req.seed, req.burnin)
+        req.problem = DeviceProblem(self.dev, req.chunk, req.cycles, req.seed, req.burnin,
+                                    vq=req.vq)
         a = req.problem.args(0)
         rid = C.c_uint64()
         rc = L.glp_server_submit(self.srv, req.problem.pb, C.byref(a), req.generations,

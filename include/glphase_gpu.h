@@ -272,7 +272,8 @@ void glp_batch_destroy(glp_batch *batch);
  * requests whose device footprint, N*S*44 + 2*H*ceil(S/64)*8 bytes
  * (emission, genotype probabilities, hmm_work scratch, both haplotype
  * buffers), fits what is left of budget_bytes, runs one generation of every
- * resident request -- all in one glp_run_batch launch, or one glp_run_batch
+ * resident request -- all in one glp_run_batch launch (one per emission
+ * source, float or GLP_GEN_VQ, when both are resident), or one glp_run_batch
  * launch per request when `plain` -- waits for it, and retires the requests
  * that have run G generations.  Generation g of a request takes the
  * template with generation = g; pen = min((g+1)/burnin, 1)^2 in binary32

@@ -104,3 +104,33 @@ def test_native_server_budget_and_mix(dev):
     with pytest.raises(ValueError, match="more than the budget"):
         small.submit(make(8, 30, 300, 2))
     small.close()
+
+
+def test_native_server_mixes_emission_sources(dev):
+    """Float and 4-bit VQ requests resident together: the tick launches each
+    emission source on its own, and every request's result equals the one
+    it gets alone."""
+    import numpy as np
+    import torch
+    from glphase_gb300.glpack import GLPack
+
+    def reqs():
+        out = [make(i, N, S, G) for i, N, S, G in SPECS[:4]]
+        for r in out[1::2]:
+            gp = GLPack(r.chunk.prob.cpu().numpy(), np.random.default_rng(r.rid))
+            r.vq = (gp.packed_gls(), gp.code_book())
+        return out
+
+    alone = reqs()
+    for r in alone:
+        s = NativeServer(dev, budget_bytes=1 << 34)
+        s.serve([r])
+        s.close()
+    mix = reqs()
+    srv = NativeServer(dev, budget_bytes=1 << 34)
+    st = srv.serve(mix)
+    srv.close()
+    assert st.peak_resident == 4
+    for a, b in zip(alone, mix):
+        assert torch.equal(a.result_haps, b.result_haps), a.rid
+        assert torch.equal(a.result_like, b.result_like), a.rid

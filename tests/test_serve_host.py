@@ -46,7 +46,7 @@ class FakeDev:
 
 
 class FakeProblem:
-    def __init__(self, dev, chunk, cycles, seed, burnin):
+    def __init__(self, dev, chunk, cycles, seed, burnin, vq=None):
         self.chunk, self.seed = chunk, seed
         self.haps, self.hnew = "a", "b"
         self.like = None
