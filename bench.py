@@ -569,12 +569,12 @@ def run_uneven(args):
 def run_serve(args):
     """Poisson-arriving phasing requests (uneven-chunk shapes, 32 generations
     each) served with continuous batching at 0.5x, 1x and 2x the measured
-    capacity; the plain form (one launch per resident request per tick) at
-    1x beside it."""
+    capacity; the plain form (one launch per resident request per tick) and
+    the library's own serving loop (glp_server_*) at 1x beside it."""
     import torch
     from glphase_gb300 import synth, synth_device as sd
     from glphase_gb300.hmmlike import HMMLikeCUDA
-    from glphase_gb300.serve import Request, Server
+    from glphase_gb300.serve import NativeServer, Request, Server
     C, G = args.cycles, args.generations
     shapes = uneven_shapes(args.requests, seed=9, scale=args.scale)
     dev = HMMLikeCUDA(0)
@@ -603,16 +603,19 @@ def run_serve(args):
     capacity_ups = per_gen / (time.perf_counter() - t0)
     capacity_rps = capacity_ups / mean_updates
     results = {}
-    for load, plain in ((0.5, False), (1.0, False), (2.0, False), (1.0, True)):
+    for load, plain, native in ((0.5, False, False), (1.0, False, False), (2.0, False, False),
+                                (1.0, True, False), (1.0, False, True)):
         rng = np.random.default_rng(int(load * 100) + plain)
         gaps = rng.exponential(1.0 / (load * capacity_rps), size=len(shapes))
         reqs = [make(i, N, S) for i, (N, S) in enumerate(shapes)]
         for r, a in zip(reqs, np.cumsum(gaps)):
             r.arrival = float(a)
         torch.cuda.synchronize()
-        srv = Server(dev, budget, plain=plain)
+        srv = (NativeServer if native else Server)(dev, budget, plain=plain)
         st = srv.serve(reqs, time_limit=args.serve_limit)
-        key = ("plain" if plain else "batched") + f"@{load}x"
+        if native:
+            srv.close()
+        key = ("native" if native else "plain" if plain else "batched") + f"@{load}x"
         results[key] = st.summary()
         del reqs, srv
         torch.cuda.empty_cache()
@@ -626,7 +629,9 @@ def run_serve(args):
                                f"shapes, {G} generations each, C={C}, panel off",
                    "hbm_budget_gb": args.budget_gb, "capacity_updates_per_s": capacity_ups,
                    "capacity_requests_per_s": capacity_rps, "results": results,
-                   "batched_over_plain_at_1x": b1["updates_per_s"] / p1["updates_per_s"]},
+                   "batched_over_plain_at_1x": b1["updates_per_s"] / p1["updates_per_s"],
+                   "native_over_python_loop_at_1x":
+                       results["native@1.0x"]["updates_per_s"] / b1["updates_per_s"]},
     }
     print(json.dumps(line), flush=True)
 
