@@ -1332,11 +1332,20 @@ int glp_server_submit(glp_server *s, glp_problem *pb, const glp_generation_args 
     return fail(c, GLP_ERR_ARG, "request needs %llu bytes, more than the budget %llu",
                 (unsigned long long)bytes, (unsigned long long)s->budget);
   glp_server::Req r;
-  r.id = s->next_id++;
   r.pb = pb;
   r.tmpl = *args;
   r.generations = generations;
   r.bytes = bytes;
+  // validate the first generation now (sizes, model inputs, buffers), so a
+  // bad request is refused here rather than failing every later tick
+  int rc = check_ctx(c);
+  if (rc)
+    return rc;
+  const glp_generation_args first = request_args(r);
+  glp::GenParams scratch;
+  if ((rc = make_params(c, pb, &first, &scratch)))
+    return rc;
+  r.id = s->next_id++;
   s->reqs.push_back(r);
   s->queue.push_back(s->reqs.size() - 1);
   if (request_id)

@@ -292,7 +292,9 @@ typedef struct glp_server glp_server;
 
 int glp_server_create(glp_ctx *ctx, uint64_t budget_bytes, int plain, glp_server **out);
 /* GLP_ERR_ARG when the footprint exceeds the whole budget, the problem
- * belongs to another context, hnew is NULL or GLP_GEN_NO_WORK is set. */
+ * belongs to another context, hnew is NULL or GLP_GEN_NO_WORK is set; the
+ * request's first generation is validated as glp_run_batch would (sizes,
+ * buffers, the problem's model inputs), with the same status codes. */
 int glp_server_submit(glp_server *server, glp_problem *problem,
                       const glp_generation_args *args, uint32_t generations,
                       uint64_t *request_id);

@@ -104,6 +104,13 @@ def test_native_server_budget_and_mix(dev):
     with pytest.raises(ValueError, match="more than the budget"):
         small.submit(make(8, 30, 300, 2))
     small.close()
+    # a request whose sizes disagree with its problem is refused at submit
+    bad = make(7, 30, 300, 2)
+    bad.chunk.H = 2 * 30 - 1
+    srv = NativeServer(dev, budget_bytes=1 << 34)
+    with pytest.raises(ValueError, match="num_haps"):
+        srv.submit(bad)
+    srv.close()
 
 
 def test_native_server_mixes_emission_sources(dev):
