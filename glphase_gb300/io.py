@@ -324,6 +324,14 @@ class GeneticMap:
         diff_genom = float(p[hi] - p[lo])
         return float(self.cm[lo]) + (pos - int(p[lo])) / diff_genom * diff_gen
 
+    def distance(self, first: int, second: int) -> float:
+        """GeneticMap::GeneticDistance (geneticMap.cpp:72-79): Morgans from
+        ``first`` to ``second``; ``first`` may not lie after ``second`` and
+        both must be on the map."""
+        if first > second:
+            raise ValueError("first is larger than second")
+        return (self.location(second) - self.location(first)) / 100
+
     def distances(self, positions) -> np.ndarray:
         """r[m] = GeneticDistance(pos[m-1], pos[m]) in Morgans
         (geneticMap.cpp:72-79); r[0] = 0.  This is the input of

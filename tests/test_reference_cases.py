@@ -236,3 +236,50 @@ def test_real_gls_nrd(oracle_lib):
     nrd, ns, nsite = gio.nrd_matched(tn, ts, tg, d.names, d.sites, gio.genotype_calls(prob))
     assert ns > 300 and nsite > 300
     assert 0 < nrd < 15, nrd
+
+
+@needs_ref
+def test_genetic_map_known_answers():
+    """other_unittests.cpp:382-418 (GeneticMap errorOK, locationOK,
+    distanceOK) on genetic_map_chr20_combined_b37."""
+    gm = gio.read_genetic_map(os.path.join(SAMPLES, "geneticMap",
+                                           "genetic_map_chr20_combined_b37.txt.gz"))
+    for a, b in ((1140749, 1140727), (0, 1140727), (1140727, 70000000)):
+        with pytest.raises(ValueError):
+            gm.distance(a, b)
+    hi, lo = 5.49294973985857, 5.49294697413266
+    assert gm.location(1140749) == pytest.approx(hi, rel=4 * 2 ** -52)
+    assert gm.location(1140727) == pytest.approx(lo, rel=4 * 2 ** -52)
+    assert gm.location(1140730) == pytest.approx(lo + (hi - lo) * 3 / 22, rel=4 * 2 ** -52)
+    assert gm.distance(1140727, 1140749) == pytest.approx((hi - lo) / 100, rel=1e-12)
+    assert gm.distance(61795, 1140727) == pytest.approx(0.0549294697413266, rel=4 * 2 ** -52)
+    assert gm.distance(61795, 62949445) == pytest.approx(1.10205396293913, rel=4 * 2 ** -52)
+    assert gm.distance(1140727, 62949445) == pytest.approx(1.0471244931978034,
+                                                           rel=4 * 2 ** -52)
+    assert gm.distance(1140727, 1140732) == pytest.approx((hi - lo) / 22 * 5 / 100, abs=1e-9)
+    assert gm.distance(1140507, 1140732) == pytest.approx(
+        ((lo - 5.49291291069285) / 270 * 220 + (hi - lo) / 22 * 5) / 100, abs=1e-8)
+
+
+@needs_ref
+@pytest.mark.parametrize("suffix", [".bin", ".vcf.gz"])
+def test_gl_reader_region_and_size_limit(suffix):
+    """glReader_tests.cpp:174-224: the region 20:11976121-11976813 and a
+    size limit of 3 both keep the first three sites, with their GLs."""
+    path = ONLY_THREE + suffix
+    read = gio.read_bin if suffix == ".bin" else gio.read_vcf_gls
+    full = read(path)
+    for d in (read(path, region=("20", 11976121, 11976813)), read(path, size_limit=3)):
+        assert d.sites.pos == full.sites.pos[:3] == [11976121, 11976755, 11976813]
+        assert np.array_equal(d.gl, full.gl[:, :3])
+    assert read(path, size_limit=3).not_read == 1021
+
+
+@needs_ref
+def test_reference_panel_needs_both_files(tmp_path):
+    """insti_unittests.cpp:424-441: a hap file without its legend, or a
+    legend without its hap file, is refused."""
+    from glphase_gb300 import phase as ph
+    for leg, hap in ((None, ONLY_THREE + ".hap"), (ONLY_THREE + ".legend", None)):
+        with pytest.raises(ValueError, match="both a legend and a hap file"):
+            ph.phase_bin(ONLY_THREE + ".bin", ref_legend=leg, ref_hap=hap)
