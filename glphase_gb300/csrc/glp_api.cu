@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/glphase_gpu.h"
+#include "glp_server_core.h"
 #include "glp_knn.cuh"
 #include "glp_launch.h"
 #include "glp_tally.cuh"
@@ -1242,66 +1243,16 @@ int glp_get_stats(glp_ctx *c, uint64_t *evaluations, uint64_t *rounds, uint32_t 
 }
 
 // ---------------------------------------------------------------------------
-// Request server: continuous batching behind the context.  Requests (a
-// problem, a generation template, a generation count) wait in a FIFO queue;
-// each tick admits the queued requests whose device footprint fits the
-// remaining budget, runs one generation of every resident request -- one
-// persistent launch for all of them (glp_run_batch; two when both emission
-// sources are resident), or one such launch per request in the plain form --
-// waits for it, and retires the requests that have done
-// their generations.  A request's generation g runs with the annealing
-// penalty of Insti::estimate (insti.cpp:1670-1671) for the template's
-// burn-in, reads the template's haps buffer on even generations and its hnew
-// buffer on odd ones (and writes the other), and applies the template's
-// kick-start range in generation 0 only.  Every draw is keyed by the
+// Request server: continuous batching behind the context.  The scheduling
+// (queue, admission, per-request generation arguments, retirement) is
+// glp::ServerCore (glp_server_core.h); here each tick's launches go to
+// glp_run_batch and the tick waits for them.  Every draw is keyed by the
 // request's seed and generation, so its result does not depend on the mix.
 
 struct glp_server {
-  struct Req {
-    uint64_t id = 0;
-    glp_problem *pb = nullptr;
-    glp_generation_args tmpl{};
-    uint32_t generations = 0, gen = 0;
-    uint64_t bytes = 0;
-    int state = GLP_REQ_QUEUED;
-  };
   glp_ctx *c = nullptr;
-  uint64_t budget = 0, used = 0;
-  bool plain = false;
-  uint64_t next_id = 1;
-  std::vector<Req> reqs;              // every request, in submission order
-  std::vector<size_t> queue, active;  // indices into reqs
-  uint64_t ticks = 0, updates = 0;
+  glp::ServerCore core;
 };
-
-namespace {
-
-uint64_t request_bytes(const glp_generation_args *a) {
-  const uint64_t N = a->num_samples, S = a->num_sites, H = a->num_haps;
-  return N * S * (16 + 12 + 16) + 2 * H * ((S + 63) / 64) * 8;
-}
-
-// The arguments of generation g of a request.
-glp_generation_args request_args(const glp_server::Req &r) {
-  glp_generation_args a = r.tmpl;
-  const uint32_t g = r.gen;
-  a.generation = g;
-  if (r.tmpl.burnin) {
-    const float x = std::min((float)(g + 1u) / (float)r.tmpl.burnin, 1.0f);
-    a.pen = x * x;
-  }
-  if (g & 1u) {
-    a.haps = r.tmpl.hnew;
-    a.hnew = const_cast<uint64_t *>(r.tmpl.haps);
-  }
-  if (r.tmpl.kick_start && g > 0) {
-    a.kick_start = 0;
-    a.sample_lo = a.sample_hi = 0;
-  }
-  return a;
-}
-
-}  // namespace
 
 int glp_server_create(glp_ctx *c, uint64_t budget_bytes, int plain, glp_server **out) {
   int rc = check_ctx(c);
@@ -1311,8 +1262,8 @@ int glp_server_create(glp_ctx *c, uint64_t budget_bytes, int plain, glp_server *
     return fail(c, GLP_ERR_ARG, "out must be non-null");
   glp_server *s = new glp_server();
   s->c = c;
-  s->budget = budget_bytes;
-  s->plain = plain != 0;
+  s->core.budget = budget_bytes;
+  s->core.plain = plain != 0;
   *out = s;
   return GLP_OK;
 }
@@ -1327,29 +1278,22 @@ int glp_server_submit(glp_server *s, glp_problem *pb, const glp_generation_args 
                                 "at least one generation");
   if (!args->hnew || (args->flags & GLP_GEN_NO_WORK))
     return fail(c, GLP_ERR_ARG, "a served request runs hmm_work: hnew is required");
-  const uint64_t bytes = request_bytes(args);
-  if (bytes > s->budget)
+  glp::ServerCore::Req r = glp::ServerCore::make(pb, *args, generations);
+  if (r.bytes > s->core.budget)
     return fail(c, GLP_ERR_ARG, "request needs %llu bytes, more than the budget %llu",
-                (unsigned long long)bytes, (unsigned long long)s->budget);
-  glp_server::Req r;
-  r.pb = pb;
-  r.tmpl = *args;
-  r.generations = generations;
-  r.bytes = bytes;
+                (unsigned long long)r.bytes, (unsigned long long)s->core.budget);
   // validate the first generation now (sizes, model inputs, buffers), so a
   // bad request is refused here rather than failing every later tick
   int rc = check_ctx(c);
   if (rc)
     return rc;
-  const glp_generation_args first = request_args(r);
+  const glp_generation_args first = glp::ServerCore::args_of(r);
   glp::GenParams scratch;
   if ((rc = make_params(c, pb, &first, &scratch)))
     return rc;
-  r.id = s->next_id++;
-  s->reqs.push_back(r);
-  s->queue.push_back(s->reqs.size() - 1);
+  const uint64_t id = s->core.add(r);
   if (request_id)
-    *request_id = r.id;
+    *request_id = id;
   return GLP_OK;
 }
 
@@ -1360,97 +1304,59 @@ int glp_server_tick(glp_server *s, uint32_t *resident, uint32_t *finished) {
   int rc = check_ctx(c);
   if (rc)
     return rc;
-  // admit in arrival order while the next request fits
-  while (!s->queue.empty()) {
-    glp_server::Req &r = s->reqs[s->queue.front()];
-    if (s->used + r.bytes > s->budget)
-      break;
-    s->used += r.bytes;
-    r.state = GLP_REQ_RESIDENT;
-    s->active.push_back(s->queue.front());
-    s->queue.erase(s->queue.begin());
-  }
-  if (resident)
-    *resident = (uint32_t)s->active.size();
-  if (finished)
-    *finished = 0;
-  if (s->active.empty())
-    return GLP_OK;
-  const size_t n = s->active.size();
-  std::vector<glp_generation_args> args(n);
-  std::vector<glp_problem *> pbs(n);
-  for (size_t i = 0; i < n; ++i) {
-    const glp_server::Req &r = s->reqs[s->active[i]];
-    args[i] = request_args(r);
-    pbs[i] = r.pb;
-  }
-  if (s->plain) {
-    for (size_t i = 0; i < n && !rc; ++i)
-      rc = glp_run_batch(c, 1, &pbs[i], &args[i]);
-  } else {
-    // one launch per emission source present (a launch holds one kind)
-    for (uint32_t vq = 0; vq < 2 && !rc; ++vq) {
-      std::vector<glp_generation_args> ga;
-      std::vector<glp_problem *> gp;
-      for (size_t i = 0; i < n; ++i)
-        if (((args[i].flags & GLP_GEN_VQ) != 0) == (vq == 1)) {
-          ga.push_back(args[i]);
-          gp.push_back(pbs[i]);
-        }
-      if (!gp.empty())
-        rc = glp_run_batch(c, (uint32_t)gp.size(), gp.data(), ga.data());
+  auto run = [c](const std::vector<glp::ServerCore::Launch> &launches) {
+    for (const auto &l : launches) {
+      std::vector<glp_problem *> pbs;
+      for (void *p : l.problems)
+        pbs.push_back(static_cast<glp_problem *>(p));
+      const int r = glp_run_batch(c, (uint32_t)pbs.size(), pbs.data(), l.args.data());
+      if (r)
+        return r;
     }
-  }
-  if (rc)
-    return rc;
-  if ((rc = glp_finish(c)))
-    return rc;
-  ++s->ticks;
-  uint32_t done = 0;
-  std::vector<size_t> still;
-  for (size_t i : s->active) {
-    glp_server::Req &r = s->reqs[i];
-    s->updates += (uint64_t)r.tmpl.num_samples * (r.tmpl.num_cycles + 1) * r.tmpl.num_sites;
-    if (++r.gen >= r.generations) {
-      r.state = GLP_REQ_DONE;
-      s->used -= r.bytes;
-      ++done;
-    } else {
-      still.push_back(i);
-    }
-  }
-  s->active.swap(still);
-  if (finished)
-    *finished = done;
-  return GLP_OK;
+    return glp_finish(c);
+  };
+  return s->core.tick(run, resident, finished);
 }
 
 int glp_server_poll(glp_server *s, uint64_t request_id, int *state, uint32_t *generations_done,
                     const uint64_t **haps) {
   if (!s)
     return GLP_ERR_ARG;
-  for (const glp_server::Req &r : s->reqs)
-    if (r.id == request_id) {
-      if (state)
-        *state = r.state;
-      if (generations_done)
-        *generations_done = r.gen;
-      if (haps)  // the buffer the last finished generation wrote
-        *haps = (r.gen & 1u) ? r.tmpl.hnew : r.tmpl.haps;
-      return GLP_OK;
-    }
-  return fail(s->c, GLP_ERR_ARG, "no request %llu", (unsigned long long)request_id);
+  const glp::ServerCore::Req *r = s->core.find(request_id);
+  if (!r)
+    return fail(s->c, GLP_ERR_ARG, "no request %llu", (unsigned long long)request_id);
+  if (state)
+    *state = r->state;
+  if (generations_done)
+    *generations_done = r->gen;
+  if (haps)
+    *haps = glp::ServerCore::current_haps(*r);
+  return GLP_OK;
+}
+
+int glp_server_release(glp_server *s, uint64_t request_id) {
+  if (!s)
+    return GLP_ERR_ARG;
+  switch (s->core.release(request_id)) {
+  case 0:
+    return GLP_OK;
+  case 1:
+    return fail(s->c, GLP_ERR_ARG, "no request %llu", (unsigned long long)request_id);
+  default:
+    return fail(s->c, GLP_ERR_STATE, "request %llu has not finished",
+                (unsigned long long)request_id);
+  }
 }
 
 int glp_server_stats(glp_server *s, uint64_t *ticks, uint64_t *updates, uint64_t *used_bytes) {
   if (!s)
     return GLP_ERR_ARG;
   if (ticks)
-    *ticks = s->ticks;
+    *ticks = s->core.ticks;
   if (updates)
-    *updates = s->updates;
+    *updates = s->core.updates;
   if (used_bytes)
-    *used_bytes = s->used;
+    *used_bytes = s->core.used;
   return GLP_OK;
 }
 

@@ -40,7 +40,7 @@ EXPORTED = [
     "glp_set_evals_per_lane", "glp_get_counters", "glp_kernel_times", "glp_vq_train",
     "glp_vq_pack", "glp_set_block_sites", "glp_get_block_sites", "glp_server_create",
     "glp_server_submit", "glp_server_tick", "glp_server_poll", "glp_server_stats",
-    "glp_server_destroy",
+    "glp_server_destroy", "glp_server_release",
 ]
 
 
@@ -139,6 +139,7 @@ def load(build_if_missing: bool = False):
     L.glp_server_tick.argtypes = [vp, C.POINTER(u32), C.POINTER(u32)]
     L.glp_server_poll.argtypes = [vp, u64, C.POINTER(i32), C.POINTER(u32), C.POINTER(vp)]
     L.glp_server_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
+    L.glp_server_release.argtypes = [vp, u64]
     L.glp_server_destroy.argtypes = [vp]
     L.glp_server_destroy.restype = None
     for name in EXPORTED:

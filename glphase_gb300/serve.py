@@ -236,6 +236,7 @@ class NativeServer(Server):
                 r.result_haps = p.haps if ptr == p.haps.data_ptr() else p.hnew
                 r.result_like = p.like
                 p.close()
+                self.dev._c(L.glp_server_release(self.srv, self._ids.pop(r.rid)))
                 done.append(r)
         ticks, updates, used = C.c_uint64(), C.c_uint64(), C.c_uint64()
         self.dev._c(L.glp_server_stats(self.srv, C.byref(ticks), C.byref(updates),

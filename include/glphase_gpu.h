@@ -304,6 +304,9 @@ int glp_server_tick(glp_server *server, uint32_t *resident, uint32_t *finished);
  * the template's hnew after an odd number of generations, else its haps. */
 int glp_server_poll(glp_server *server, uint64_t request_id, int *state,
                     uint32_t *generations_done, const uint64_t **haps);
+/* Forget a finished request (its record; the caller owns its buffers):
+ * GLP_ERR_ARG for an unknown id, GLP_ERR_STATE before it has finished. */
+int glp_server_release(glp_server *server, uint64_t request_id);
 /* Ticks run, site updates done (N*(C+1)*S per request generation), bytes
  * held by resident requests. */
 int glp_server_stats(glp_server *server, uint64_t *ticks, uint64_t *updates,

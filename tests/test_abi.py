@@ -51,6 +51,7 @@ def test_null_context_errors(lib):
     assert lib.glp_server_tick(None, None, None) == 1
     assert lib.glp_server_poll(None, 1, None, None, None) == 1
     assert lib.glp_server_stats(None, None, None, None) == 1
+    assert lib.glp_server_release(None, 1) == 1
     lib.glp_server_destroy(None)
 
 
