@@ -2,8 +2,10 @@
 admission against the HBM budget, one generation per resident request per
 tick (one launch for the batched form, one per request for the plain form,
 a mixed-generation launch when residents are at different generations),
-retirement and latency bookkeeping.  The device calls are faked; the GPU
-behaviour (results identical alone and in the mix) is tests/test_gpu_serve.py."""
+retirement and latency bookkeeping; and the NativeServer wrapper over the
+library's glp_server_* calls.  The device calls are faked; the GPU
+behaviour (results identical alone and in the mix) is tests/test_gpu_serve.py,
+and the library's own scheduling is tests/test_server_core.py."""
 from dataclasses import dataclass
 
 import pytest
@@ -144,3 +146,126 @@ def test_serve_records_latencies(fake):
     assert len(stats.latencies) == 4 and all(l >= 0 for l in stats.latencies)
     s = stats.summary()
     assert s["requests"] == 4 and s["ticks"] == 2 and s["p99_latency_s"] >= s["p50_latency_s"]
+
+
+class FakeServerLib(FakeLib):
+    """glp_server_* over a small Python model of the library's scheduling:
+    FIFO admission under the budget, one generation per resident request
+    per tick, retirement, release."""
+
+    def __init__(self, log):
+        super().__init__(log)
+        self.reqs, self.queue, self.active = {}, [], []
+        self.budget = self.used = self.ticks = self.updates = 0
+        self.released = []
+
+    def glp_last_error(self, ctx):
+        return b"request needs many bytes, more than the budget"
+
+    def glp_server_create(self, ctx, budget, plain, out):
+        self.budget = budget
+        out._obj.value = 1
+        return 0
+
+    def glp_server_submit(self, srv, pb, args, G, rid):
+        a = args._obj
+        need = a.num_samples * a.num_sites * 44 + 2 * a.num_haps * ((a.num_sites + 63) // 64) * 8
+        if need > self.budget:
+            return 1
+        i = len(self.reqs) + 1
+        self.reqs[i] = dict(G=G, gen=0, need=need, state=0, haps=a.haps, hnew=a.hnew,
+                            upd=a.num_samples * (a.num_cycles + 1) * a.num_sites)
+        self.queue.append(i)
+        rid._obj.value = i
+        return 0
+
+    def glp_server_tick(self, srv, resident, finished):
+        while self.queue and self.used + self.reqs[self.queue[0]]["need"] <= self.budget:
+            i = self.queue.pop(0)
+            self.used += self.reqs[i]["need"]
+            self.reqs[i]["state"] = 1
+            self.active.append(i)
+        resident._obj.value, finished._obj.value = len(self.active), 0
+        if self.active:
+            self.ticks += 1
+        for i in list(self.active):
+            r = self.reqs[i]
+            r["gen"] += 1
+            self.updates += r["upd"]
+            if r["gen"] >= r["G"]:
+                r["state"] = 2
+                self.used -= r["need"]
+                self.active.remove(i)
+                finished._obj.value += 1
+        return 0
+
+    def glp_server_poll(self, srv, i, state, gen, ptr):
+        r = self.reqs[i]
+        state._obj.value, gen._obj.value = r["state"], r["gen"]
+        ptr._obj.value = r["hnew"] if r["gen"] % 2 else r["haps"]
+        return 0
+
+    def glp_server_stats(self, srv, ticks, updates, used):
+        ticks._obj.value, updates._obj.value, used._obj.value = \
+            self.ticks, self.updates, self.used
+        return 0
+
+    def glp_server_release(self, srv, i):
+        assert self.reqs[i]["state"] == 2
+        self.released.append(i)
+        return 0
+
+    def glp_server_destroy(self, srv):
+        self.log.append(("destroy",))
+
+
+class Tensor:
+    def __init__(self, addr):
+        self.addr = addr
+
+    def data_ptr(self):
+        return self.addr
+
+
+class PtrProblem(FakeProblem):
+    _next = 0x1000
+
+    def __init__(self, *a, **k):
+        super().__init__(*a, **k)
+        PtrProblem._next += 0x100
+        self.haps, self.hnew = Tensor(PtrProblem._next), Tensor(PtrProblem._next + 8)
+
+    def args(self, generation):
+        a = super().args(generation)
+        c = self.chunk
+        a.num_samples, a.num_sites, a.num_cycles, a.num_haps = c.N, c.S, 10, c.H
+        a.haps, a.hnew = self.haps.data_ptr(), self.hnew.data_ptr()
+        return a
+
+
+def test_native_server_wrapper(monkeypatch):
+    """serve.NativeServer over the glp_server_* calls: queued requests move
+    to active once the library admits them, finished ones take the buffer
+    the library names as their result and are released."""
+    dev = FakeDev()
+    dev.L = FakeServerLib(dev.log)
+    monkeypatch.setattr(serve, "DeviceProblem", PtrProblem)
+    a, b, c = request(0, G=1), request(1, G=2), request(2, G=1)
+    srv = serve.NativeServer(dev, budget_bytes=a.footprint() + b.footprint())
+    for r in (a, b, c):
+        srv.submit(r)
+    assert [r.rid for r in srv.queue] == [0, 1, 2]
+    done = srv.tick(0.0)                  # a and b resident; a finishes
+    assert [r.rid for r in done] == [0] and [r.rid for r in srv.active] == [1]
+    assert a.result_haps is a.problem.hnew and a.problem.closed
+    assert [r.rid for r in srv.queue] == [2]
+    done = srv.tick(0.1)                  # b finishes (its result back in haps); c admitted
+    assert sorted(r.rid for r in done) == [1, 2]
+    assert b.result_haps is b.problem.haps and c.result_haps is c.problem.hnew
+    assert dev.L.released == [1, 2, 3] and srv.used == 0 and srv.stats.ticks == 2
+    assert srv.stats.peak_resident == 2
+    srv.close()
+    assert ("destroy",) in dev.log
+    big = serve.NativeServer(dev, budget_bytes=10)
+    with pytest.raises(ValueError, match="more than the budget"):
+        big.submit(request(5))
