@@ -64,3 +64,17 @@ def test_shim_header_compiles():
         open(f, "w").write(src)
         subprocess.run(["g++", "-std=c++11", "-fsyntax-only", "-I",
                         os.path.join(ROOT, "include"), f], check=True)
+
+
+def test_header_compiles_as_c99():
+    """include/glphase_gpu.h is a C header: strict C99, no C++ constructs, so
+    a C caller (or a cgo / FFI binding generator) can include it."""
+    import subprocess, tempfile
+    src = ('#include "glphase_gpu.h"\n'
+           'int main(void) { glp_generation_args a = {0}; glp_ctx *c = 0; (void)a; (void)c;\n'
+           '  return GLP_REQ_DONE == 2 ? 0 : 1; }\n')
+    with tempfile.TemporaryDirectory() as d:
+        f = os.path.join(d, "t.c")
+        open(f, "w").write(src)
+        subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                        "-fsyntax-only", "-I", os.path.join(ROOT, "include"), f], check=True)
