@@ -153,6 +153,27 @@ def phred2prob(phred: int) -> np.float32:
     return F32(10.0 ** float(F32(-F32(phred)) / F32(10)))
 
 
+UINT_MAX = 2 ** 32 - 1
+
+
+def parse_region(region: str) -> tuple[str, int, int] | None:
+    """``Bio::Region`` (bio.cpp:6-24): ``chrom:start-end``, the end may be
+    left out (open to the end of the chromosome), the start may not be 0 or
+    missing.  Returns (chrom, first, last) for the readers' ``region``, or
+    None for an empty string (no region)."""
+    import re
+    if not region:
+        return None
+    m = re.fullmatch(r"(\S+):(\d*)-(\d*)", region)
+    if not m:
+        raise ValueError(f"Could not parse region: [{region}]")
+    start = int(m.group(2)) if m.group(2) else 0
+    if start == 0:
+        raise ValueError("0 is not a valid genomic coordinate")
+    end = int(m.group(3)) if m.group(3) else UINT_MAX
+    return m.group(1), start, end
+
+
 def read_bin(path: str, keep: set[str] | None = None,
              region: tuple[str, int, int] | None = None, size_limit: int = 0) -> BinGLs:
     """Read a ``.bin`` file (glReader.cpp:64-82, 215-285).

@@ -105,16 +105,19 @@ def prepare(gl_het_alt: np.ndarray, positions: np.ndarray,
 
 def phase_bin(bin_path: str, vcf_path: str | None = None, map_path: str | None = None,
               opts: PhaseOptions | None = None, keep: set[str] | None = None,
-              command_line: str = "", region: tuple[str, int, int] | None = None,
+              command_line: str = "", region: str | tuple[str, int, int] | None = None,
               ref_legend: str | None = None, ref_hap: str | None = None):
     """Phase the samples of a GL file and (optionally) write the phased VCF:
     ``insti -g map -C.. -B.. -i.. -m.. [--region chr:a-b] [-h hap -l legend]
     file.bin`` (or ``-Fbcf file.vcf.gz``) on one GPU.  ``.vcf`` / ``.vcf.gz``
     files are read for their GL or PL field, anything else as ``.bin``;
-    ``region`` = (chrom, first, last) keeps the sites inside it; a reference
+    ``region`` ("chr:first-last" as ``--region`` takes it, or a (chrom,
+    first, last) tuple) keeps the sites inside it; a reference
     panel (legend + hap) becomes the haplotype rows after the 2N sample
     rows.  Returns (prob [S][2N], the parsed input)."""
     opts = opts or PhaseOptions()
+    if isinstance(region, str):
+        region = gio.parse_region(region)
     if bin_path.endswith((".vcf", ".vcf.gz")):
         data = gio.read_vcf_gls(bin_path, keep=keep, region=region)
     else:

@@ -108,6 +108,18 @@ def test_nrd_matched_pairs_samples_and_sites_by_name():
     assert nrd == pytest.approx(100 / 3)
 
 
+def test_parse_region():
+    """Bio::Region (bio.cpp:6-24) as --region / -R parse it."""
+    assert gio.parse_region("20:101363-") == ("20", 101363, 2 ** 32 - 1)
+    assert gio.parse_region("20:5335724-5861377") == ("20", 5335724, 5861377)
+    assert gio.parse_region("chrX:1-") == ("chrX", 1, 2 ** 32 - 1)
+    assert gio.parse_region("") is None
+    for bad, msg in (("20", "Could not parse"), ("20:a-b", "Could not parse"),
+                     ("20:-100", "0 is not a valid"), ("20:0-5", "0 is not a valid")):
+        with pytest.raises(ValueError, match=msg):
+            gio.parse_region(bad)
+
+
 def test_gl_conversions():
     """Bio::gl2prob / Bio::phred2prob (bio.hpp:154-170) and the GL trio the
     reference keeps (glReader.cpp:202-213)."""

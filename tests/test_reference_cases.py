@@ -224,7 +224,7 @@ def test_real_gls_nrd(oracle_lib):
     src = os.path.join(SAMPLES, "multi_gls")
     d = gio.read_bin(os.path.join(src, "chr20.5335724-5861377.1024_site_subset.HRC.r1.AC5."
                                        "TGPP3_samples.likelihoods.winniFilter.bin"),
-                     region=("20", 5335724, 5861377))
+                     region=gio.parse_region("20:5335724-5861377"))
     assert len(d.names) == 2495 and len(d.sites) == 1024
     gm = gio.read_genetic_map(os.path.join(SAMPLES, "geneticMap",
                                            "genetic_map_chr20_combined_b37.txt.gz"))
