@@ -277,3 +277,31 @@ def test_kick_start_first_proposal(oracle_lib):
     nbr = np.tile(np.array([3, 7, 9], np.uint32)[None, :], (N, 1))
     _, p1 = O.sample_surrogates(9, 3, N, 40, 0, 0, nbr=nbr, kick_first=True, H=H)
     assert p1[0].min() >= 2 * N and p1[0].max() < H
+
+
+def test_fp16_gl_storage_exceeds_the_loglik_bound(oracle_lib):
+    """Why GLs and emissions stay binary32: rounding either to FP16 before
+    the recursion moves the log-likelihood by more than the 1e-5 relative
+    bound (measured against the binary64 yardstick on synthetic data at
+    depth 2: emission in FP16 up to ~7e-5, GLs in FP16 up to ~4e-5)."""
+    O = oracle_lib
+    w = synth.Workload("fp16", N=64, S=1024, founders=20, depth=2.0, burnin=1, sampling=1,
+                       seed=3)
+    ds = synth.generate(w)
+    m, haps = synth.initial_state(ds, seed=2)
+    e16 = m.emit.astype(np.float16).astype(np.float32)
+    e_gl16 = mdl.emission(m.t.astype(np.float16).astype(np.float32), m.pc)
+    rng = np.random.default_rng(5)
+    worst_e = worst_gl = 0.0
+    for _ in range(100):
+        s = int(rng.integers(0, m.N))
+        q = rng.integers(0, haps.shape[0], 4).astype(np.uint32)
+        ref = O.hmm_like_f64(np.ascontiguousarray(m.emit[s]), m.tran, haps, q)
+        for emit, name in ((e16, "e"), (e_gl16, "gl")):
+            rel = abs(O.hmm_like_f64(np.ascontiguousarray(emit[s]), m.tran, haps, q) - ref)
+            rel /= abs(ref)
+            if name == "e":
+                worst_e = max(worst_e, rel)
+            else:
+                worst_gl = max(worst_gl, rel)
+    assert worst_e > 1e-5 and worst_gl > 1e-5, (worst_e, worst_gl)
