@@ -419,10 +419,17 @@ def read_legend(path: str, chrom: str) -> Sites:
     return sites
 
 
+def _atoi(token: str) -> int:
+    """C's atoi: optional sign and the leading digits; 0 without digits."""
+    import re
+    m = re.match(r"\s*([+-]?\d+)", token)
+    return int(m.group(1)) if m else 0
+
+
 def read_hap(path: str) -> np.ndarray:
     """Insti::OpenHap (insti.cpp:1080-1137): one row per site, one 0/1
-    column per haplotype, the same column count on every row.  Returns uint8
-    [sites][haplotypes]."""
+    column per haplotype, the same column count on every row; each column is
+    read as atoi reads it.  Returns uint8 [sites][haplotypes]."""
     rows = []
     width = None
     with _open_read(path) as fd:
@@ -432,7 +439,7 @@ def read_hap(path: str) -> np.ndarray:
                 width = len(tokens)
             if len(tokens) != width:
                 raise ValueError("Every row of hap file must have the same number of columns")
-            vals = [int(t) for t in tokens]
+            vals = [_atoi(t) for t in tokens]
             if any(v not in (0, 1) for v in vals):
                 raise ValueError(f"All alleles are not 0 or 1 In haplotypes file {path} at "
                                  f"line number {line_num} (0-based)")

@@ -149,6 +149,10 @@ def test_reference_panel_rules(tmp_path):
     leg, hap = _panel_files(tmp_path, rows, haps[:4] + ["0 2"])
     with pytest.raises(ValueError, match="not 0 or 1"):
         gio.load_reference_panel(leg, hap, sites)
+    # columns are read as atoi reads them
+    leg, hap = _panel_files(tmp_path, rows, ["1 1", "0.9 1x", "1 0", "1 1", "a +0"])
+    assert mdl.unpack_haplotypes(gio.load_reference_panel(leg, hap, sites), 3).tolist() == \
+        [[0, 1, 0], [1, 1, 0]]
     leg, hap = _panel_files(tmp_path, rows[:2] + [""] + rows[2:], haps)
     with pytest.raises(ValueError, match="empty lines"):
         gio.load_reference_panel(leg, hap, sites)
