@@ -9,6 +9,7 @@
 // across the boundary or resets the device (the reference's HMMLikeCUDA calls
 // exit(EXIT_FAILURE) on CUDA errors, src/hmmLike.cu:240-300, and
 // cudaDeviceReset in Cleanup, src/hmmLike.cu:396).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -239,18 +240,22 @@ int set_tran(glp_problem *pb, const float *tran, uint32_t S) {
   glp_ctx *c = pb->ctx;
   if (!tran || S == 0)
     return fail(c, GLP_ERR_ARG, "tran must be non-null with num_sites > 0");
-  std::vector<float4> t4(S);
-  t4[0] = make_float4(1.f, 0.f, 0.f, 1.f);  // row 0 is unused by the recursion
+  // rows 0 and S are the identity: row 0 is unused by the reference's
+  // recursion (the forward pass starts from it), row S ends the backward pass
+  std::vector<float4> t4(S + 1);
+  t4[0] = make_float4(1.f, 0.f, 0.f, 1.f);
   for (uint32_t m = 1; m < S; ++m)
     t4[m] = make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
                         tran[3 * m] - tran[3 * m + 2]);
+  t4[S] = make_float4(1.f, 0.f, 0.f, 1.f);
   if (pb->S != S) {
     release(pb->d_tran4);
     pb->S = 0;
-    GLP_CUDA(c, cudaMalloc((void **)&pb->d_tran4, sizeof(float4) * S));
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_tran4, sizeof(float4) * (S + 1)));
     pb->S = S;
   }
-  GLP_CUDA(c, cudaMemcpy(pb->d_tran4, t4.data(), sizeof(float4) * S, cudaMemcpyHostToDevice));
+  GLP_CUDA(c, cudaMemcpy(pb->d_tran4, t4.data(), sizeof(float4) * (S + 1),
+                         cudaMemcpyHostToDevice));
   return GLP_OK;
 }
 
@@ -307,21 +312,22 @@ int set_emission(glp_problem *pb, const float *emit, const float *prob, uint32_t
 using glp::MultiFn;
 using glp::SingleFn;
 
-// Speculation shape of a launch: P lanes per sample, V evaluations per lane.
+// Speculation shape of a launch: P lanes per sample (P/2 lane pairs, one
+// evaluation each per round).
 struct Shape {
-  uint32_t P = 1, V = 1;
+  uint32_t P = 2;
   uint32_t sub = 1;  // normalisations per 8-site block (2: every 4 sites)
 };
 
 SingleFn single_kernel(Shape sh, bool vq) {
   if (sh.sub == 2)
     return vq ? glp::single_kernel_vq_sub4(sh.P) : glp::single_kernel_f32_sub4(sh.P);
-  return vq ? glp::single_kernel_vq(sh.P, sh.V) : glp::single_kernel_f32(sh.P, sh.V);
+  return vq ? glp::single_kernel_vq(sh.P) : glp::single_kernel_f32(sh.P);
 }
 MultiFn multi_kernel(Shape sh, bool vq) {
   if (sh.sub == 2)
     return vq ? glp::multi_kernel_vq_sub4(sh.P) : glp::multi_kernel_f32_sub4(sh.P);
-  return vq ? glp::multi_kernel_vq(sh.P, sh.V) : glp::multi_kernel_f32(sh.P, sh.V);
+  return vq ? glp::multi_kernel_vq(sh.P) : glp::multi_kernel_f32(sh.P);
 }
 
 // hmm_work of a generation: the recursions (blocks of two warps over 32
@@ -354,7 +360,7 @@ void launch_work(const glp::MultiParams &mp, uint64_t samples, cudaStream_t st) 
 // SM), or 0 when the occupancy query fails.
 template <class Fn>
 double resident_threads(Fn fn, uint32_t P, int sms) {
-  const size_t smem = glp::stage_bytes((int)P, 1);
+  const size_t smem = glp::stage_bytes((int)P);
   int occ = 0;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess ||
@@ -364,39 +370,40 @@ double resident_threads(Fn fn, uint32_t P, int sms) {
   return (double)occ * glp::kThreads * sms;
 }
 
-// Speculation width for N samples at acceptance rate a.  A round of P
-// evaluations keeps (1 - (1-a)^P) / (a P) of them useful.  A lane-round costs
-// kLaneRoundCost[P] relative to P = 8 when the GPU is full (measured on
-// GB300 at 4,096 sites: narrow groups stage more rows per lane, and below
-// 4 lanes the staging rings cap the resident blocks).  The kernels are
-// issue-bound, so lane-rounds run at a rate that saturates with the share u
-// = min(N P, threads resident with P lanes) / the most resident for any P:
-// rate(u) = u (1 + h) / (u + h), h = 0.08 (measured: 0.93 of the full rate at
-// half the warps, 0.87 between u = 0.21 and 0.41 on 2,000 samples x 8,192
-// sites).  The score is useful fraction x rate / cost.
-constexpr double kLaneRoundCost[6] = {6.4, 2.44, 1.34, 1.0, 0.955, 0.953};
+// Speculation width for N samples at acceptance rate a.  A group of P lanes
+// scores n = P/2 positions of the chain a round (one per lane pair), of which
+// (1 - (1-a)^n) / (a n) are useful.  A lane-round costs kLaneRoundCost[P]
+// relative to P = 8 when the GPU is full (narrow groups stage more rows per
+// lane, and at 2 lanes the staging rings cap the resident blocks).  The
+// kernels are issue-bound, so lane-rounds run at a rate that saturates with
+// the share u = min(N P, threads resident with P lanes) / the most resident
+// for any P: rate(u) = u (1 + h) / (u + h), h = 0.08 (0.93 of the full rate
+// at half the warps).  The score is useful fraction x rate / cost.
+constexpr double kLaneRoundCost[6] = {0.0, 2.44, 1.34, 1.0, 0.955, 0.953};
 
 template <class FnOf>
 uint32_t pick_lanes(double a, uint64_t N, int sms, FnOf kernel_for, double *cache = nullptr,
                     bool *known = nullptr) {
-  double local[6];
+  double local[6] = {};
   double *res = cache ? cache : local;
   if (!known || !*known) {
-    for (int i = 0; i < 6; ++i)
+    res[0] = 0.0;
+    for (int i = 1; i < 6; ++i)
       res[i] = resident_threads(kernel_for(1u << i), 1u << i, sms);
     if (known)
       *known = true;
   }
   double most = 0;
-  for (int i = 0; i < 6; ++i)
+  for (int i = 1; i < 6; ++i)
     most = std::max(most, res[i]);
   if (most <= 0)
     return 8;
-  uint32_t best = 1;
+  uint32_t best = 2;
   double best_score = 0;
-  for (int i = 0; i < 6; ++i) {
+  for (int i = 1; i < 6; ++i) {
     const uint32_t P = 1u << i;
-    const double eff = (1.0 - std::pow(1.0 - a, (double)P)) / (a * P);
+    const double n = P / 2;
+    const double eff = (1.0 - std::pow(1.0 - a, n)) / (a * n);
     const double u = std::min((double)N * P, res[i]) / most;
     constexpr double h = 0.08;
     const double rate = u * (1.0 + h) / (u + h);
@@ -425,17 +432,14 @@ uint32_t choose_lanes(glp_ctx *c, uint64_t N, bool multi, bool vq, float pen) {
       c->resident[multi][vq], &c->resident_known[multi][vq]);
 }
 
-// Lanes from choose_lanes; two evaluations per lane only on request
-// (glp_set_evals_per_lane), and only where that kernel exists (P = 2, 4, 8).
+// Lanes from choose_lanes (a request below two lanes gets two: one
+// evaluation a round), normalisation block from the context's rule.
 Shape choose_shape(glp_ctx *c, uint64_t N, bool multi, bool vq, float pen) {
   Shape sh;
-  sh.P = choose_lanes(c, N, multi, vq, pen);
+  sh.P = std::max<uint32_t>(2u, choose_lanes(c, N, multi, vq, pen));
   c->launch_pen = pen;
-  sh.V = (c->evals == 2 && (sh.P == 2 || sh.P == 4 || sh.P == 8)) ? 2u : 1u;
-  if (c->block_sites == 4 || (c->block_sites == 0 && c->short_blocks)) {
+  if (c->block_sites == 4 || (c->block_sites == 0 && c->short_blocks))
     sh.sub = 2;
-    sh.V = 1;
-  }
   return sh;
 }
 
@@ -539,8 +543,8 @@ int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
 }
 
 template <class Fn>
-unsigned grid_for(glp_ctx *c, Fn fn, uint64_t samples, uint32_t P, uint32_t V, int *rc) {
-  const size_t smem = glp::stage_bytes((int)P, (int)V);
+unsigned grid_for(glp_ctx *c, Fn fn, uint64_t samples, uint32_t P, int *rc) {
+  const size_t smem = glp::stage_bytes((int)P);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
   if (e == cudaSuccess)
@@ -566,14 +570,14 @@ int launch_single(glp_ctx *c, glp_problem *pb, const glp_generation_args *a) {
   const Shape sh = choose_shape(c, a->num_samples, false, vq, a->pen);
   const uint32_t P = sh.P;
   SingleFn fn = single_kernel(sh, vq);
-  const unsigned grid = grid_for(c, fn, a->num_samples, P, sh.V, &rc);
+  const unsigned grid = grid_for(c, fn, a->num_samples, P, &rc);
   if (rc)
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), c->stream));
   cudaEvent_t *ev = c->ev[c->ev_count++ % glp_ctx::kTimed];
   GLP_CUDA(c, cudaEventRecord(ev[0], c->stream));
-  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(p);
+  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P), c->stream>>>(p);
   GLP_CUDA(c, cudaGetLastError());
   GLP_CUDA(c, cudaEventRecord(ev[1], c->stream));
   if (p.do_work) {
@@ -860,14 +864,14 @@ int glp_run_batch(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   const Shape sh = choose_shape(c, total, true, vq, c->h_table[0].pen);
   const uint32_t P = sh.P;
   MultiFn fn = multi_kernel(sh, vq);
-  const unsigned grid = grid_for(c, fn, total, P, sh.V, &rc);
+  const unsigned grid = grid_for(c, fn, total, P, &rc);
   if (rc)
     return rc;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), c->stream));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), c->stream));
   cudaEvent_t *ev = c->ev[c->ev_count++ % glp_ctx::kTimed];
   GLP_CUDA(c, cudaEventRecord(ev[0], c->stream));
-  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P, (int)sh.V), c->stream>>>(mp);
+  fn<<<grid, glp::kThreads, glp::stage_bytes((int)P), c->stream>>>(mp);
   GLP_CUDA(c, cudaGetLastError());
   GLP_CUDA(c, cudaEventRecord(ev[1], c->stream));
   launch_work(mp, total, c->stream);
@@ -884,7 +888,7 @@ struct glp_batch {
   glp_ctx *c = nullptr;
   uint32_t count = 0;
   uint64_t total = 0, chain_cycles = 0;
-  uint32_t P = 4, V = 1;
+  uint32_t P = 8;
   unsigned grid = 1;
   glp::GenParams *d_table = nullptr;
   uint32_t *d_offsets = nullptr;
@@ -900,7 +904,7 @@ int batch_enqueue(glp_batch *b, cudaStream_t st) {
   glp_ctx *c = b->c;
   GLP_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(uint32_t), st));
   GLP_CUDA(c, cudaMemsetAsync(c->d_stats, 0, glp::kStats * sizeof(unsigned long long), st));
-  b->fn<<<b->grid, glp::kThreads, glp::stage_bytes((int)b->P, (int)b->V), st>>>(b->mp);
+  b->fn<<<b->grid, glp::kThreads, glp::stage_bytes((int)b->P), st>>>(b->mp);
   GLP_CUDA(c, cudaGetLastError());
   launch_work(b->mp, b->total, st);
   GLP_CUDA(c, cudaGetLastError());
@@ -987,9 +991,8 @@ int glp_batch_prepare(glp_ctx *c, uint32_t count, glp_problem *const *problems,
   b->mp.error = c->d_error;
   const Shape sh = choose_shape(c, total, true, vq, table[0].pen);
   b->P = sh.P;
-  b->V = sh.V;
   b->fn = multi_kernel(sh, vq);
-  b->grid = grid_for(c, b->fn, total, b->P, b->V, &rc);
+  b->grid = grid_for(c, b->fn, total, b->P, &rc);
   if (rc)
     return bail(rc);
   if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
@@ -1207,8 +1210,8 @@ int glp_set_lanes_per_sample(glp_ctx *c, uint32_t lanes) {
 int glp_set_evals_per_lane(glp_ctx *c, uint32_t evals) {
   if (!c)
     return GLP_ERR_ARG;
-  if (evals > 2)
-    return fail(c, GLP_ERR_ARG, "evaluations per lane must be 0, 1 or 2");
+  if (evals > 1)
+    return fail(c, GLP_ERR_ARG, "each lane pair scores one evaluation a round: evals must be 0 or 1");
   c->evals = evals;
   return GLP_OK;
 }
@@ -1618,30 +1621,117 @@ extern "C" int glp_measure_fp32_peak(glp_ctx *c, float ms_target, double *tflops
 //   [0, 4)     work-queue counter          (cleared by every call)
 //   [8, 56)    generation counters, 6 x uint64 (cleared by every call)
 //   [64, 68)   device error flag           (cleared by every call)
-//   [256, 256 + round_up(16 S, 256))        transition table, float4 [S]
+//   [256, 256 + round_up(16 (S + 1), 256))  transition table, float4 [S + 1]
 //   then       hmm_work rows, float4 [N][S] (written before they are read)
 // Host code never dereferences g_noalloc_scratch: its name there is a host
-// stand-in, so the device address is looked up with cudaGetSymbolAddress once
-// per device (with that device current) and passed to the kernels.
+// stand-in.  The array's device address belongs to a CUDA context, so it is
+// looked up with cudaGetSymbolAddress once per context, with that context
+// current (for the usual primary context: once per device), and cached under
+// the context's unique id (cuCtxGetId), together with the launch set-up of
+// the kernels (shared-memory attributes, resident threads per lane width).
+// A context created later -- after cudaDeviceReset, or one a caller made with
+// the driver API -- has another id and gets its own lookup.
 
 namespace {
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[GLP_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kNoallocMaxDevices = 64;
+// Set-up of one CUDA context: the scratch array's device address there and
+// the generation kernel's resident threads per lane width 1 .. 32.
+struct NoallocSetup {
+  unsigned long long ctx_id = 0;  // 0: slot unused
+  unsigned char *base = nullptr;
+  int sms = 0;
+  double resident[6] = {};
+};
+constexpr int kNoallocContexts = 16;
 std::mutex g_noalloc_mutex;
-void *g_noalloc_addr[kNoallocMaxDevices];
+NoallocSetup g_noalloc_setup[kNoallocContexts];
+unsigned g_noalloc_next = 0;
+
+// Driver entry points (through the runtime, so the library needs no link to
+// libcuda): the current context and its process-unique id.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+bool g_ctx_fns_loaded = false;
+
+// Id of the calling thread's current context (0 if there is none or the
+// driver cannot tell); call with g_noalloc_mutex held.
+unsigned long long current_ctx_id() {
+  if (!g_ctx_fns_loaded) {
+    g_ctx_fns_loaded = true;
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault,
+                                         &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) ==
+            cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+      g_ctx_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!g_ctx_current || g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx ||
+      g_ctx_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// The set-up of the caller's current context, made on first use; a copy is
+// returned so no lock is held while the call launches.
+int noalloc_setup(NoallocSetup *out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  unsigned long long id = current_ctx_id();
+  if (id) {
+    for (const NoallocSetup &e : g_noalloc_setup)
+      if (e.ctx_id == id) {
+        *out = e;
+        return GLP_OK;
+      }
+  }
+  NoallocSetup e;
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+    return GLP_ERR_CUDA;
+  e.base = static_cast<unsigned char *>(p);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&e.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      allow_chain_smem() != cudaSuccess)
+    return GLP_ERR_CUDA;
+  for (int i = 1; i < 6; ++i) {  // also sets each kernel's shared-memory attribute
+    Shape sh;
+    sh.P = 1u << i;
+    e.resident[i] = resident_threads(single_kernel(sh, false), sh.P, e.sms);
+    if (e.resident[i] <= 0)
+      return GLP_ERR_CUDA;
+  }
+  // the lookup above made a context current if there was none
+  e.ctx_id = id ? id : current_ctx_id();
+  if (e.ctx_id) {
+    g_noalloc_setup[g_noalloc_next] = e;
+    g_noalloc_next = (g_noalloc_next + 1) % kNoallocContexts;
+  }
+  *out = e;
+  return GLP_OK;
+}
 
 // Kernel layout of the reference's tran [S][3] (row 0 unused,
-// hmmLike.cu:325): row 0 becomes the identity so that the first forward step
-// reproduces l = e / 4; the fourth component is t0 - t2.
+// hmmLike.cu:325): S + 1 rows, rows 0 and S the identity (the forward pass
+// starts from row 0 so that the first step reproduces l = e / 4; the backward
+// pass starts from row S); the fourth component is t0 - t2.
 __global__ void tran4_kernel(const float *__restrict__ tran, uint32_t S,
                              float4 *__restrict__ out) {
   const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m < S)
-    out[m] = m ? make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
-                             __fsub_rn(tran[3 * m], tran[3 * m + 2]))
-               : make_float4(1.f, 0.f, 0.f, 1.f);
+  if (m <= S)
+    out[m] = (m && m < S) ? make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
+                                        __fsub_rn(tran[3 * m], tran[3 * m + 2]))
+                          : make_float4(1.f, 0.f, 0.f, 1.f);
 }
 
 size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -1675,30 +1765,21 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
     return GLP_ERR_ARG;
   if (a->neighbors && a->neighbors_per_sample == 0)
     return GLP_ERR_ARG;
-  const size_t tran_off = 256, beta_off = tran_off + round256((size_t)16 * S);
+  const bool draws = !a->hap_idxs_in || (C && !a->props);
+  const bool kick_first = (a->flags & GLP_GEN_KICK_FIRST) != 0;
+  if (kick_first && draws && C && H < 2 * N + 1)  // as make_params
+    return GLP_ERR_ARG;
+  const size_t tran_off = 256, beta_off = tran_off + round256((size_t)16 * (S + 1));
   const size_t need = beta_off + (work ? (size_t)16 * N * S : 0);
   if (need > GLP_NOALLOC_SCRATCH_BYTES)
     return GLP_ERR_TOO_LARGE;
 
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess)
-    return GLP_ERR_CUDA;
-  if (dev < 0 || dev >= kNoallocMaxDevices)
-    return GLP_ERR_DEVICE;
-  unsigned char *base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[dev]) {
-      void *p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
-        return GLP_ERR_CUDA;
-      g_noalloc_addr[dev] = p;
-    }
-    base = static_cast<unsigned char *>(g_noalloc_addr[dev]);
-  }
-  int sms = 0;
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return GLP_ERR_CUDA;
+  NoallocSetup su;
+  const int src = noalloc_setup(&su);
+  if (src)
+    return src;
+  unsigned char *const base = su.base;
+  const int sms = su.sms;
   cudaStream_t st = (cudaStream_t)stream;
 
   glp::GenParams p;
@@ -1731,7 +1812,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   p.klen = a->neighbors_per_sample;
   p.samp_lo = lo;
   p.samp_hi = hi;
-  p.kick_first = ((a->flags & GLP_GEN_KICK_FIRST) && H > 2 * N) ? 1u : 0u;
+  p.kick_first = kick_first ? 1u : 0u;
   std::memcpy(p.pc, pc16, sizeof(p.pc));
   p.pen = a->pen;
   p.seed = a->seed;
@@ -1739,31 +1820,31 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   p.do_work = work ? 1u : 0u;
 
   // speculation width for an acceptance rate of about 0.12 (the rule of
-  // choose_lanes without a context's history)
-  const uint32_t P = pick_lanes(0.12, N, sms, [](uint32_t w) {
-    Shape s1;
-    s1.P = w;
-    return (const void *)single_kernel(s1, false);
-  });
+  // choose_lanes without a context's history), from the resident threads
+  // measured at set-up
+  bool known = true;
+  const uint32_t P = pick_lanes(
+      0.12, N, sms,
+      [](uint32_t w) {
+        Shape s1;
+        s1.P = w;
+        return (const void *)single_kernel(s1, false);
+      },
+      su.resident, &known);
   Shape sh;
   sh.P = P;
   SingleFn fn = single_kernel(sh, false);
-  int occ = 0;
-  const size_t smem = glp::stage_bytes((int)P, 1);
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, glp::kThreads, smem) !=
-          cudaSuccess ||
-      (work && allow_chain_smem() != cudaSuccess))
-    return GLP_ERR_CUDA;
+  const size_t smem = glp::stage_bytes((int)P);
+  const uint64_t resident_blocks =
+      (uint64_t)(su.resident[__builtin_ctz(P)] / glp::kThreads + 0.5);
   const uint64_t groups = (uint64_t)glp::kThreads / P;
   const uint64_t want = ((uint64_t)N + groups - 1) / groups;
-  const unsigned grid =
-      (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)std::max(occ, 1) * sms));
+  const unsigned grid = (unsigned)std::max<uint64_t>(
+      1, std::min<uint64_t>(want, std::max<uint64_t>(resident_blocks, (uint64_t)sms)));
 
   if (cudaMemsetAsync(base, 0, 256, st) != cudaSuccess)
     return GLP_ERR_CUDA;
-  tran4_kernel<<<(S + 255) / 256, 256, 0, st>>>(tran, S, (float4 *)(base + tran_off));
+  tran4_kernel<<<(S + 256) / 256, 256, 0, st>>>(tran, S, (float4 *)(base + tran_off));
   fn<<<grid, glp::kThreads, smem, st>>>(p);
   if (work)
     launch_work(p, N, st);

@@ -170,14 +170,16 @@ int glp_run_generation_host(glp_ctx *ctx, const glp_generation_args *args);
 /* Wait for the context stream and report device-side errors. */
 int glp_finish(glp_ctx *ctx);
 
-/* Lanes that score one sample's chain speculatively: 1, 2, 4, 8, 16 or 32
- * (0 = choose from the last generation's acceptance rate). */
+/* Lanes that score one sample's chain speculatively: 2, 4, 8, 16 or 32, as
+ * lane pairs that each score one chain position a round (one lane the
+ * forward half of the sites, the other the backward half); 1 is taken as 2
+ * (one position a round: the sequential chain); 0 = choose from the last
+ * generation's acceptance rate. */
 int glp_set_lanes_per_sample(glp_ctx *ctx, uint32_t lanes);
 
-/* Evaluations each lane scores per speculative round: 1, or 2 with 2, 4 or 8
- * lanes per sample (a round then covers 2P chain positions with the same
- * accept decisions); 0 = 1.  No reference counterpart (a tuning knob of the
- * speculative scheme). */
+/* Evaluations each lane pair scores per speculative round: 1 (or 0, the
+ * same); other values are refused with GLP_ERR_ARG.  No reference
+ * counterpart (a tuning knob of the speculative scheme). */
 int glp_set_evals_per_lane(glp_ctx *ctx, uint32_t evals);
 
 /* Sites per normalisation block of the likelihood (no counterpart in the
@@ -383,7 +385,7 @@ int glp_result(glp_ctx *ctx, const uint32_t *hsum, uint32_t num_samples, uint32_
  * kernel layout and the hmm_work rows -- in one fixed array of
  * GLP_NOALLOC_SCRATCH_BYTES (32 MiB) of device memory that every GPU loading
  * this library holds until the process exits.  It needs
- * 256 + 16*ceil(S/16)*16 + 16*N*S bytes of it and returns GLP_ERR_TOO_LARGE
+ * 256 + 16*ceil((S+1)/16)*16 + 16*N*S bytes of it and returns GLP_ERR_TOO_LARGE
  * beyond that (about N*S <= 2.0e6 site-samples).
  *
  * All array arguments are DEVICE pointers except pc16 (host, row-major
@@ -393,10 +395,18 @@ int glp_result(glp_ctx *ctx, const uint32_t *hsum, uint32_t num_samples, uint32_
  * when it has finished, reporting GLP_ERR_INDEX for an out-of-range
  * haplotype index.
  *
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  Calls share the one array: calls that overlap on the GPU (other
- * host threads, other streams) race and must be serialized by the caller. */
+ * The array's device address belongs to a CUDA context.  The first call in
+ * each context -- with the usual primary context, the first call on each
+ * device -- looks it up (cudaGetSymbolAddress, with that context current) and
+ * sets the kernels' launch attributes; later calls in the same context reuse
+ * that set-up.  Any context is supported: the set-up is kept per context id,
+ * so a context made after cudaDeviceReset or with the driver API gets its
+ * own.  Make the first call in a context before any stream capture begins.
+ * Every call copies the device error flag back and synchronizes `stream`
+ * before it returns.  Calls share the one array, which keeps what the last
+ * call left there (each call clears the counters and flag it reads): calls
+ * that overlap on the GPU (other host threads, other streams) race and must
+ * be serialized by the caller. */
 #define GLP_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
 int glp_run_generation_noalloc(const glp_generation_args *args, const float *tran,
                                const float *pc16, const float *emit, const float *prob,
