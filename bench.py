@@ -44,7 +44,6 @@ def parse():
     ap.add_argument("--sites", type=int, default=0, help="override S (tests)")
     ap.add_argument("--cycles", type=int, default=100)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per sample (0 = auto)")
-    ap.add_argument("--evals", type=int, default=0, help="evaluations per lane (0 = auto)")
     ap.add_argument("--block-sites", type=int, default=0,
                     help="sites per normalisation block (8, 4; 0 = auto)")
     ap.add_argument("--vq", action="store_true", help="score with 4-bit VQ GL codes")
@@ -304,7 +303,7 @@ def run_ours(args):
         gp = GLPack(m.t, np.random.default_rng(1))
         packed, codebook = gp.packed_gls(), gp.code_book()
     eng = Engine(m.emit, m.t, m.tran, m.pc, haps, C, device=local, lanes=args.lanes,
-                 packed=packed, codebook=codebook, evals=args.evals,
+                 packed=packed, codebook=codebook,
                  block_sites=args.block_sites)
     dev = torch.device("cuda", local)
     torch.cuda.synchronize()
@@ -394,15 +393,15 @@ def run_ours(args):
                 "samples": N, "sites": S, "cycles": C, "haplotypes": H,
                 "emission": "vq4" if args.vq else "f32",
                 "lanes_per_sample": lanes,
-                "evals_per_lane": 2 if args.evals == 2 and lanes in (2, 4, 8) else 1,
+                "positions_per_round": lanes // 2,
                 "evaluations_per_step": ev,
                 "speculative_rounds": rounds,
                 "site_by_site_redos": cnt[3],
                 "block_sites": eng.dev.block_sites(),
                 "lane_occupancy": round(cnt[5] / max(32 * cnt[4], 1), 4),
-                # lane-rounds run per counted evaluation: above 1 by the lanes
-                # of a chain's last round that score past its end
-                "lane_rounds_per_evaluation": round(cnt[5] / max(cnt[0], 1), 4),
+                # lane-pair rounds run per counted evaluation: above 1 by the
+                # pairs of a chain's last round that score past its end
+                "pair_rounds_per_evaluation": round(cnt[5] / 2 / max(cnt[0], 1), 4),
                 "useful_fraction": round(N * (C + 1) / max(ev, 1), 4),
                 "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6),
                 "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
@@ -554,7 +553,7 @@ def run_uneven(args):
                    "accept_rate": round(cnt_b[2] / max(cnt_b[1], 1), 4),
                    "useful_fraction": round(sum(N for N, _ in shapes) * (C + 1)
                                             / max(cnt_b[0], 1), 4),
-                   "lane_rounds_per_evaluation": round(cnt_b[5] / max(cnt_b[0], 1), 4),
+                   "pair_rounds_per_evaluation": round(cnt_b[5] / 2 / max(cnt_b[0], 1), 4),
                    "plain_value": v_p, "plain_ms_per_step": t_plain / args.steps * 1e3,
                    "batched_over_plain": v_b / v_p,
                    "form": "batched = one persistent launch per generation replayed from a "

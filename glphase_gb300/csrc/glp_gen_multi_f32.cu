@@ -2,5 +2,5 @@
 #include "glp_launch.h"
 
 namespace glp {
-GLP_GEN_TABLE(multi_kernel_f32, MultiFn, generation_multi_kernel, EmitF32)
+GLP_GEN_TABLE(multi_kernel_f32, MultiFn, generation_multi_kernel, EmitF32, 1)
 }  // namespace glp

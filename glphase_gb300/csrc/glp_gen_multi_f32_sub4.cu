@@ -3,5 +3,5 @@
 #include "glp_launch.h"
 
 namespace glp {
-GLP_GEN_TABLE_SUB4(multi_kernel_f32_sub4, MultiFn, generation_multi_kernel, EmitF32)
+GLP_GEN_TABLE(multi_kernel_f32_sub4, MultiFn, generation_multi_kernel, EmitF32, 2)
 }  // namespace glp

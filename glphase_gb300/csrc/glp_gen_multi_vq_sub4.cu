@@ -3,5 +3,5 @@
 #include "glp_launch.h"
 
 namespace glp {
-GLP_GEN_TABLE_SUB4(multi_kernel_vq_sub4, MultiFn, generation_multi_kernel, EmitVQ)
+GLP_GEN_TABLE(multi_kernel_vq_sub4, MultiFn, generation_multi_kernel, EmitVQ, 2)
 }  // namespace glp

@@ -3,5 +3,5 @@
 #include "glp_launch.h"
 
 namespace glp {
-GLP_GEN_TABLE_SUB4(single_kernel_f32_sub4, SingleFn, generation_kernel, EmitF32)
+GLP_GEN_TABLE(single_kernel_f32_sub4, SingleFn, generation_kernel, EmitF32, 2)
 }  // namespace glp

@@ -3,5 +3,5 @@
 #include "glp_launch.h"
 
 namespace glp {
-GLP_GEN_TABLE_SUB4(single_kernel_vq_sub4, SingleFn, generation_kernel, EmitVQ)
+GLP_GEN_TABLE(single_kernel_vq_sub4, SingleFn, generation_kernel, EmitVQ, 2)
 }  // namespace glp

@@ -13,17 +13,18 @@
 //
 // Work decomposition (one warp = 32/P groups of P lanes, one sample per group):
 //  * A sample's MH chain is inherently sequential, so its parallelism comes
-//    from speculation: the P lanes of a group evaluate the next P evaluations
-//    of the chain (the current quadruple and the next P-1 proposals), each
-//    built on the current state, i.e. assuming all earlier ones are rejected.
-//    The group then replays the accept rule in order; evaluations after the
-//    first accepted proposal are discarded and re-evaluated from the new
-//    state.  Decisions are exactly those of the sequential chain.
-//  * Each lane computes one likelihood as a forward pass over the first half
-//    of the words and a backward pass over the second half, interleaved in
-//    one instruction stream (8 independent FMA chains), joined by a 4-term
-//    dot product: L = alpha_{h-1} . beta_{h-1}.  Same flop count as the
-//    plain forward pass, half the latency.
+//    from speculation: the P/2 lane pairs of a group evaluate the next P/2
+//    evaluations of the chain (the current quadruple and the next proposals),
+//    each built on the current state, i.e. assuming all earlier ones are
+//    rejected.  The group then replays the accept rule in order; evaluations
+//    after the first accepted proposal are discarded and re-evaluated from the
+//    new state.  Decisions are exactly those of the sequential chain.
+//  * A pair computes one likelihood: its even lane a forward pass over the
+//    lower half of the sites, its odd lane a backward pass over the upper
+//    half, both in one code path (x <- D T x), joined by a 4-term dot product
+//    L = alpha_h . beta_h.  Half the sites per lane means half as many
+//    speculative positions per round for the same lanes per sample, so fewer
+//    of them are discarded.
 //  * Scaling is by exact powers of two with an integer exponent per half;
 //    the log-likelihood is assembled in binary64 (log(dot) + k*ln2).
 //  * hmm_work runs one sample per thread in a second kernel over the final
@@ -34,7 +35,7 @@
 //   haps/hnew  uint64 [H][wn] hap-major   (parent words: L2-resident gathers)
 //   emit       float4 [N][S]              (streamed, shared by a group)
 //   packed     uint32 [ceil(S/8)][N]      (VQ codes; 16-entry table in smem)
-//   tran4      float4 [S]                 (t0, t1, t2, 0); tran4[0] = (1,0,0,0)
+//   tran4      float4 [S + 1]             (t0, t1, t2, t0 - t2); rows 0 and S = identity
 //   beta       float4 [N][S]              (hmm_work scratch)
 #pragma once
 
@@ -131,20 +132,29 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // Staging of 8-site blocks: one slot = 8 transition rows followed by the 8
-// sites' emission data (8 float4, or the block's VQ word in the first 4 bytes).
+// sites' emission data (8 float4, or the block's VQ word in the first 4
+// bytes).  A forward slot holds sites m0 .. m0+7 in order with the rows
+// T_m0 .. T_m0+7 the forward recursion applies there; a backward slot holds
+// sites n0+7 .. n0 (row j is site n0 + 7 - j) with the rows T_{n0+8-j} the
+// backward recursion applies there, so both directions read slot row j at
+// step j of a block.
 constexpr int kSlotF4 = 16;
-constexpr int kRing = 3;                   // slots per stream: two blocks in flight
-constexpr int kGroupF4 = 2 * kRing * kSlotF4;  // forward + backward rings
-// Rings of neighbouring groups are kGroupF4 + 1 float4 apart, so the 16-byte
-// reads of the 8 groups of a warp start 4 banks apart and never conflict.
-constexpr int kGroupStrideF4 = kGroupF4 + 1;
+constexpr int kRing = 3;  // slots per direction: two blocks in flight
+// A group's ring: forward slots at [0, 48) and backward slots at [52, 100)
+// float4, so the forward and the backward row a group reads at one step are 4
+// float4 (16 banks) apart; rings of neighbouring groups are 105 float4 apart
+// (1 mod 8), so the 16-byte reads of the four 8-lane groups of a warp -- two
+// rows a group -- fall in eight distinct bank quads.
+constexpr int kBwdOffF4 = kRing * kSlotF4 + 4;
+constexpr int kGroupF4 = kBwdOffF4 + kRing * kSlotF4;
+constexpr int kGroupStrideF4 = kGroupF4 + 5;
 
 // The rows of an 8-row block that lane li of a P-lane group copies: nr rows
 // from rb.  From P = 8 up lanes 0..7 take one row each; narrower groups take
 // 8/P consecutive rows per lane, so that one copy instruction of the warp
-// writes rows 8/P apart in each group: with the groups' rings 4 banks apart,
-// the 16-byte writes of the two, four or eight groups in a quarter warp then
-// fall in disjoint banks (consecutive rows per instruction would overlap).
+// writes rows 8/P apart in each group: with the groups' rings 1 mod 8 float4
+// apart, the 16-byte writes of the groups in a quarter warp then fall in
+// disjoint banks (consecutive rows per instruction would overlap).
 struct StageRows {
   uint32_t rb, nr;
 };
@@ -161,9 +171,10 @@ __device__ __forceinline__ StageRows stage_rows(uint32_t li, uint32_t P) {
   return r;
 }
 
-// Copies 8 consecutive float4 from src into dst: this lane's rows of the
-// block (kMaxRows = 8/P bounds nr for the group size P the kernel starts with;
-// a group only widens later).
+// Copies 8 consecutive float4 from src into dst (stage8) or into dst in
+// reverse order, dst[7 - i] = src[i] (stage8_rev): this lane's rows of the
+// block (kMaxRows = 8/P bounds nr for the group size P the kernel starts
+// with; a group only widens later).
 template <int kMaxRows>
 __device__ __forceinline__ void stage8(float4 *dst, const float4 *src, StageRows r) {
 #pragma unroll
@@ -171,34 +182,47 @@ __device__ __forceinline__ void stage8(float4 *dst, const float4 *src, StageRows
     if (k < r.nr)
       cp_async16(dst + r.rb + k, src + r.rb + k);
 }
+template <int kMaxRows>
+__device__ __forceinline__ void stage8_rev(float4 *dst, const float4 *src, StageRows r) {
+#pragma unroll
+  for (uint32_t k = 0; k < (uint32_t)kMaxRows; ++k)
+    if (k < r.nr)
+      cp_async16(dst + 7 - (r.rb + k), src + r.rb + k);
+}
 
-// Sites are consumed in blocks of 8 (m0 a multiple of 8): stage(dst, m0, ..)
-// copies a block's emission data into a staging slot and staged(src, j)
-// returns site m0 + j from it; get1(m) reads one site directly (ragged tails
-// and single-word chunks).
+// Emission sources.  stage / stage_rev copy one block's emission data into
+// a forward / backward slot; block(src, rev) prepares a staged block and
+// at(b, j) returns the emission of the slot's row j; get1(m) reads site m
+// directly (the sites above the last full block, and the site-by-site pass).
 struct EmitF32 {
   const float4 *row;
+  using Blk = const float4 *;
   __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *) {
     row = p.emit + (size_t)s * p.S;
   }
   __device__ __forceinline__ float4 get1(uint32_t m) const { return __ldg(row + m); }
-  // copy this lane's rows of the emission of sites m0..m0+7 into dst
   template <int kMaxRows>
   __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, StageRows r) const {
     stage8<kMaxRows>(dst, row + m0, r);
   }
-  __device__ __forceinline__ float4 staged(const float4 *src, uint32_t j) const {
-    return src[j];
+  template <int kMaxRows>
+  __device__ __forceinline__ void stage_rev(float4 *dst, uint32_t n0, StageRows r) const {
+    stage8_rev<kMaxRows>(dst, row + n0, r);
   }
+  __device__ __forceinline__ Blk block(const float4 *src, bool) const { return src; }
+  __device__ __forceinline__ float4 at(Blk b, uint32_t j) const { return b[j]; }
 };
 
 // 4-bit VQ codes, eight per uint32, most significant nibble first
 // (glPack.cpp:104-109, hmmLike.cu:20-24), so one block of 8 sites is one
-// word; table[c] = FillEmit(decode(c)) computed once on the host.
+// word; table[c] = FillEmit(decode(c)) computed once on the host.  A backward
+// slot holds the same word; block() reverses its nibbles so that code j is
+// the site of row j.
 struct EmitVQ {
   const uint32_t *col;
   const float4 *table;
   uint32_t stride;
+  using Blk = uint32_t;
   __device__ __forceinline__ void init(const GenParams &p, uint32_t s, const float4 *tab) {
     col = p.packed + s;
     stride = p.N;
@@ -213,21 +237,33 @@ struct EmitVQ {
     if (r.rb == 0 && r.nr != 0)  // lane 0 of the group
       cp_async4(dst, col + (size_t)(m0 >> 3) * stride);
   }
-  __device__ __forceinline__ float4 staged(const float4 *src, uint32_t j) const {
+  template <int kMaxRows>
+  __device__ __forceinline__ void stage_rev(float4 *dst, uint32_t n0, StageRows r) const {
+    stage<kMaxRows>(dst, n0, r);
+  }
+  __device__ __forceinline__ Blk block(const float4 *src, bool rev) const {
     const uint32_t w = *reinterpret_cast<const uint32_t *>(src);
+    const uint32_t b = __byte_perm(w, 0u, 0x0123u);  // bytes reversed
+    const uint32_t r = ((b >> 4) & 0x0f0f0f0fu) | ((b & 0x0f0f0f0fu) << 4);
+    return rev ? r : w;
+  }
+  __device__ __forceinline__ float4 at(Blk w, uint32_t j) const {
     return table[(w >> (28u - 4u * j)) & 15u];
   }
 };
 
 // ---------------------------------------------------------------------------
-// Forward / backward steps of the 4-state recursion (impute.cpp:353-373).
+// The 4-state recursion (impute.cpp:353-373).
+//
+// Both halves of an evaluation run in one form, x <- D_m (T x): the forward
+// half carries alpha_m = D_m T_m alpha_{m-1} up from site 0 (T_0 = I on the
+// uniform start); the backward half carries v_m = D_m beta_m = D_m T_{m+1}
+// v_{m+1} down from the top site (T_S = I on the all-ones start).  The two
+// meet at L = alpha_h . (T_{h+1} v_{h+1}).  T is symmetric, so this is the
+// reference's likelihood; one code path serves both halves.
 
 struct FState {
   float l00, l01, l10, l11, p1, p2;
-  int k;
-};
-struct BState {
-  float b00, b01, b10, b11;
   int k;
 };
 
@@ -242,6 +278,7 @@ __device__ __forceinline__ void select4(const float4 e, bool a0, bool a1, bool c
   s11 = c1 ? hi1 : lo1;
 }
 
+// One step with per-site power-of-two rescaling (the site-by-site pass).
 __device__ __forceinline__ void fwd_step(FState &f, const float4 t, float s00, float s01,
                                          float s10, float s11) {
   const float b00 = fmaf(f.l11, t.z, fmaf(f.p1, t.y, f.l00 * t.x));
@@ -265,28 +302,8 @@ __device__ __forceinline__ void fwd_step(FState &f, const float4 t, float s00, f
   }
 }
 
-// beta_{m-1} = T_m D_m beta_m (T symmetric, so the forward formulas apply).
-__device__ __forceinline__ void bwd_step(BState &b, const float4 t, float s00, float s01,
-                                         float s10, float s11) {
-  float v00 = b.b00 * s00, v01 = b.b01 * s01, v10 = b.b10 * s10, v11 = b.b11 * s11;
-  float q1 = v01 + v10, q2 = v00 + v11;
-  if (q1 + q2 < kTiny) {
-    v00 *= kHuge;
-    v01 *= kHuge;
-    v10 *= kHuge;
-    v11 *= kHuge;
-    q1 *= kHuge;
-    q2 *= kHuge;
-    b.k -= 64;
-  }
-  b.b00 = fmaf(v11, t.z, fmaf(q1, t.y, v00 * t.x));
-  b.b01 = fmaf(v10, t.z, fmaf(q2, t.y, v01 * t.x));
-  b.b10 = fmaf(v01, t.z, fmaf(q2, t.y, v10 * t.x));
-  b.b11 = fmaf(v00, t.z, fmaf(q1, t.y, v11 * t.x));
-}
-
-// The same steps without per-site rescaling, in a shared-term form of T:
-// with p1 = l01 + l10 and p2 = l00 + l11,
+// The same step without rescaling, in a shared-term form of T: with
+// p1 = l01 + l10 and p2 = l00 + l11,
 //   (T l)_00 = (x - z) l00 + c1,  (T l)_11 = (x - z) l11 + c1,  c1 = y p1 + z p2
 //   (T l)_01 = (x - z) l01 + c2,  (T l)_10 = (x - z) l10 + c2,  c2 = y p2 + z p1
 // for t = (x, y, z, x - z): 14 operations a site instead of 18.  The caller
@@ -303,16 +320,14 @@ __device__ __forceinline__ void fwd_fast(FState &f, const float4 t, float s00, f
   f.p2 = f.l00 + f.l11;
 }
 
-__device__ __forceinline__ void bwd_fast(BState &b, const float4 t, float s00, float s01,
-                                         float s10, float s11) {
-  const float v00 = b.b00 * s00, v01 = b.b01 * s01, v10 = b.b10 * s10, v11 = b.b11 * s11;
-  const float q1 = v01 + v10, q2 = v00 + v11;
-  const float c1 = fmaf(t.z, q2, t.y * q1);
-  const float c2 = fmaf(t.z, q1, t.y * q2);
-  b.b00 = fmaf(t.w, v00, c1);
-  b.b01 = fmaf(t.w, v01, c2);
-  b.b10 = fmaf(t.w, v10, c2);
-  b.b11 = fmaf(t.w, v11, c1);
+// x <- T x alone (the backward half's last step, T_{h+1} v_{h+1}).
+__device__ __forceinline__ void apply_tran(FState &f, const float4 t) {
+  const float c1 = fmaf(t.z, f.p2, t.y * f.p1);
+  const float c2 = fmaf(t.z, f.p1, t.y * f.p2);
+  f.l00 = fmaf(t.w, f.l00, c1);
+  f.l01 = fmaf(t.w, f.l01, c2);
+  f.l10 = fmaf(t.w, f.l10, c2);
+  f.l11 = fmaf(t.w, f.l11, c1);
 }
 
 // Exact power-of-two normalisation at a block boundary: scales the state so
@@ -336,28 +351,19 @@ __device__ __forceinline__ uint32_t fwd_norm(FState &f) {
   f.k += e - 189;
   return (uint32_t)(e - 65);
 }
-__device__ __forceinline__ uint32_t bwd_norm(BState &b) {
-  const uint32_t eb = __float_as_uint((b.b00 + b.b11) + (b.b01 + b.b10)) & 0x7f800000u;
-  const float sc = __uint_as_float(0x9e000000u - eb);
-  b.b00 *= sc;
-  b.b01 *= sc;
-  b.b10 *= sc;
-  b.b11 *= sc;
-  const int e = (int)(eb >> 23);
-  b.k += e - 189;
-  return (uint32_t)(e - 65);
-}
 // The same for a state kept in range site by site (any sum down to 2^-65 is
 // legitimate there): the exponent is clamped so the scale stays a normal float.
-__device__ __forceinline__ void bwd_renorm(BState &b) {
-  const int e = (int)((__float_as_uint((b.b00 + b.b11) + (b.b01 + b.b10)) >> 23) & 0xffu);
+__device__ __forceinline__ void fwd_renorm(FState &f) {
+  const int e = (int)((__float_as_uint(f.p1 + f.p2) >> 23) & 0xffu);
   const int ec = max(e, 62);
   const float sc = __uint_as_float((uint32_t)(316 - ec) << 23);  // 2^(189 - ec)
-  b.b00 *= sc;
-  b.b01 *= sc;
-  b.b10 *= sc;
-  b.b11 *= sc;
-  b.k += ec - 189;
+  f.l00 *= sc;
+  f.l01 *= sc;
+  f.l10 *= sc;
+  f.l11 *= sc;
+  f.p1 *= sc;
+  f.p2 *= sc;
+  f.k += ec - 189;
 }
 
 // Overflow guard of the site-by-site pass (emissions above 1 could grow it).
@@ -387,6 +393,25 @@ __device__ __forceinline__ Parents load_parents(const uint64_t *haps, uint32_t w
   return r;
 }
 
+// Bit-reversed parent words: bit 63 - i holds site i of the word, so the
+// backward half reads its descending sites as ascending bits.
+__device__ __forceinline__ Parents reverse_parents(const Parents &p) {
+  Parents r;
+  r.f0 = __brevll(p.f0);
+  r.f1 = __brevll(p.f1);
+  r.m0 = __brevll(p.m0);
+  r.m1 = __brevll(p.m1);
+  return r;
+}
+
+__device__ __forceinline__ void prefetch_parents(const uint64_t *haps, uint32_t wn, uint4 q,
+                                                 uint32_t w) {
+  prefetch_l1(haps + (size_t)q.x * wn + w);
+  prefetch_l1(haps + (size_t)q.y * wn + w);
+  prefetch_l1(haps + (size_t)q.z * wn + w);
+  prefetch_l1(haps + (size_t)q.w * wn + w);
+}
+
 // 8-bit windows of the four parent words for one block of 8 sites.
 struct Bits8 {
   uint32_t f0, f1, m0, m1;
@@ -409,76 +434,30 @@ __device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, u
           (bw.m1 & bit) != 0u, s00, s01, s10, s11);
 }
 
-// One staged block pair for V quadruples: forward over the 8 sites of slot
-// sf, backward over the 8 sites of slot sb (highest first), then both states
-// normalised (kSub = 2: also after the first 4 sites of each); eacc[v]
-// collects the range codes.  Every staged emission and transition row is
-// read once and used by all V quadruples: 8 V independent FMA chains per
-// lane.
-template <int V, class E, int kSub = 1>
-__device__ __forceinline__ void both_staged8(FState (&f)[V], BState (&b)[V], const E &ef,
-                                             const E &eb, const float4 *sf, const float4 *sb,
-                                             const Bits8 (&wf)[V], const Bits8 (&wb)[V],
-                                             uint32_t (&eacc)[V]) {
+// One staged block of 8 sites: row j of the slot (transition rows first,
+// emission data from slot + 8) with bit j of the parent windows; the state
+// is normalised at the end (kSub = 2: also after the first 4 sites) and
+// eacc collects the range codes.
+template <class E, int kSub>
+__device__ __forceinline__ void block8(FState &x, const E &em, const float4 *slot,
+                                       typename E::Blk eb, const Bits8 &bw, uint32_t &eacc) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
-    const float4 ex = ef.staged(sf + 8, j), ey = eb.staged(sb + 8, 7 - j);
-    const float4 tx = sf[j], ty = sb[7 - j];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      float s00, s01, s10, s11, r00, r01, r10, r11;
-      site_emission(ex, wf[v], j, s00, s01, s10, s11);
-      site_emission(ey, wb[v], 7 - j, r00, r01, r10, r11);
-      fwd_fast(f[v], tx, s00, s01, s10, s11);
-      bwd_fast(b[v], ty, r00, r01, r10, r11);
-    }
-    if (kSub == 2 && j == 3) {
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-        eacc[v] |= fwd_norm(f[v]) | bwd_norm(b[v]);
-    }
+    const float4 e = em.at(eb, j), t = slot[j];
+    float s00, s01, s10, s11;
+    site_emission(e, bw, j, s00, s01, s10, s11);
+    fwd_fast(x, t, s00, s01, s10, s11);
+    if (kSub == 2 && j == 3)
+      eacc |= fwd_norm(x);
   }
-#pragma unroll
-  for (int v = 0; v < V; ++v)
-    eacc[v] |= fwd_norm(f[v]) | bwd_norm(b[v]);
-}
-
-template <int V, class E, int kSub = 1>
-__device__ __forceinline__ void fwd_staged8(FState (&f)[V], const E &ef, const float4 *sf,
-                                            const Bits8 (&wf)[V], uint32_t (&eacc)[V]) {
-#pragma unroll
-  for (uint32_t j = 0; j < 8; ++j) {
-    const float4 ex = ef.staged(sf + 8, j), tx = sf[j];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      float s00, s01, s10, s11;
-      site_emission(ex, wf[v], j, s00, s01, s10, s11);
-      fwd_fast(f[v], tx, s00, s01, s10, s11);
-    }
-    if (kSub == 2 && j == 3) {
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-        eacc[v] |= fwd_norm(f[v]);
-    }
-  }
-#pragma unroll
-  for (int v = 0; v < V; ++v)
-    eacc[v] |= fwd_norm(f[v]);
-}
-
-__device__ __forceinline__ void prefetch_parents(const uint64_t *haps, uint32_t wn, uint4 q,
-                                                 uint32_t w) {
-  prefetch_l1(haps + (size_t)q.x * wn + w);
-  prefetch_l1(haps + (size_t)q.y * wn + w);
-  prefetch_l1(haps + (size_t)q.z * wn + w);
-  prefetch_l1(haps + (size_t)q.w * wn + w);
+  eacc |= fwd_norm(x);
 }
 
 // Log-likelihood of one quadruple by a plain forward pass, site by site, with
 // the per-site power-of-two rescaling of fwd_step (the scheme of
 // impute.cpp:327-376), reading emission, transition and parent words straight
-// from global memory.  Used for single-word chunks and, rarely, for an
-// evaluation whose blocked pass may have lost range.
+// from global memory.  Used, rarely, for an evaluation whose blocked pass may
+// have lost range.
 template <class E>
 __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, uint32_t wn,
                                             uint32_t S, const float4 *__restrict__ tran4,
@@ -503,161 +482,112 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
   return log(sum) + (double)f.k * 0.69314718055994530942;
 }
 
-// Log-likelihoods (natural log, binary64) of V quadruples of one sample.
-//
-// Words [0, wf) run forward and words [wf, wn) backward, one block of 8
-// sites of each at a time, in one instruction stream; the blocks' emission
-// and transition rows are staged by the P lanes of the group into the
-// group's shared-memory ring two block pairs ahead (cp.async), so the
-// arithmetic reads shared memory only.  States are normalised at block
-// boundaries (exact powers of two); a quadruple whose block sums left the
-// safe range is recomputed by like_forward.  A ragged last word
-// (S % 64 != 0) runs backward alone, site by site, before the rest; a
-// single-word chunk runs like_forward.  All P lanes of the group call this
-// together; gmask names the lanes that synchronise at each block (the group,
-// or the whole warp when every group runs the same loop).
-template <int V, int kMaxRows, class E, int kSub = 1>
-__device__ __forceinline__ void eval_like(const GenParams &p, const E &em0,
-                                          const uint4 (&q)[V], float4 *stage, uint32_t li,
-                                          uint32_t P, unsigned gmask, double (&out)[V]) {
+// Log-likelihood (natural log, binary64) of quadruple q, scored by a lane
+// pair of a P-lane group: the even lane runs the forward half over the
+// blocks [0, nf) of the nb = floor(S/8) full 8-site blocks, nf = ceil(nb/2);
+// the odd lane first runs the sites above the last full block site by site
+// (straight from global memory), then the backward half over blocks
+// [nf, nb) from the top.  Step t stages forward block t and backward block
+// nb-1-t of every pair's rows into the group's ring (cp.async, two steps
+// ahead), so the arithmetic reads shared memory only.  States are normalised
+// at block boundaries (exact powers of two); a quadruple whose block sums left
+// the safe range is recomputed site by site by the even lane.  The pair joins
+// with two exact-product shuffles, so both lanes return the same value.  All P
+// lanes of the group call this together; gmask names the lanes that
+// synchronise at each step (the group, or the whole warp when every group
+// runs the same loop).  tran4 holds S + 1 rows, rows 0 and S the identity.
+template <int kMaxRows, class E, int kSub = 1>
+__device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uint4 q,
+                                            float4 *stage, uint32_t li, uint32_t P,
+                                            unsigned gmask) {
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tran4 = p.tran4;
-  if (wn == 1) {
-#pragma unroll
-    for (int v = 0; v < V; ++v)
-      out[v] = like_forward(p.haps, wn, S, tran4, em0, q[v]);
-    return;
-  }
+  const bool bwd = (li & 1u) != 0;
+  const uint32_t nb = S >> 3, nf = (nb + 1) >> 1, nbk = nb - nf;
   // block-normalised states start at sum 2^62: the forward state 1/4 scaled
   // by 2^62, the backward state 1 scaled by 2^60
-  FState f[V];
-  BState b[V];
-  uint32_t eacc[V];  // OR of the blocks' range codes (fwd_norm)
-#pragma unroll
-  for (int v = 0; v < V; ++v) {
-    f[v].l00 = f[v].l01 = f[v].l10 = f[v].l11 = 0x1p60f;
-    f[v].p1 = f[v].p2 = 0x1p61f;
-    f[v].k = -62;
-    b[v].b00 = b[v].b01 = b[v].b10 = b[v].b11 = 0x1p60f;
-    b[v].k = -60;
-    eacc[v] = 0;
-  }
-  E ef = em0, eb = em0;
-  const uint32_t wf = (wn + 1) >> 1;
-  uint32_t wb = wn - 1;
-  if (S & 63u) {
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const Parents pw = load_parents(p.haps, wn, q[v], wb);
+  FState x;
+  x.l00 = x.l01 = x.l10 = x.l11 = 0x1p60f;
+  x.p1 = x.p2 = 0x1p61f;
+  x.k = bwd ? -60 : -62;
+  uint32_t eacc = 0;  // OR of the blocks' range codes (fwd_norm)
+  if (bwd && (S & 7u)) {
+    const Parents pw = load_parents(p.haps, wn, q, (S - 1) >> 6);
 #pragma unroll 1
-      for (int m = (int)S - 1; m >= (int)(wb * 64); --m) {
-        const uint32_t j = (uint32_t)m & 63u;
-        float s00, s01, s10, s11;
-        select4(eb.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1,
-                (pw.m0 >> j) & 1, (pw.m1 >> j) & 1, s00, s01, s10, s11);
-        bwd_step(b[v], __ldg(tran4 + m), s00, s01, s10, s11);
-      }
-      bwd_renorm(b[v]);
+    for (int m = (int)S - 1; m >= (int)(nb * 8); --m) {
+      const uint32_t j = (uint32_t)m & 63u;
+      float s00, s01, s10, s11;
+      select4(em.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
+              (pw.m1 >> j) & 1, s00, s01, s10, s11);
+      fwd_step(x, __ldg(tran4 + m + 1), s00, s01, s10, s11);
     }
-    --wb;
+    fwd_renorm(x);
   }
-  const uint32_t nb = (wb + 1 >= wf) ? wb + 1 - wf : 0;
-  float4 *stF = stage, *stB = stage + kRing * kSlotF4;
+  float4 *const stF = stage, *const stB = stage + kBwdOffF4;
   const StageRows rows = stage_rows<kMaxRows>(li, P);
-  // Block pairs t = 8 i + blk: forward sites i*64 + 8*blk .. +7 and
-  // backward sites (wb - i)*64 + 8*(7 - blk) .. +7.
-  const uint32_t T = nb * 8;
-  auto issue_pair = [&](uint32_t t) {
-    const uint32_t i = t >> 3, blk = t & 7u;
-    const uint32_t m0 = i * 64 + blk * 8, n0 = (wb - i) * 64 + (7 - blk) * 8;
-    float4 *sf = stF + (t % kRing) * kSlotF4, *sb = stB + (t % kRing) * kSlotF4;
-    stage8<kMaxRows>(sf, tran4 + m0, rows);
-    stage8<kMaxRows>(sb, tran4 + n0, rows);
-    ef.template stage<kMaxRows>(sf + 8, m0, rows);
-    eb.template stage<kMaxRows>(sb + 8, n0, rows);
+  auto issue = [&](uint32_t t) {
+    const uint32_t so = (t % kRing) * kSlotF4, m0 = t * 8;
+    stage8<kMaxRows>(stF + so, tran4 + m0, rows);
+    em.template stage<kMaxRows>(stF + so + 8, m0, rows);
+    if (t < nbk) {
+      const uint32_t n0 = (nb - 1 - t) * 8;
+      stage8_rev<kMaxRows>(stB + so, tran4 + n0 + 1, rows);
+      em.template stage_rev<kMaxRows>(stB + so + 8, n0, rows);
+    }
   };
-  if (T > 0)
-    issue_pair(0);
+  if (nf > 0)
+    issue(0);
   cp_async_commit();
-  if (T > 1)
-    issue_pair(1);
+  if (nf > 1)
+    issue(1);
   cp_async_commit();
-  Parents pf[V], pb[V];
+  float4 *const mine = bwd ? stB : stF;
+  Parents pw = {0, 0, 0, 0};
+  uint32_t wcur = 0xffffffffu;
 #pragma unroll 1
-  for (uint32_t t = 0; t < T; ++t) {
-    if (t + 2 < T)
-      issue_pair(t + 2);
+  for (uint32_t t = 0; t < nf; ++t) {
+    if (t + 2 < nf)
+      issue(t + 2);
     cp_async_commit();
-    const uint32_t i = t >> 3, blk = t & 7u;
-    if (blk == 0) {
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        pf[v] = load_parents(p.haps, wn, q[v], i);
-        pb[v] = load_parents(p.haps, wn, q[v], wb - i);
-        if (i + 1 < nb) {  // next words' parents
-          prefetch_parents(p.haps, wn, q[v], i + 1);
-          prefetch_parents(p.haps, wn, q[v], wb - i - 1);
-        }
-      }
+    const bool act = !bwd || t < nbk;
+    const uint32_t blk = bwd ? nb - 1 - t : t;
+    const uint32_t w = blk >> 3;
+    if (act && w != wcur) {
+      wcur = w;
+      const Parents raw = load_parents(p.haps, wn, q, w);
+      pw = bwd ? reverse_parents(raw) : raw;
+      // next word of this lane's direction, if it holds one of its blocks
+      if (bwd ? (w * 8 > nf) : ((w + 1) * 8 < nf))
+        prefetch_parents(p.haps, wn, q, bwd ? w - 1 : w + 1);
     }
-    Bits8 xf[V], xb[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      xf[v] = window8(pf[v], blk * 8);
-      xb[v] = window8(pb[v], (7 - blk) * 8);
-    }
+    const Bits8 xb = window8(pw, bwd ? 56u - 8u * (blk & 7u) : 8u * (blk & 7u));
     cp_async_wait<2>();
     __syncwarp(gmask);
-    const uint32_t slot = (t % kRing) * kSlotF4;
-    both_staged8<V, E, kSub>(f, b, ef, eb, stF + slot, stB + slot, xf, xb, eacc);
+    const float4 *slot = mine + (t % kRing) * kSlotF4;
+    if (act)
+      block8<E, kSub>(x, em, slot, em.block(slot + 8, bwd), xb, eacc);
     __syncwarp(gmask);
   }
-  // forward-only words [nb, wf) (wn odd, or a ragged last word)
-  const uint32_t T2 = (wf - nb) * 8;
-  auto issue_fwd = [&](uint32_t t) {
-    const uint32_t m0 = (nb + (t >> 3)) * 64 + (t & 7u) * 8;
-    float4 *sf = stF + (t % kRing) * kSlotF4;
-    stage8<kMaxRows>(sf, tran4 + m0, rows);
-    ef.template stage<kMaxRows>(sf + 8, m0, rows);
-  };
-  if (T2 > 0)
-    issue_fwd(0);
-  cp_async_commit();
-  if (T2 > 1)
-    issue_fwd(1);
-  cp_async_commit();
-#pragma unroll 1
-  for (uint32_t t = 0; t < T2; ++t) {
-    if (t + 2 < T2)
-      issue_fwd(t + 2);
-    cp_async_commit();
-    const uint32_t blk = t & 7u;
-    if (blk == 0) {
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-        pf[v] = load_parents(p.haps, wn, q[v], nb + (t >> 3));
-    }
-    Bits8 xf[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v)
-      xf[v] = window8(pf[v], blk * 8);
-    cp_async_wait<2>();
-    __syncwarp(gmask);
-    fwd_staged8<V, E, kSub>(f, ef, stF + (t % kRing) * kSlotF4, xf, eacc);
-    __syncwarp(gmask);
-  }
-#pragma unroll
-  for (int v = 0; v < V; ++v) {
-    if ((eacc[v] & ~127u) == 0) {
-      const double dot = (double)f[v].l00 * (double)b[v].b00 + (double)f[v].l01 * (double)b[v].b01 +
-                         (double)f[v].l10 * (double)b[v].b10 + (double)f[v].l11 * (double)b[v].b11;
-      out[v] = log(dot) + (double)(f[v].k + b[v].k) * 0.69314718055994530942;
-    } else {
+  if (bwd)  // beta_{8 nf - 1} = T_{8 nf} v_{8 nf} (row S is the identity)
+    apply_tran(x, __ldg(tran4 + nf * 8));
+  const float y00 = __shfl_xor_sync(gmask, x.l00, 1), y01 = __shfl_xor_sync(gmask, x.l01, 1),
+              y10 = __shfl_xor_sync(gmask, x.l10, 1), y11 = __shfl_xor_sync(gmask, x.l11, 1);
+  const int yk = __shfl_xor_sync(gmask, x.k, 1);
+  const uint32_t bad = (eacc | __shfl_xor_sync(gmask, eacc, 1)) & ~127u;
+  // alpha . beta on both lanes: the same exact products in the same order
+  const double dot = (double)x.l00 * (double)y00 + (double)x.l01 * (double)y01 +
+                     (double)x.l10 * (double)y10 + (double)x.l11 * (double)y11;
+  double L = log(dot) + (double)(x.k + yk) * 0.69314718055994530942;
+  if (__any_sync(gmask, bad != 0u)) {
+    double Lf = L;
+    if (bad && !bwd) {
       if (p.stats)
         atomicAdd(p.stats + 3, 1ull);
-      out[v] = like_forward(p.haps, wn, S, tran4, em0, q[v]);
+      Lf = like_forward(p.haps, wn, S, tran4, em, q);
     }
+    L = __shfl_sync(gmask, Lf, (threadIdx.x & 31u) & ~1u);
   }
+  return L;
 }
 
 // ---------------------------------------------------------------------------
@@ -1359,12 +1289,11 @@ __device__ __forceinline__ LaneGroups regroup(uint32_t lane, uint32_t na) {
   return g;
 }
 
-template <int P, int V, class E, class Src, int kSub = 1>
+template <int P, class E, class Src, int kSub = 1>
 __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counter,
                                                 unsigned long long *stats, int *error,
                                                 const float4 *vq_smem) {
-  static_assert(P == 1 || P == 2 || P == 4 || P == 8 || P == 16 || P == 32, "P");
-  static_assert(V == 1 || V == 2, "V");
+  static_assert(P == 2 || P == 4 || P == 8 || P == 16 || P == 32, "P");
   constexpr unsigned FULL = 0xffffffffu;
   constexpr uint32_t G0 = 32u / P;  // group slots (staging rings) per warp
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -1467,45 +1396,36 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
 
     const GenParams &p = src.chunk(c);
     const uint32_t N = p.N, C = p.C, H = p.H;
-    // one speculative round of Pc V evaluations: lane li scores evaluations
-    // e + li V + v, v < V (round position r = li V + v)
-    const uint32_t PV = Pc * (uint32_t)V;
-    const uint32_t k = active ? min(PV, C + 1 - e) : 0u;
-    uint32_t slot[V], phap[V];
-    double u[V];
-    uint4 myq[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const uint32_t r = li * V + v, ev = e + r;
-      slot[v] = 0;
-      phap[v] = 0;
-      u[v] = 0.0;
-      myq[v] = q;
-      if (r < k && ev > 0) {
-        const uint32_t cyc = ev - 1;
-        if (p.tr_slot) {
-          slot[v] = p.tr_slot[(size_t)s * C + cyc] & 3u;
-          u[v] = p.tr_u[(size_t)s * C + cyc];
-        } else {
-          glp_mh_draw(p.seed, p.generation, s, cyc, &slot[v], &u[v]);
-        }
-        phap[v] = p.props ? __ldg(p.props + (size_t)cyc * N + s)
-                  : (p.kick_first && cyc == 0)
-                      ? glp_surrogate_ref(p.seed, p.generation, s, cyc, GLP_TAG_PROP, 2u * N,
-                                          H, p.nbr, p.klen)
-                      : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP, p.samp_lo,
-                                      p.samp_hi, p.nbr, p.klen);
-        if (phap[v] >= H) {
-          atomicOr(error, 1);
-          phap[v] = 0;
-        }
-        set_slot(myq[v], slot[v], phap[v]);
+    // One speculative round: the group's Pc/2 lane pairs score the next Pc/2
+    // positions of the chain, pair r = li/2 position e + r (its even lane the
+    // forward half, its odd lane the backward half of the evaluation).
+    const uint32_t npos = Pc >> 1, r = li >> 1, ev = e + r;
+    const bool lead_lane = (li & 1u) == 0;
+    const uint32_t k = active ? min(npos, C + 1 - e) : 0u;
+    uint32_t slot = 0, phap = 0;
+    double u = 0.0;
+    uint4 myq = q;
+    if (r < k && ev > 0) {
+      const uint32_t cyc = ev - 1;
+      if (p.tr_slot) {
+        slot = p.tr_slot[(size_t)s * C + cyc] & 3u;
+        u = p.tr_u[(size_t)s * C + cyc];
+      } else {
+        glp_mh_draw(p.seed, p.generation, s, cyc, &slot, &u);
       }
+      phap = p.props ? __ldg(p.props + (size_t)cyc * N + s)
+             : (p.kick_first && cyc == 0)
+                 ? glp_surrogate_ref(p.seed, p.generation, s, cyc, GLP_TAG_PROP, 2u * N, H,
+                                     p.nbr, p.klen)
+                 : glp_surrogate(p.seed, p.generation, s, cyc, GLP_TAG_PROP, p.samp_lo,
+                                 p.samp_hi, p.nbr, p.klen);
+      if (phap >= H) {
+        atomicOr(error, 1);
+        phap = 0;
+      }
+      set_slot(myq, slot, phap);
     }
-    double L[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v)
-      L[v] = 0.0;
+    double L = 0.0;
     // When every lane of the warp scores a chunk of the same length, all
     // groups run the same block loop and synchronise as one warp: a
     // group-masked __syncwarp would let the groups drift apart and issue the
@@ -1514,94 +1434,58 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
     __match_all_sync(FULL, active ? p.S : 0u, (int *)&same);
     const bool warp_lockstep = same && amask == FULL;
     if (active) {
-      // every lane of an active group evaluates (positions past k score the
+      // every pair of an active group evaluates (positions past k score the
       // base quadruple and drop the result) so the group shares its ring
       E em;
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
       const unsigned gm = (Pc == 32 || warp_lockstep) ? FULL : (((1u << Pc) - 1u) << gbase);
       float4 *ring = glp_stage + ((size_t)warp * G0 + gidx) * kGroupStrideF4;
-      eval_like<V, (P >= 8 ? 1 : 8 / P), E, kSub>(p, em, myq, ring, li, Pc, gm, L);
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-        if (li * V + v >= k)
-          L[v] = 0.0;
+      L = eval_pair<(P >= 8 ? 1 : 8 / P), E, kSub>(p, em, myq, ring, li, Pc, gm);
+      if (r >= k)
+        L = 0.0;
     }
     // The accept rule of MHSampler.hpp:86-93 in chain order.  Every
     // evaluation of the round was built on the round's starting state, and
     // until the first acceptance the chain's current likelihood is the
     // starting one, so each position tests its own proposal against it in
     // parallel and the first accepting position (in chain order) wins: the
-    // same decisions as the sequential loop.  A lane's first accepting
-    // position is its candidate; the group's lowest candidate lane wins.
-    const double L0 = __shfl_sync(FULL, L[0], gbase);
+    // same decisions as the sequential loop.  The even lanes vote.
+    const double L0 = __shfl_sync(FULL, L, gbase);
     const double curr0 = (e == 0) ? L0 : curr;
-    uint32_t vfirst = V;
-#pragma unroll
-    for (int v = V - 1; v >= 0; --v) {
-      const uint32_t r = li * V + v;
-      const bool acc = r < k && e + r > 0 &&
-                       (L[v] >= curr0 || u[v] < exp((L[v] - curr0) * (double)p.pen));
-      if (acc)
-        vfirst = (uint32_t)v;
-    }
+    const bool acc = lead_lane && r < k && ev > 0 &&
+                     (L >= curr0 || u < exp((L - curr0) * (double)p.pen));
     const unsigned gmask = (Pc == 32) ? FULL : (((1u << Pc) - 1u) << gbase);
-    const unsigned abal = __ballot_sync(FULL, vfirst < (uint32_t)V) & gmask;
+    const unsigned abal = __ballot_sync(FULL, acc) & gmask;
     const uint32_t srcl = abal ? (uint32_t)(__ffs(abal) - 1) : gbase;
-    const uint32_t vw = __shfl_sync(FULL, vfirst, srcl);
-    const uint32_t first_acc = abal ? (srcl - gbase) * V + vw : PV;
-    double Lw = L[0];
-    uint32_t slw = slot[0], phw = phap[0];
-#pragma unroll
-    for (int v = 1; v < V; ++v)
-      if ((uint32_t)v == vw) {
-        Lw = L[v];
-        slw = slot[v];
-        phw = phap[v];
-      }
-    const double La = __shfl_sync(FULL, Lw, srcl);
-    const uint32_t sla = __shfl_sync(FULL, slw, srcl);
-    const uint32_t pha = __shfl_sync(FULL, phw, srcl);
+    const uint32_t first_acc = abal ? (srcl - gbase) >> 1 : npos;
+    const double La = __shfl_sync(FULL, L, srcl);
+    const uint32_t sla = __shfl_sync(FULL, slot, srcl);
+    const uint32_t pha = __shfl_sync(FULL, phap, srcl);
     // The positions after the first acceptance that replace the same slot
     // scored exactly the quadruple the sequential chain builds there (it
     // differs from the round's start only in that slot), so the chain goes on
     // through them -- each tested against the likelihood accepted last --
     // up to the first position that replaces another slot.
     uint32_t last = first_acc, hap = pha;
-    uint64_t more = 0;  // accepted positions after first_acc
+    uint32_t more = 0;  // accepted positions after first_acc
     double cur = La;
     bool go = active && abal != 0;
-    for (uint32_t d = 1; d < 32u * V; ++d) {
-      const uint32_t r = first_acc + d;
-      go = go && r < k;
-      const uint32_t rr = go ? r : 0u, src = gbase + rr / V, vr = rr % V;
-      uint32_t sl_r = __shfl_sync(FULL, slot[0], src);
-#pragma unroll
-      for (int v = 1; v < V; ++v) {
-        const uint32_t t = __shfl_sync(FULL, slot[v], src);
-        if ((uint32_t)v == vr)
-          sl_r = t;
-      }
+    for (uint32_t d = 1; d < 16u; ++d) {
+      const uint32_t r2 = first_acc + d;
+      go = go && r2 < k;
+      const uint32_t from = gbase + 2u * (go ? r2 : 0u);
+      const uint32_t sl_r = __shfl_sync(FULL, slot, from);
       go = go && sl_r == sla;
       if (!__any_sync(FULL, go))
         break;
-      double L_r = __shfl_sync(FULL, L[0], src), u_r = __shfl_sync(FULL, u[0], src);
-      uint32_t ph_r = __shfl_sync(FULL, phap[0], src);
-#pragma unroll
-      for (int v = 1; v < V; ++v) {
-        const double tl = __shfl_sync(FULL, L[v], src), tu = __shfl_sync(FULL, u[v], src);
-        const uint32_t tp = __shfl_sync(FULL, phap[v], src);
-        if ((uint32_t)v == vr) {
-          L_r = tl;
-          u_r = tu;
-          ph_r = tp;
-        }
-      }
+      const double L_r = __shfl_sync(FULL, L, from), u_r = __shfl_sync(FULL, u, from);
+      const uint32_t ph_r = __shfl_sync(FULL, phap, from);
       if (go) {
-        last = r;
+        last = r2;
         if (L_r >= cur || u_r < exp((L_r - cur) * (double)p.pen)) {
           cur = L_r;
           hap = ph_r;
-          more |= 1ull << r;
+          more |= 1u << r2;
         }
       }
     }
@@ -1612,23 +1496,19 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
         curr = cur;
       }
     }
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const uint32_t r = li * V + v, ev = e + r;
-      if (r < k && r <= last) {
-        if (p.eval_trace)
-          p.eval_trace[(size_t)s * (C + 1) + ev] = L[v];
-        if (ev > 0 && p.accept_trace)
-          p.accept_trace[(size_t)s * C + ev - 1] =
-              (uint8_t)(r == first_acc || ((more >> r) & 1ull));
-      }
+    if (lead_lane && r < k && r <= last) {
+      if (p.eval_trace)
+        p.eval_trace[(size_t)s * (C + 1) + ev] = L;
+      if (ev > 0 && p.accept_trace)
+        p.accept_trace[(size_t)s * C + ev - 1] =
+            (uint8_t)(r == first_acc || ((more >> r) & 1u));
     }
     if (active) {
-      e = (first_acc < PV) ? e + last + 1 : e + k;
+      e = (first_acc < npos) ? e + last + 1 : e + k;
       if (li == 0) {
         n_evals += k;
         ++n_rounds;
-        n_acc += first_acc < PV ? 1u + (uint32_t)__popcll(more) : 0u;
+        n_acc += first_acc < npos ? 1u + (uint32_t)__popc(more) : 0u;
       }
     }
 
@@ -1656,34 +1536,33 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
   }
 }
 
-// Dynamic shared memory of a generation kernel with P lanes per sample and V
-// evaluations per lane: one staging ring pair per group.
-__host__ __device__ constexpr size_t stage_bytes(int P, int /*V*/) {
+// Dynamic shared memory of a generation kernel with P lanes per sample: one
+// staging ring (both directions) per group.
+__host__ __device__ constexpr size_t stage_bytes(int P) {
   return sizeof(float4) * (size_t)kWarps * (32 / P) * kGroupStrideF4;
 }
 
 // One chunk per launch (the reference's RunHMMOnDevice granularity).  P lanes
-// per sample, V evaluations per lane and round; kSub = 2 normalises every 4
-// sites instead of every 8 (for GLs confident enough that 8-site blocks
-// often leave the normalisation range).
-template <int P, int V, class E, int kSub = 1>
-__global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
-    generation_kernel(const GenParams p) {
+// per sample (P/2 evaluations a round); kSub = 2 normalises every 4 sites
+// instead of every 8 (for GLs confident enough that 8-site blocks often leave
+// the normalisation range).
+template <int P, class E, int kSub = 1>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) generation_kernel(const GenParams p) {
   __shared__ float4 s_vq[16];
   if (threadIdx.x < 16 && p.vq_table)
     s_vq[threadIdx.x] = p.vq_table[threadIdx.x];
   __syncthreads();
   const OneChunk src{p};
-  generation_body<P, V, E, OneChunk, kSub>(src, p.counter, p.stats, p.error, s_vq);
+  generation_body<P, E, OneChunk, kSub>(src, p.counter, p.stats, p.error, s_vq);
 }
 
 // Many chunks of uneven size in one persistent launch: one queue over all
 // samples of all chunks.
-template <int P, int V, class E, int kSub = 1>
-__global__ void __launch_bounds__(kThreads, V == 1 ? kMinBlocks : 1)
+template <int P, class E, int kSub = 1>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     generation_multi_kernel(const MultiParams mp) {
   const ManyChunks src{mp};
-  generation_body<P, V, E, ManyChunks, kSub>(src, mp.counter, mp.stats, mp.error, nullptr);
+  generation_body<P, E, ManyChunks, kSub>(src, mp.counter, mp.stats, mp.error, nullptr);
 }
 
 // hmm_work after the generation kernel, over the published final

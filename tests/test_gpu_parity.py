@@ -114,7 +114,8 @@ def check_against_oracle(O, m, haps, quad, props, pen, out, seed, gen, trace=Non
     return worst, worst64
 
 
-@pytest.mark.parametrize("S", [1, 2, 16, 17, 33, 63, 64, 65, 130, 300, 1024])
+@pytest.mark.parametrize("S", [1, 2, 7, 8, 9, 16, 17, 24, 25, 33, 63, 64, 65, 130, 136, 300,
+                               513, 1024])
 def test_generation_matches_oracle_sites(dev, oracle_lib, S):
     m, haps, quad, props = make_problem(N=16, S=S, C=12)
     out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
@@ -138,31 +139,6 @@ def test_speculation_width_is_exact(dev, oracle_lib, lanes):
         dev.set_lanes_per_sample(0)
     assert np.array_equal(out["quad"], ref["quad"])
     assert np.array_equal(out["evals"], ref["evals"], equal_nan=True)
-    assert np.array_equal(out["hnew"], ref["hnew"])
-
-
-@pytest.mark.parametrize("lanes", [2, 4, 8])
-@pytest.mark.parametrize("S", [64, 257, 1000])
-def test_two_evaluations_per_lane_is_exact(dev, oracle_lib, lanes, S):
-    """Rounds of 2P evaluations (two per lane) give the sequential chain's
-    results, bit for bit, including the hmm_work haplotypes."""
-    m, haps, quad, props = make_problem(N=40, S=S, C=30, seed=5)
-    dev.set_lanes_per_sample(lanes)
-    dev.set_evals_per_lane(2)
-    try:
-        out = run_gpu(dev, m, haps, quad, props, 0.3, seed=3, gen=2)
-    finally:
-        dev.set_lanes_per_sample(0)
-        dev.set_evals_per_lane(0)
-    check_against_oracle(oracle_lib, m, haps, quad, props, 0.3, out, 3, 2)
-    dev.set_lanes_per_sample(1)
-    try:
-        ref = run_gpu(dev, m, haps, quad, props, 0.3, seed=3, gen=2)
-    finally:
-        dev.set_lanes_per_sample(0)
-    assert np.array_equal(out["quad"], ref["quad"])
-    assert np.array_equal(out["evals"], ref["evals"], equal_nan=True)
-    assert np.array_equal(out["acc"], ref["acc"])
     assert np.array_equal(out["hnew"], ref["hnew"])
 
 
@@ -239,8 +215,10 @@ def test_counters_describe_the_generation(dev):
 
 
 def test_evals_per_lane_argument(dev):
-    with pytest.raises(nat.GlpError):
-        dev.set_evals_per_lane(3)
+    for bad in (2, 3):
+        with pytest.raises(nat.GlpError):
+            dev.set_evals_per_lane(bad)
+    dev.set_evals_per_lane(1)
     dev.set_evals_per_lane(0)
 
 
