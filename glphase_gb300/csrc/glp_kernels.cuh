@@ -139,15 +139,19 @@ __device__ __forceinline__ void cp_async_wait() {
 // backward recursion applies there, so both directions read slot row j at
 // step j of a block.
 constexpr int kSlotF4 = 16;
-constexpr int kRing = 3;  // slots per direction: two blocks in flight
-// A group's ring: forward slots at [0, 48) and backward slots at [52, 100)
+// Slots per direction: block t uses slot t mod 4, so within the 4-block
+// quarter words the loop runs, every slot offset is a constant; two blocks
+// are in flight while one is read.
+constexpr int kRing = 4;
+// A group's ring: forward slots at [0, 64) and backward slots at [68, 132)
 // float4, so the forward and the backward row a group reads at one step are 4
-// float4 (16 banks) apart; rings of neighbouring groups are 105 float4 apart
+// float4 (16 banks) apart; rings of neighbouring groups are 137 float4 apart
 // (1 mod 8), so the 16-byte reads of the four 8-lane groups of a warp -- two
 // rows a group -- fall in eight distinct bank quads.
 constexpr int kBwdOffF4 = kRing * kSlotF4 + 4;
 constexpr int kGroupF4 = kBwdOffF4 + kRing * kSlotF4;
 constexpr int kGroupStrideF4 = kGroupF4 + 5;
+static_assert(kGroupStrideF4 % 8 == 1 && kBwdOffF4 % 8 == 4, "ring bank layout");
 
 // The rows of an 8-row block that lane li of a P-lane group copies: nr rows
 // from rb.  From P = 8 up lanes 0..7 take one row each; narrower groups take
@@ -201,13 +205,14 @@ struct EmitF32 {
     row = p.emit + (size_t)s * p.S;
   }
   __device__ __forceinline__ float4 get1(uint32_t m) const { return __ldg(row + m); }
+  // copy block t (sites 8t .. 8t+7) into a forward / backward slot
   template <int kMaxRows>
-  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, StageRows r) const {
-    stage8<kMaxRows>(dst, row + m0, r);
+  __device__ __forceinline__ void stage(float4 *dst, uint32_t t, StageRows r) const {
+    stage8<kMaxRows>(dst, row + 8 * (size_t)t, r);
   }
   template <int kMaxRows>
-  __device__ __forceinline__ void stage_rev(float4 *dst, uint32_t n0, StageRows r) const {
-    stage8_rev<kMaxRows>(dst, row + n0, r);
+  __device__ __forceinline__ void stage_rev(float4 *dst, uint32_t t, StageRows r) const {
+    stage8_rev<kMaxRows>(dst, row + 8 * (size_t)t, r);
   }
   __device__ __forceinline__ Blk block(const float4 *src, bool) const { return src; }
   __device__ __forceinline__ float4 at(Blk b, uint32_t j) const { return b[j]; }
@@ -233,13 +238,13 @@ struct EmitVQ {
     return table[(w >> (28u - 4u * (m & 7u))) & 15u];
   }
   template <int kMaxRows>
-  __device__ __forceinline__ void stage(float4 *dst, uint32_t m0, StageRows r) const {
+  __device__ __forceinline__ void stage(float4 *dst, uint32_t t, StageRows r) const {
     if (r.rb == 0 && r.nr != 0)  // lane 0 of the group
-      cp_async4(dst, col + (size_t)(m0 >> 3) * stride);
+      cp_async4(dst, col + (size_t)t * stride);
   }
   template <int kMaxRows>
-  __device__ __forceinline__ void stage_rev(float4 *dst, uint32_t n0, StageRows r) const {
-    stage<kMaxRows>(dst, n0, r);
+  __device__ __forceinline__ void stage_rev(float4 *dst, uint32_t t, StageRows r) const {
+    stage<kMaxRows>(dst, t, r);
   }
   __device__ __forceinline__ Blk block(const float4 *src, bool rev) const {
     const uint32_t w = *reinterpret_cast<const uint32_t *>(src);
@@ -412,21 +417,21 @@ __device__ __forceinline__ void prefetch_parents(const uint64_t *haps, uint32_t 
   prefetch_l1(haps + (size_t)q.w * wn + w);
 }
 
-// 8-bit windows of the four parent words for one block of 8 sites.
-struct Bits8 {
+// 32-bit halves of the four parent words: the bits of four 8-site blocks.
+struct Bits32 {
   uint32_t f0, f1, m0, m1;
 };
 
-__device__ __forceinline__ Bits8 window8(const Parents &pw, uint32_t shift) {
-  Bits8 r;
-  r.f0 = (uint32_t)(pw.f0 >> shift);
-  r.f1 = (uint32_t)(pw.f1 >> shift);
-  r.m0 = (uint32_t)(pw.m0 >> shift);
-  r.m1 = (uint32_t)(pw.m1 >> shift);
+__device__ __forceinline__ Bits32 half_words(const Parents &pw, uint32_t h) {
+  Bits32 r;
+  r.f0 = (uint32_t)(pw.f0 >> (32 * h));
+  r.f1 = (uint32_t)(pw.f1 >> (32 * h));
+  r.m0 = (uint32_t)(pw.m0 >> (32 * h));
+  r.m1 = (uint32_t)(pw.m1 >> (32 * h));
   return r;
 }
 
-__device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, uint32_t j,
+__device__ __forceinline__ void site_emission(const float4 e, const Bits32 &bw, uint32_t j,
                                               float &s00, float &s01, float &s10,
                                               float &s11) {
   const uint32_t bit = 1u << j;  // j is a compile-time constant in the unrolled block
@@ -435,17 +440,17 @@ __device__ __forceinline__ void site_emission(const float4 e, const Bits8 &bw, u
 }
 
 // One staged block of 8 sites: row j of the slot (transition rows first,
-// emission data from slot + 8) with bit j of the parent windows; the state
-// is normalised at the end (kSub = 2: also after the first 4 sites) and
-// eacc collects the range codes.
-template <class E, int kSub>
+// emission data from slot + 8) with bit 8B + j of the parent halves; the
+// state is normalised at the end (kSub = 2: also after the first 4 sites)
+// and eacc collects the range codes.
+template <int B, class E, int kSub>
 __device__ __forceinline__ void block8(FState &x, const E &em, const float4 *slot,
-                                       typename E::Blk eb, const Bits8 &bw, uint32_t &eacc) {
+                                       typename E::Blk eb, const Bits32 &bw, uint32_t &eacc) {
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
     const float4 e = em.at(eb, j), t = slot[j];
     float s00, s01, s10, s11;
-    site_emission(e, bw, j, s00, s01, s10, s11);
+    site_emission(e, bw, 8 * B + j, s00, s01, s10, s11);
     fwd_fast(x, t, s00, s01, s10, s11);
     if (kSub == 2 && j == 3)
       eacc |= fwd_norm(x);
@@ -482,20 +487,39 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
   return log(sum) + (double)f.k * 0.69314718055994530942;
 }
 
+// ln(dot) + k ln 2 for a positive dot product: the binary64 exponent of dot
+// joins k exactly, and the logarithm of its mantissa m in [1, 2) is taken in
+// binary32 (absolute error below 3e-7, against log-likelihoods of order
+// -S), so the FP64 pipe only adds the two parts.  Dots far below the block
+// range (never in the blocked pass) take the binary64 logarithm.
+__device__ __forceinline__ double log_scaled(double dot, int k) {
+  constexpr double kLn2 = 0.69314718055994530942;
+  if (!(dot > 0x1p-1000))
+    return log(dot) + (double)k * kLn2;
+  const long long bits = __double_as_longlong(dot);
+  const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+  const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  return (double)logf((float)m) + (double)(e + k) * kLn2;
+}
+
 // Log-likelihood (natural log, binary64) of quadruple q, scored by a lane
-// pair of a P-lane group: the even lane runs the forward half over the
-// blocks [0, nf) of the nb = floor(S/8) full 8-site blocks, nf = ceil(nb/2);
-// the odd lane first runs the sites above the last full block site by site
-// (straight from global memory), then the backward half over blocks
-// [nf, nb) from the top.  Step t stages forward block t and backward block
-// nb-1-t of every pair's rows into the group's ring (cp.async, two steps
-// ahead), so the arithmetic reads shared memory only.  States are normalised
-// at block boundaries (exact powers of two); a quadruple whose block sums left
-// the safe range is recomputed site by site by the even lane.  The pair joins
-// with two exact-product shuffles, so both lanes return the same value.  All P
-// lanes of the group call this together; gmask names the lanes that
-// synchronise at each step (the group, or the whole warp when every group
-// runs the same loop).  tran4 holds S + 1 rows, rows 0 and S the identity.
+// pair of a P-lane group.  Of the nw = floor(S/64) full 64-site words, the
+// even lane runs the forward half over words [0, wf), wf = ceil(nw/2); the
+// odd lane first runs the sites of the partial top word site by site
+// (straight from global memory), then the backward half over words
+// [wf, nw) from the top.  Each word is eight 8-site blocks, run four at a
+// time so that ring slots and parent-bit positions are constants: step t
+// stages forward block t and backward block 8 nw - 1 - t of every pair into
+// the group's ring (cp.async, two steps ahead), so the arithmetic reads
+// shared memory only.  With an odd word count the odd lane idles through
+// the last word (it computes on stale rows and restores its state after).
+// States are normalised at block boundaries (exact powers of two); a
+// quadruple whose block sums left the safe range is recomputed site by site
+// by the even lane.  The pair joins with two exact-product shuffles, so both
+// lanes return the same value.  All P lanes of the group call this together;
+// gmask names the lanes that synchronise at each step (the group, or the
+// whole warp when every group runs the same loop).  tran4 holds S + 1 rows,
+// rows 0 and S the identity.
 template <int kMaxRows, class E, int kSub = 1>
 __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uint4 q,
                                             float4 *stage, uint32_t li, uint32_t P,
@@ -503,7 +527,8 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tran4 = p.tran4;
   const bool bwd = (li & 1u) != 0;
-  const uint32_t nb = S >> 3, nf = (nb + 1) >> 1, nbk = nb - nf;
+  const uint32_t nw = S >> 6, wf = (nw + 1) >> 1, wb = nw - wf;
+  const uint32_t nbf = 8 * wf, nbb = 8 * wb, top = 8 * nw - 1;  // blocks per direction
   // block-normalised states start at sum 2^62: the forward state 1/4 scaled
   // by 2^62, the backward state 1 scaled by 2^60
   FState x;
@@ -511,10 +536,10 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
   x.p1 = x.p2 = 0x1p61f;
   x.k = bwd ? -60 : -62;
   uint32_t eacc = 0;  // OR of the blocks' range codes (fwd_norm)
-  if (bwd && (S & 7u)) {
-    const Parents pw = load_parents(p.haps, wn, q, (S - 1) >> 6);
+  if (bwd && (S & 63u)) {
+    const Parents pw = load_parents(p.haps, wn, q, nw);
 #pragma unroll 1
-    for (int m = (int)S - 1; m >= (int)(nb * 8); --m) {
+    for (int m = (int)S - 1; m >= (int)(nw * 64); --m) {
       const uint32_t j = (uint32_t)m & 63u;
       float s00, s01, s10, s11;
       select4(em.get1((uint32_t)m), (pw.f0 >> j) & 1, (pw.f1 >> j) & 1, (pw.m0 >> j) & 1,
@@ -525,51 +550,65 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
   }
   float4 *const stF = stage, *const stB = stage + kBwdOffF4;
   const StageRows rows = stage_rows<kMaxRows>(li, P);
-  auto issue = [&](uint32_t t) {
-    const uint32_t so = (t % kRing) * kSlotF4, m0 = t * 8;
-    stage8<kMaxRows>(stF + so, tran4 + m0, rows);
-    em.template stage<kMaxRows>(stF + so + 8, m0, rows);
-    if (t < nbk) {
-      const uint32_t n0 = (nb - 1 - t) * 8;
-      stage8_rev<kMaxRows>(stB + so, tran4 + n0 + 1, rows);
-      em.template stage_rev<kMaxRows>(stB + so + 8, n0, rows);
+  // block t0 + d of both directions into slot (t0 + d) mod 4: forward sites
+  // 8t .. 8t+7 with rows T_8t .., backward sites of block top - t reversed
+  // with the rows T_{m+1} of its sites m.  t0 is a multiple of 4 and d a
+  // constant, so the sources are base pointers of the quarter word plus
+  // constant offsets.
+  auto issue = [&](uint32_t t0, uint32_t d) {
+    const uint32_t t = t0 + d, slot = d & 3u;
+    if (t < nbf) {
+      stage8<kMaxRows>(stF + slot * kSlotF4, tran4 + 8 * (size_t)t0 + 8 * d, rows);
+      em.template stage<kMaxRows>(stF + slot * kSlotF4 + 8, t, rows);
     }
-  };
-  if (nf > 0)
-    issue(0);
-  cp_async_commit();
-  if (nf > 1)
-    issue(1);
-  cp_async_commit();
-  float4 *const mine = bwd ? stB : stF;
-  Parents pw = {0, 0, 0, 0};
-  uint32_t wcur = 0xffffffffu;
-#pragma unroll 1
-  for (uint32_t t = 0; t < nf; ++t) {
-    if (t + 2 < nf)
-      issue(t + 2);
+    if (t < nbb) {
+      stage8_rev<kMaxRows>(stB + slot * kSlotF4, tran4 + 8 * (size_t)(top - t0) + 1 - 8 * d,
+                           rows);
+      em.template stage_rev<kMaxRows>(stB + slot * kSlotF4 + 8, top - t, rows);
+    }
     cp_async_commit();
-    const bool act = !bwd || t < nbk;
-    const uint32_t blk = bwd ? nb - 1 - t : t;
-    const uint32_t w = blk >> 3;
-    if (act && w != wcur) {
-      wcur = w;
-      const Parents raw = load_parents(p.haps, wn, q, w);
-      pw = bwd ? reverse_parents(raw) : raw;
-      // next word of this lane's direction, if it holds one of its blocks
-      if (bwd ? (w * 8 > nf) : ((w + 1) * 8 < nf))
-        prefetch_parents(p.haps, wn, q, bwd ? w - 1 : w + 1);
+  };
+  issue(0, 0);
+  issue(0, 1);
+  float4 *const mine = bwd ? stB : stF;
+#pragma unroll 1
+  for (uint32_t i = 0; i < wf; ++i) {
+    const bool act = !bwd || i < wb;
+    const FState xs = x;
+    const uint32_t es = eacc;
+    const uint32_t w = bwd ? nw - 1 - i : i;
+    const Parents raw = load_parents(p.haps, wn, q, w);
+    const Parents pw = bwd ? reverse_parents(raw) : raw;
+    if (i + 1 < (bwd ? wb : wf))  // this lane's next word
+      prefetch_parents(p.haps, wn, q, bwd ? w - 1 : w + 1);
+#pragma unroll 1
+    for (uint32_t h = 0; h < 2; ++h) {
+      const uint32_t t0 = 8 * i + 4 * h;
+      const Bits32 bw = half_words(pw, h);
+#pragma unroll
+      for (uint32_t b = 0; b < 4; ++b) {
+        // One barrier a block: the slot staged here, (t + 2) mod 4, was last
+        // read at step t - 2, which every lane of the group finished before
+        // the barrier of step t - 1 let this one go on.
+        issue(t0, b + 2);
+        cp_async_wait<2>();
+        __syncwarp(gmask);
+        const float4 *slot = mine + b * kSlotF4;
+        switch (b) {  // bit positions 8b + j as constants
+          case 0: block8<0, E, kSub>(x, em, slot, em.block(slot + 8, bwd), bw, eacc); break;
+          case 1: block8<1, E, kSub>(x, em, slot, em.block(slot + 8, bwd), bw, eacc); break;
+          case 2: block8<2, E, kSub>(x, em, slot, em.block(slot + 8, bwd), bw, eacc); break;
+          default: block8<3, E, kSub>(x, em, slot, em.block(slot + 8, bwd), bw, eacc); break;
+        }
+      }
     }
-    const Bits8 xb = window8(pw, bwd ? 56u - 8u * (blk & 7u) : 8u * (blk & 7u));
-    cp_async_wait<2>();
-    __syncwarp(gmask);
-    const float4 *slot = mine + (t % kRing) * kSlotF4;
-    if (act)
-      block8<E, kSub>(x, em, slot, em.block(slot + 8, bwd), xb, eacc);
-    __syncwarp(gmask);
+    if (!act) {  // the odd lane's idle word
+      x = xs;
+      eacc = es;
+    }
   }
-  if (bwd)  // beta_{8 nf - 1} = T_{8 nf} v_{8 nf} (row S is the identity)
-    apply_tran(x, __ldg(tran4 + nf * 8));
+  if (bwd)  // beta_{64 wf - 1} = T_{64 wf} v_{64 wf} (row S is the identity)
+    apply_tran(x, __ldg(tran4 + 64 * (size_t)wf));
   const float y00 = __shfl_xor_sync(gmask, x.l00, 1), y01 = __shfl_xor_sync(gmask, x.l01, 1),
               y10 = __shfl_xor_sync(gmask, x.l10, 1), y11 = __shfl_xor_sync(gmask, x.l11, 1);
   const int yk = __shfl_xor_sync(gmask, x.k, 1);
@@ -577,7 +616,7 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
   // alpha . beta on both lanes: the same exact products in the same order
   const double dot = (double)x.l00 * (double)y00 + (double)x.l01 * (double)y01 +
                      (double)x.l10 * (double)y10 + (double)x.l11 * (double)y11;
-  double L = log(dot) + (double)(x.k + yk) * 0.69314718055994530942;
+  double L = log_scaled(dot, x.k + yk);
   if (__any_sync(gmask, bad != 0u)) {
     double Lf = L;
     if (bad && !bwd) {
@@ -1289,6 +1328,21 @@ __device__ __forceinline__ LaneGroups regroup(uint32_t lane, uint32_t na) {
   return g;
 }
 
+// The accept rule of MHSampler<T>::SampleHap (MHSampler.hpp:86-93) for a
+// uniform u in [0, 1) with 53-bit resolution: accept when prop >= curr or
+// u < exp((prop - curr) pen).  For d = (prop - curr) pen in (-37, 0) the
+// exponential is taken in binary32 (relative error below 3e-6: a decision can
+// differ from the binary64 one only where |d - ln u| < 3e-6); below -37 it
+// is under 2^-53, so only u = 0 accepts, as in binary64.
+__device__ __forceinline__ bool mh_accept(double prop, double curr, float pen, double u) {
+  if (prop >= curr)
+    return true;
+  const double d = (prop - curr) * (double)pen;
+  if (d > -37.0)
+    return u < (double)expf((float)d);
+  return u == 0.0 && u < exp(d);
+}
+
 template <int P, class E, class Src, int kSub = 1>
 __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counter,
                                                 unsigned long long *stats, int *error,
@@ -1452,8 +1506,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
     // same decisions as the sequential loop.  The even lanes vote.
     const double L0 = __shfl_sync(FULL, L, gbase);
     const double curr0 = (e == 0) ? L0 : curr;
-    const bool acc = lead_lane && r < k && ev > 0 &&
-                     (L >= curr0 || u < exp((L - curr0) * (double)p.pen));
+    const bool acc = lead_lane && r < k && ev > 0 && mh_accept(L, curr0, p.pen, u);
     const unsigned gmask = (Pc == 32) ? FULL : (((1u << Pc) - 1u) << gbase);
     const unsigned abal = __ballot_sync(FULL, acc) & gmask;
     const uint32_t srcl = abal ? (uint32_t)(__ffs(abal) - 1) : gbase;
@@ -1482,7 +1535,7 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       const uint32_t ph_r = __shfl_sync(FULL, phap, from);
       if (go) {
         last = r2;
-        if (L_r >= cur || u_r < exp((L_r - cur) * (double)p.pen)) {
+        if (mh_accept(L_r, cur, p.pen, u_r)) {
           cur = L_r;
           hap = ph_r;
           more |= 1u << r2;
