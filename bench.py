@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--generations", type=int, default=32, help="serving: generations/request")
     ap.add_argument("--budget-gb", type=float, default=180.0, help="serving: HBM budget")
     ap.add_argument("--serve-limit", type=float, default=600.0)
+    ap.add_argument("--no-vs-plain", action="store_true",
+                    help="skip the uneven-chunk batched-vs-plain leg of the default line")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the serving p50/p99 leg of the default line")
     return ap.parse_args()
 
 
@@ -81,6 +85,49 @@ def workload(args, rank):
     m, haps = synth.initial_state(ds, seed=7 + rank)
     workload.dataset = ds
     return w, m, haps
+
+
+def knn_k(w, args, H):
+    """Neighbours per haplotype of the configuration's kNN sampler, capped
+    at what H haplotypes allow (reduced test sizes); 0 = uniform sampler."""
+    if not w.knn or args.uniform:
+        return 0
+    return min(w.knn, (H - 2) // 2 * 2)
+
+
+def sampler_name(K):
+    if K:
+        return f"the K={K} nearest haplotypes by Hamming distance (KNN::ClusterHaps)"
+    return "uniform over all other haplotypes (UnifSampler)"
+
+
+def workload_config(args, w, N, S, C, H):
+    """The workload definition both arms report under `config` (the arms
+    differ in how they run it, which each line says outside `config`)."""
+    sampler = sampler_name(knn_k(w, args, H))
+    return {"workload": f"{args.config}: {N} samples x {S} sites x C={C} cycles per "
+                        f"generation, surrogates from {sampler}",
+            "samples": N, "sites": S, "cycles": C, "haplotypes": H, "sampler": sampler,
+            "emission": "vq4" if args.vq else "f32",
+            "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6)}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu; /proc/cpuinfo as a fallback)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 def accuracy(w, m, haps, ds, seed, device):
@@ -234,6 +281,7 @@ def cpu_baseline(m, haps, quad, props, C, pen, seconds, seed=1, gen=0):
     O.generation(pb, tr, quad, props, pen, 0, n1, True, nthreads=1)
     dt1 = time.perf_counter() - t0
     return {"value": ups, "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": f"{n2} of {m.N} samples of one generation (C={C}, S={m.S}), "
                       f"{dt:.1f} s on {threads} host threads",
             "single_thread_value": n1 * (C + 1) * m.S / dt1,
@@ -241,40 +289,65 @@ def cpu_baseline(m, haps, quad, props, C, pen, seconds, seed=1, gen=0):
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle port: impute.cpp's hmm_like and
+    hmm_work in their operation order, OpenMP over samples) on the same
+    workload and the same surrogate sampler as the GPU arm: for the kNN
+    configurations the neighbour table of the starting haplotypes is built by
+    the oracle's KNN::ClusterHaps restatement, and every generation draws its
+    surrogates from it with the GPU arm's counter-based streams.  The table
+    and the draws are set-up, outside the timed region."""
     world, rank, local = dist_env()
     if rank != 0:
         return
     w, m, haps = workload(args, 0)
     C = args.cycles
-    rng = np.random.default_rng(5)
-    from glphase_gb300 import synth
-    quad, props = synth.uniform_proposals(m.N, haps.shape[0], C, rng)
-    per_step = max(args.cpu_seconds / max(args.steps, 1), 1.0)
-    base, _ = cpu_baseline(m, haps, quad, props, C, 1.0, per_step)
+    N, S = m.N, m.S
+    H = haps.shape[0]
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
+    O.build(ref=False)
+    nbr, knn_s = None, None
+    K = knn_k(w, args, H)
+    if K:
+        t0 = time.perf_counter()
+        nbr = np.ascontiguousarray(O.knn(haps, S, K)[:N])
+        knn_s = time.perf_counter() - t0
+    seed = 1
+    q0, p0 = O.sample_surrogates(seed, 0, N, C, 0, H, nbr=nbr)
+    per_step = max(args.cpu_seconds / max(args.steps, 1), 1.0)
+    base, _ = cpu_baseline(m, haps, q0, p0, C, 1.0, per_step)
     threads = base["cores"]
     pb = O.OracleProblem(haps, m.emit, m.t, m.tran, m.pc, C)
     n = int(base["sample"].split()[0])
+
+    def gen(g, count):
+        quad, props = O.sample_surrogates(seed, g, N, C, 0, H, nbr=nbr)
+        return quad, props, pb.trace(seed=seed, generation=g), pen_for(g, w.burnin), count
+
     for g in range(args.warmup):
-        O.generation(pb, pb.trace(seed=1, generation=g), quad, props, pen_for(g, w.burnin), 0,
-                     min(n, 2 * threads), True, nthreads=threads)
-    t0 = time.perf_counter()
-    for g in range(args.steps):
-        O.generation(pb, pb.trace(seed=1, generation=args.warmup + g), quad, props,
-                     pen_for(args.warmup + g, w.burnin), 0, n, True, nthreads=threads)
-    dt = time.perf_counter() - t0
-    value = args.steps * n * (C + 1) * m.S / dt
+        quad, props, tr, pen, cnt = gen(g, min(n, 2 * threads))
+        O.generation(pb, tr, quad, props, pen, 0, cnt, True, nthreads=threads)
+    dt = 0.0
+    for i in range(args.steps):
+        quad, props, tr, pen, cnt = gen(args.warmup + i, n)
+        t0 = time.perf_counter()
+        O.generation(pb, tr, quad, props, pen, 0, cnt, True, nthreads=threads)
+        dt += time.perf_counter() - t0
+    value = args.steps * n * (C + 1) * S / dt
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"{args.config}: {m.N} samples x {m.S} sites, C={C}",
-                   "samples": m.N, "sites": m.S, "cycles": C,
-                   "sampler": "uniform over all other haplotypes"},
+        "config": workload_config(args, w, N, S, C, H),
+        "reference_path": "oracle port of the reference CPU path (impute.cpp:327-485, "
+                          "MHSampler.hpp:81-96), all host threads; surrogate table "
+                          + ("built by the oracle's KNN::ClusterHaps in %.1f s, " % knn_s
+                             if knn_s is not None else "")
+                          + "draws per generation outside the timed region",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} of {m.N} samples per step, {args.steps} steps",
+                         "cpu_model": base["cpu_model"],
+                         "sample": f"{n} of {N} samples per step, {args.steps} steps",
                          "single_thread_value": base["single_thread_value"],
                          "single_thread_sample": base["single_thread_sample"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -311,11 +384,12 @@ def run_ours(args):
     # (KNN::ClusterHaps) computed once on the device from the starting
     # haplotypes; every generation then draws its surrogates in the kernel
     nbr, knn_ms = None, None
-    if w.knn and not args.uniform:
+    K = knn_k(w, args, H)
+    if K:
         k0 = torch.cuda.Event(enable_timing=True)
         k1 = torch.cuda.Event(enable_timing=True)
         k0.record(eng.stream)
-        nbr = eng.knn(w.knn)
+        nbr = eng.knn(K)
         k1.record(eng.stream)
         eng.finish()
         knn_ms = k0.elapsed_time(k1)
@@ -377,21 +451,21 @@ def run_ours(args):
         # the same surrogates the kernel draws, at full penalty
         q0, p0 = surrogates(seed, args.warmup, N, C, H, nbr_host)
         base, _ = cpu_baseline(m, haps, q0, p0, C, 1.0, args.cpu_seconds)
-    sampler = (f"kNN K={w.knn} nearest by Hamming distance, device-built once "
-               f"({knn_ms:.1f} ms), drawn in-kernel" if nbr is not None
-               else "uniform over all other haplotypes, drawn in-kernel")
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
 
     if rank == 0:
+        sm_mhz = ck.get("sm_mhz")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {
-                "workload": f"{args.config}: {N} samples x {S} sites x C={C} cycles per "
-                            f"generation, surrogates {sampler}",
-                "samples": N, "sites": S, "cycles": C, "haplotypes": H,
-                "emission": "vq4" if args.vq else "f32",
+            "config": workload_config(args, w, N, S, C, H),
+            "surrogates": ("neighbour table built once on the device from the starting "
+                           f"haplotypes ({knn_ms:.1f} ms), drawn in the kernel"
+                           if nbr is not None else "drawn in the kernel"),
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+            "speculation": {
                 "lanes_per_sample": lanes,
                 "positions_per_round": lanes // 2,
                 "evaluations_per_step": ev,
@@ -402,16 +476,20 @@ def run_ours(args):
                 # lane-pair rounds run per counted evaluation: above 1 by the
                 # pairs of a chain's last round that score past its end
                 "pair_rounds_per_evaluation": round(cnt[5] / 2 / max(cnt[0], 1), 4),
-                "useful_fraction": round(N * (C + 1) / max(ev, 1), 4),
-                "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6),
-                "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+                "useful_fraction": round(N * (C + 1) / max(ev, 1), 4)},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value,
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
                          "traffic": traffic_per_launch(N, S, C, args),
-                         "note": "29 algorithmic FP32 flops per update; peak = measured FP32 "
-                                 "FMA rate on this GPU (glp_measure_fp32_peak); traffic = "
-                                 "DRAM bytes per launch from one ncu capture at S=1024 scaled "
-                                 "by S (profiles/generation_kernel_10000x1024_full.md)"},
+                         "peak_basis": {
+                             "sms": sm_count, "sm_mhz_median": sm_mhz,
+                             "fp32_lanes_per_sm": 128,
+                             "lanes_x_sms_x_2_x_clock_tflops":
+                                 128 * sm_count * 2 * sm_mhz * 1e6 / 1e12 if sm_mhz else None},
+                         "note": "29 algorithmic FP32 flops per update over the generation "
+                                 "kernel's CUDA-event time; peak = FP32 FMA rate measured on "
+                                 "this GPU (glp_measure_fp32_peak, dependent-free FMA chains on "
+                                 "every SM); traffic = DRAM bytes per launch from one ncu "
+                                 "capture at S=1024 scaled by S"},
             "roofline_hbm": hbm_roofline(N, S, H, wn, kernel_ms, traffic_per_launch(N, S, C, args),
                                          args),
             "clocks": ck,
@@ -426,6 +504,25 @@ def run_ours(args):
             line["cpu_baseline"] = base
         if not args.no_accuracy:
             line["accuracy"] = accuracy(w, m, haps, workload.dataset, seed, local)
+        if world == 1 and args.config == "batched" and not (args.no_vs_plain and args.no_serve):
+            # the metric's other halves, on the same GPU after the main leg:
+            # batched vs plain GPU form on the uneven chunks, p50/p99 serving
+            del eng
+            torch.cuda.empty_cache()
+            if not args.no_vs_plain:
+                line["vs_plain"], _ = measure_uneven(args, 4, 2)
+            if not args.no_serve:
+                sv = measure_serve(args, ((1.0, False, False), (1.0, True, False)))
+                b1, p1 = sv["results"]["batched@1.0x"], sv["results"]["plain@1.0x"]
+                line["serving"] = {
+                    "p50_latency_s": b1["p50_latency_s"], "p99_latency_s": b1["p99_latency_s"],
+                    "updates_per_s": b1["updates_per_s"], "load": "1x measured capacity",
+                    "plain_p50_latency_s": p1["p50_latency_s"],
+                    "plain_p99_latency_s": p1["p99_latency_s"],
+                    "plain_updates_per_s": p1["updates_per_s"],
+                    "batched_over_plain": b1["updates_per_s"] / max(p1["updates_per_s"], 1e-9),
+                    **{k: sv[k] for k in ("workload", "capacity_updates_per_s",
+                                          "capacity_requests_per_s")}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -481,9 +578,10 @@ def uneven_shapes(n_chunks, seed=4, scale=1.0):
     return [(int(n), int(s)) for n, s in zip(N, S)]
 
 
-def run_uneven(args):
+def measure_uneven(args, steps, warmup):
     """Batched (one persistent launch per generation, replayed CUDA graph)
-    vs plain (one launch per chunk) on the uneven-chunk workload."""
+    vs plain (one launch per chunk) on the uneven-chunk workload; returns the
+    measurements and the clock record of the batched leg."""
     import torch
     from glphase_gb300 import synth, synth_device as sd
     from glphase_gb300.batch import DeviceProblem, PreparedBatch
@@ -505,11 +603,11 @@ def run_uneven(args):
     setup_s = time.perf_counter() - t0
     upd = sum(N * (C + 1) * S for N, S in shapes)
 
-    def timed(fn, steps):
+    def timed(fn, n):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(steps):
+        for _ in range(n):
             fn()
         e1.record(stream)
         e1.synchronize()
@@ -517,12 +615,12 @@ def run_uneven(args):
         return e0.elapsed_time(e1) / 1e3
 
     batch = PreparedBatch(dev, probs, generation=0)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.run()
     dev._c(dev.L.glp_finish(dev.ctx))
     clocks = ClockSampler(0)
     clocks.start()
-    t_batched = timed(batch.run, args.steps)
+    t_batched = timed(batch.run, steps)
     ck = clocks.stop()
     _, _, lanes_b = dev.stats()
     cnt_b = dev.counters()
@@ -531,45 +629,54 @@ def run_uneven(args):
     singles = [PreparedBatch(dev, [p], generation=gen) for p in probs]
 
     def plain():
-        for s in singles:
-            s.run(graph=False)
+        for sg in singles:
+            sg.run(graph=False)
     plain()
     dev._c(dev.L.glp_finish(dev.ctx))
-    t_plain = timed(plain, args.steps)
-    for s in singles:
-        s.close()
-    v_b = args.steps * upd / t_batched
-    v_p = args.steps * upd / t_plain
+    t_plain = timed(plain, steps)
+    for sg in singles:
+        sg.close()
+    for p in probs:
+        p.close()
+    dev.cleanup()
+    v_b = steps * upd / t_batched
+    v_p = steps * upd / t_plain
+    res = {"workload": f"uneven: {len(shapes)} chunks, sites U{{512..16384}}/64, "
+                       f"samples U{{100..5000}}" + (f" scaled by {args.scale}" if args.scale != 1 else "")
+                       + f", C={C}, own seed/founders/map each",
+           "chunks": len(shapes), "samples_total": int(sum(n for n, _ in shapes)),
+           "updates_per_step": upd, "steps": steps, "warmup": warmup,
+           "setup_s": round(setup_s, 1),
+           "batched": v_b, "plain": v_p, "ratio": v_b / v_p,
+           "batched_ms_per_step": t_batched / steps * 1e3,
+           "plain_ms_per_step": t_plain / steps * 1e3,
+           "lanes_per_sample": lanes_b,
+           "accept_rate": round(cnt_b[2] / max(cnt_b[1], 1), 4),
+           "useful_fraction": round(sum(N for N, _ in shapes) * (C + 1) / max(cnt_b[0], 1), 4),
+           "form": "batched = one persistent launch per generation replayed from a captured "
+                   "CUDA graph; plain = one launch per chunk"}
+    return res, ck
+
+
+def run_uneven(args):
+    """The uneven-chunk configuration as its own line."""
+    res, ck = measure_uneven(args, args.steps, args.warmup)
     line = {
-        "metric": METRIC, "value": v_b, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_batched / args.steps * 1e3,
+        "metric": METRIC, "value": res["batched"], "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["batched_ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": f"uneven: {len(shapes)} chunks, sites U{{512..16384}}/64, "
-                               f"samples U{{100..5000}}, C={C}, own seed/founders/map each",
-                   "chunks": len(shapes), "samples_total": int(sum(n for n, _ in shapes)),
-                   "updates_per_step": upd, "setup_s": round(setup_s, 1),
-                   "lanes_per_sample": lanes_b,
-                   "accept_rate": round(cnt_b[2] / max(cnt_b[1], 1), 4),
-                   "useful_fraction": round(sum(N for N, _ in shapes) * (C + 1)
-                                            / max(cnt_b[0], 1), 4),
-                   "pair_rounds_per_evaluation": round(cnt_b[5] / 2 / max(cnt_b[0], 1), 4),
-                   "plain_value": v_p, "plain_ms_per_step": t_plain / args.steps * 1e3,
-                   "batched_over_plain": v_b / v_p,
-                   "form": "batched = one persistent launch per generation replayed from a "
-                           "captured CUDA graph; plain = one launch per chunk"},
+        "data": "synthetic", "config": {"workload": res["workload"]}, "vs_plain": res,
         "clocks": ck, "gpu_launches": 4 * args.steps,
     }
     print(json.dumps(line), flush=True)
-    for p in probs:
-        p.close()
 
 
-def run_serve(args):
-    """Poisson-arriving phasing requests (uneven-chunk shapes, 32 generations
-    each) served with continuous batching at 0.5x, 1x and 2x the measured
-    capacity; the plain form (one launch per resident request per tick) and
-    the library's own serving loop (glp_server_*) at 1x beside it."""
+def measure_serve(args, legs):
+    """Poisson-arriving phasing requests (uneven-chunk shapes, G generations
+    each) served with continuous batching.  legs: (load, plain, native)
+    triples -- load in multiples of the measured capacity, plain = one launch
+    per resident request per tick, native = the library's own loop
+    (glp_server_*).  Returns per-leg summaries and the capacity."""
     import torch
     from glphase_gb300 import synth, synth_device as sd
     from glphase_gb300.hmmlike import HMMLikeCUDA
@@ -588,7 +695,7 @@ def run_serve(args):
         return Request(rid=i, chunk=sd.generate(w, N, S, seed=300 + i), generations=G,
                        cycles=C, seed=9000 + i, burnin=8)
 
-    # capacity: saturated throughput of all requests resident at once
+    # capacity: saturated throughput of 8 requests resident at once
     reqs = [make(i, N, S) for i, (N, S) in enumerate(shapes)]
     mean_updates = float(np.mean([r.updates for r in reqs]))
     cal = Server(dev, budget)
@@ -601,9 +708,9 @@ def run_serve(args):
     per_gen = sum(r.chunk.N * (C + 1) * r.chunk.S for r in reqs[:8])
     capacity_ups = per_gen / (time.perf_counter() - t0)
     capacity_rps = capacity_ups / mean_updates
+    del reqs, cal
     results = {}
-    for load, plain, native in ((0.5, False, False), (1.0, False, False), (2.0, False, False),
-                                (1.0, True, False), (1.0, False, True)):
+    for load, plain, native in legs:
         rng = np.random.default_rng(int(load * 100) + plain)
         gaps = rng.exponential(1.0 / (load * capacity_rps), size=len(shapes))
         reqs = [make(i, N, S) for i, (N, S) in enumerate(shapes)]
@@ -618,19 +725,29 @@ def run_serve(args):
         results[key] = st.summary()
         del reqs, srv
         torch.cuda.empty_cache()
-    b1, p1 = results["batched@1.0x"], results["plain@1.0x"]
+    dev.cleanup()
+    return {"workload": f"serving: {len(shapes)} Poisson-arriving requests, uneven-chunk "
+                        f"shapes" + (f" scaled by {args.scale}" if args.scale != 1 else "")
+                        + f", {G} generations each, C={C}, panel off",
+            "hbm_budget_gb": args.budget_gb, "capacity_updates_per_s": capacity_ups,
+            "capacity_requests_per_s": capacity_rps, "results": results}
+
+
+def run_serve(args):
+    """Serving at 0.5x, 1x and 2x the measured capacity; the plain form and
+    the library's own serving loop at 1x beside it."""
+    res = measure_serve(args, ((0.5, False, False), (1.0, False, False), (2.0, False, False),
+                               (1.0, True, False), (1.0, False, True)))
+    r = res["results"]
+    b1, p1 = r["batched@1.0x"], r["plain@1.0x"]
+    res["batched_over_plain_at_1x"] = b1["updates_per_s"] / p1["updates_per_s"]
+    res["native_over_python_loop_at_1x"] = r["native@1.0x"]["updates_per_s"] / b1["updates_per_s"]
     line = {
         "metric": "serving: p50/p99 request latency and site-updates/s", "value":
-            b1["updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": len(shapes),
+            b1["updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": args.requests,
         "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"serving: {len(shapes)} Poisson-arriving requests, uneven-chunk "
-                               f"shapes, {G} generations each, C={C}, panel off",
-                   "hbm_budget_gb": args.budget_gb, "capacity_updates_per_s": capacity_ups,
-                   "capacity_requests_per_s": capacity_rps, "results": results,
-                   "batched_over_plain_at_1x": b1["updates_per_s"] / p1["updates_per_s"],
-                   "native_over_python_loop_at_1x":
-                       results["native@1.0x"]["updates_per_s"] / b1["updates_per_s"]},
+        "dtype": "f32", "data": "synthetic", "config": {"workload": res["workload"]},
+        "serving": res,
     }
     print(json.dumps(line), flush=True)
 

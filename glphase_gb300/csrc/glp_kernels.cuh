@@ -520,10 +520,13 @@ __device__ __forceinline__ double log_scaled(double dot, int k) {
 // gmask names the lanes that synchronise at each step (the group, or the
 // whole warp when every group runs the same loop).  tran4 holds S + 1 rows,
 // rows 0 and S the identity.
-template <int kMaxRows, class E, int kSub = 1>
+// kFull: every lane of the warp takes part (gmask is the full mask, known to
+// the compiler).
+template <int kMaxRows, class E, int kSub = 1, bool kFull = false>
 __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uint4 q,
                                             float4 *stage, uint32_t li, uint32_t P,
-                                            unsigned gmask) {
+                                            unsigned gmask_in) {
+  const unsigned gmask = kFull ? 0xffffffffu : gmask_in;
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tran4 = p.tran4;
   const bool bwd = (li & 1u) != 0;
@@ -1494,7 +1497,9 @@ __device__ __forceinline__ void generation_body(const Src &src, uint32_t *counte
       em.init(p, s, Src::kMulti ? p.vq_table : vq_smem);
       const unsigned gm = (Pc == 32 || warp_lockstep) ? FULL : (((1u << Pc) - 1u) << gbase);
       float4 *ring = glp_stage + ((size_t)warp * G0 + gidx) * kGroupStrideF4;
-      L = eval_pair<(P >= 8 ? 1 : 8 / P), E, kSub>(p, em, myq, ring, li, Pc, gm);
+      L = (gm == FULL)
+              ? eval_pair<(P >= 8 ? 1 : 8 / P), E, kSub, true>(p, em, myq, ring, li, Pc, gm)
+              : eval_pair<(P >= 8 ? 1 : 8 / P), E, kSub, false>(p, em, myq, ring, li, Pc, gm);
       if (r >= k)
         L = 0.0;
     }

@@ -4,6 +4,14 @@
 // (src/hmmLike.cpp, Insti::cudaSolve) includes this header instead of
 // hmmLike.h and links libglphase_gpu.so; nothing else changes.
 //
+// Two ways to use it:
+//  * include it in place of hmmLike.h: the functions are inline;
+//  * keep the reference's own hmmLike.h (it declares the functions extern)
+//    and compile ONE translation unit that defines HMMLIKE_CUDA_SHIM_OUT_OF_LINE
+//    before including this header: it then defines the functions with external
+//    linkage, so src/hmmLike.cpp compiles unchanged and links against them in
+//    place of hmmLike.cu.
+//
 // Status codes become std::runtime_error, the reference's own convention for
 // size errors (src/hmmLike.cu:333-336, 409-414); unlike the reference, CUDA
 // errors no longer call exit().  One context per process, as the reference's
@@ -21,6 +29,12 @@
 #include "glphase_gpu.h"
 
 static_assert(sizeof(unsigned) == sizeof(uint32_t), "unsigned must be 32 bits");
+
+#ifdef HMMLIKE_CUDA_SHIM_OUT_OF_LINE
+#define HMMLIKE_CUDA_SHIM_FN
+#else
+#define HMMLIKE_CUDA_SHIM_FN inline
+#endif
 
 namespace HMMLikeCUDA {
 
@@ -42,14 +56,14 @@ inline glp_ctx *need() {
 }  // namespace detail
 
 // src/hmmLike.cu:266-320
-inline void CheckDevice() {
+HMMLIKE_CUDA_SHIM_FN void CheckDevice() {
   int n = 0, ma = 0, mi = 0, sms = 0;
   if (glp_check_device(0, &n, &ma, &mi, &sms) != GLP_OK)
     throw std::runtime_error("[HMMLikeCUDA] no sm_103 device found");
 }
 
 // src/hmmLike.cu:244-264
-inline void SetDevice(int devID) {
+HMMLIKE_CUDA_SHIM_FN void SetDevice(int devID) {
   if (detail::context()) {
     glp_destroy(detail::context());
     detail::context() = 0;
@@ -58,7 +72,7 @@ inline void SetDevice(int devID) {
 }
 
 // src/hmmLike.cu:322-337
-inline void CopyTranToDevice(const std::vector<float> &tran) {
+HMMLIKE_CUDA_SHIM_FN void CopyTranToDevice(const std::vector<float> &tran) {
   if (tran.size() % 3)
     throw std::runtime_error("[HMMLikeCUDA] tran size is not a multiple of 3");
   detail::check(glp_set_tran(detail::need(), tran.data(), (uint32_t)(tran.size() / 3)),
@@ -66,19 +80,19 @@ inline void CopyTranToDevice(const std::vector<float> &tran) {
 }
 
 // src/hmmLike.cu:339-355
-inline void CopyMutationMatToDevice(const float (*mutMat)[4][4]) {
+HMMLIKE_CUDA_SHIM_FN void CopyMutationMatToDevice(const float (*mutMat)[4][4]) {
   detail::check(glp_set_mutation_mat(detail::need(), &(*mutMat)[0][0]),
                 "CopyMutationMatToDevice");
 }
 
 // src/hmmLike.cu:357-366
-inline void CopyPackedGLsToDevice(const std::vector<uint32_t> &packedGLs) {
+HMMLIKE_CUDA_SHIM_FN void CopyPackedGLsToDevice(const std::vector<uint32_t> &packedGLs) {
   detail::check(glp_set_packed_gls(detail::need(), packedGLs.data(), packedGLs.size()),
                 "CopyPackedGLsToDevice");
 }
 
 // src/hmmLike.cu:368-383
-inline void CopyCodeBookToDevice(const std::vector<std::pair<float, float> > &codeBook) {
+HMMLIKE_CUDA_SHIM_FN void CopyCodeBookToDevice(const std::vector<std::pair<float, float> > &codeBook) {
   std::vector<float> flat;
   flat.reserve(codeBook.size() * 2);
   for (size_t i = 0; i < codeBook.size(); ++i) {
@@ -90,7 +104,7 @@ inline void CopyCodeBookToDevice(const std::vector<std::pair<float, float> > &co
 }
 
 // src/hmmLike.cu:399-572
-inline void RunHMMOnDevice(const std::vector<uint64_t> &hapPanel,
+HMMLIKE_CUDA_SHIM_FN void RunHMMOnDevice(const std::vector<uint64_t> &hapPanel,
                            const std::vector<unsigned> &extraPropHaps, unsigned numSites,
                            unsigned numSamples, unsigned numCycles,
                            std::vector<unsigned> &hapIdxs, unsigned long seed) {
@@ -104,7 +118,7 @@ inline void RunHMMOnDevice(const std::vector<uint64_t> &hapPanel,
 }
 
 // src/hmmLike.cu:385-397 (without the device reset)
-inline void Cleanup() {
+HMMLIKE_CUDA_SHIM_FN void Cleanup() {
   if (detail::context()) {
     glp_destroy(detail::context());
     detail::context() = 0;
