@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the untimed full-schedule phasing accuracy run")
+    ap.add_argument("--recluster", type=int, default=0,
+                    help="kNN configurations: rebuild the neighbour table from the current "
+                         "haplotypes every R generations after burn-in, inside the timed "
+                         "steps (the reference's -r; 0 = its default, never)")
     ap.add_argument("--uniform", action="store_true",
                     help="uniform surrogates instead of the configuration's kNN restriction")
     ap.add_argument("--chunks", type=int, default=64, help="uneven workload: chunk count")
@@ -105,9 +109,13 @@ def workload_config(args, w, N, S, C, H):
     """The workload definition both arms report under `config` (the arms
     differ in how they run it, which each line says outside `config`)."""
     sampler = sampler_name(knn_k(w, args, H))
+    K = knn_k(w, args, H)
+    rc = (f", rebuilt from the current haplotypes every {args.recluster} generations after "
+          f"burn-in" if K and args.recluster else "")
     return {"workload": f"{args.config}: {N} samples x {S} sites x C={C} cycles per "
-                        f"generation, surrogates from {sampler}",
+                        f"generation, surrogates from {sampler}{rc}",
             "samples": N, "sites": S, "cycles": C, "haplotypes": H, "sampler": sampler,
+            "recluster_every": args.recluster if K else 0,
             "emission": "vq4" if args.vq else "f32",
             "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6)}
 
@@ -130,7 +138,7 @@ def cpu_model():
     return "unknown"
 
 
-def accuracy(w, m, haps, ds, seed, device):
+def accuracy(w, m, haps, ds, seed, device, recluster=0):
     """Phasing accuracy of the workload's full schedule (burn-in + sampling
     generations, the configuration's surrogate sampler, device tallies and
     result; glphase_gb300.phase): NRD of the called genotypes against the
@@ -139,7 +147,7 @@ def accuracy(w, m, haps, ds, seed, device):
     from glphase_gb300 import io as gio, phase as ph
     N = m.N
     opts = ph.PhaseOptions(sa_burnin=w.burnin, burnin=0, sampling=w.sampling, cycles=w.cycles,
-                           seed=seed, knn=w.knn, cluster_start=0,
+                           seed=seed, knn=w.knn, cluster_start=0, recluster=recluster,
                            kick_start=bool(w.panel_haps), kick_first=bool(w.panel_haps),
                            device=device)
     prob, _ = ph.phase(m, haps, opts)
@@ -324,12 +332,20 @@ def run_reference(args):
         quad, props = O.sample_surrogates(seed, g, N, C, 0, H, nbr=nbr)
         return quad, props, pb.trace(seed=seed, generation=g), pen_for(g, w.burnin), count
 
+    def rebuild(g):
+        return K and args.recluster and g > w.burnin and (g - w.burnin) % args.recluster == 0
+
     for g in range(args.warmup):
         quad, props, tr, pen, cnt = gen(g, min(n, 2 * threads))
         O.generation(pb, tr, quad, props, pen, 0, cnt, True, nthreads=threads)
     dt = 0.0
     for i in range(args.steps):
-        quad, props, tr, pen, cnt = gen(args.warmup + i, n)
+        g = args.warmup + i
+        t0 = time.perf_counter()
+        if rebuild(g):  # KNN::ClusterHaps on the haplotypes, as the timed GPU step does
+            nbr = np.ascontiguousarray(O.knn(haps, S, K)[:N])
+        dt += time.perf_counter() - t0
+        quad, props, tr, pen, cnt = gen(g, n)
         t0 = time.perf_counter()
         O.generation(pb, tr, quad, props, pen, 0, cnt, True, nthreads=threads)
         dt += time.perf_counter() - t0
@@ -344,7 +360,8 @@ def run_reference(args):
                           "MHSampler.hpp:81-96), all host threads; surrogate table "
                           + ("built by the oracle's KNN::ClusterHaps in %.1f s, " % knn_s
                              if knn_s is not None else "")
-                          + "draws per generation outside the timed region",
+                          + "draws per generation outside the timed region"
+                          + (", rebuilds of the table inside it" if K and args.recluster else ""),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "cpu_model": base["cpu_model"],
                          "sample": f"{n} of {N} samples per step, {args.steps} steps",
@@ -398,7 +415,14 @@ def run_ours(args):
     stream = eng.stream
     seed = replicas.plan(w.seed, rank=rank, world=max(world, rank + 1)).rng_seed
 
+    rebuilds = [0]
+
     def step(g):
+        nonlocal nbr
+        if nbr is not None and args.recluster and g > w.burnin and \
+                (g - w.burnin) % args.recluster == 0:
+            nbr = eng.knn(K)  # from the current haplotypes, on the engine's stream
+            rebuilds[0] += 1
         a = eng.args(None, None, pen_for(g, w.burnin), seed=seed, generation=g, neighbors=nbr)
         if w.panel_haps and g == 0:
             # the first generation draws its surrogates from the panel only
@@ -409,6 +433,7 @@ def run_ours(args):
     for g in range(args.warmup):
         step(g)
     eng.finish()
+    rebuilds[0] = 0
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.4)
@@ -493,7 +518,7 @@ def run_ours(args):
             "roofline_hbm": hbm_roofline(N, S, H, wn, kernel_ms, traffic_per_launch(N, S, C, args),
                                          args),
             "clocks": ck,
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": 3 * args.steps + 2 * rebuilds[0],
             "step_ms": step_ms,
             "kernel_ms": kernel_ms,
             "hmm_work_ms": work_ms,
@@ -503,7 +528,8 @@ def run_ours(args):
         if base:
             line["cpu_baseline"] = base
         if not args.no_accuracy:
-            line["accuracy"] = accuracy(w, m, haps, workload.dataset, seed, local)
+            line["accuracy"] = accuracy(w, m, haps, workload.dataset, seed, local,
+                                        args.recluster)
         if world == 1 and args.config == "batched" and not (args.no_vs_plain and args.no_serve):
             # the metric's other halves, on the same GPU after the main leg:
             # batched vs plain GPU form on the uneven chunks, p50/p99 serving

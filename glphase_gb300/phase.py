@@ -16,7 +16,12 @@ the final probabilities and haplotypes come back.
 The surrogate sampler is uniform over all other haplotypes
 (``UnifSampler``), or, from generation ``cluster_start`` on, the K nearest
 haplotypes by Hamming distance built on the device from the haplotypes of
-that generation (``KNN``, kNN.cpp:99-206).  With reference-panel rows after
+that generation (``KNN``, kNN.cpp:99-206); with ``recluster`` = r > 0 the
+table is rebuilt from the current haplotypes at every generation g > B + I
+with (g - B - I) mod r = 0 (the reference's ``-r``, insti.cpp:1675-1684).
+The reference builds its first table from a pre-phased scaffold
+(insti.cpp:1576-1586); without one, the first table here comes from the
+haplotypes of generation ``cluster_start``.  With reference-panel rows after
 the 2N sample haplotypes, ``kick_start`` draws generation 0's surrogates
 from the panel only (the README's kick-start) and ``kick_first`` every
 chain's first proposal in every generation (the code's ``--kickstart``,
@@ -43,6 +48,7 @@ class PhaseOptions:
     seed: int = 1             # seeds the device's counter-based draws
     knn: int = 0              # K nearest-neighbour surrogates (0: uniform)
     cluster_start: int = 0    # generation from which the kNN sampler is used
+    recluster: int = 0        # -r: rebuild the kNN table every r generations after burn-in
     lanes: int = 0            # speculation width (0: chosen per generation)
     kick_start: bool = False  # generation 0 draws its surrogates from the panel rows only
     kick_first: bool = False  # every chain's first proposal from the panel (--kickstart)
@@ -51,6 +57,22 @@ class PhaseOptions:
     @property
     def generations(self) -> int:
         return self.sa_burnin + self.burnin + self.sampling
+
+
+def knn_builds(opts: PhaseOptions) -> list[int]:
+    """Generations at whose start the kNN table is built from the current
+    haplotypes: every g > bn with (g - bn) mod r = 0 for bn = B + I and r =
+    ``recluster`` (insti.cpp:1675-1677: not at bn itself), and
+    ``cluster_start`` when no table exists by then."""
+    if not opts.knn:
+        return []
+    bn = opts.sa_burnin + opts.burnin
+    out = []
+    for g in range(opts.generations):
+        rebuild = opts.recluster > 0 and g > bn and (g - bn) % opts.recluster == 0
+        if rebuild or (g >= opts.cluster_start and not out):
+            out.append(g)
+    return out
 
 
 def phase(model: mdl.Model, haps: np.ndarray, opts: PhaseOptions):
@@ -68,10 +90,13 @@ def phase(model: mdl.Model, haps: np.ndarray, opts: PhaseOptions):
     prob = torch.zeros(2 * N * S, dtype=torch.float32, device=eng.device)
     torch.cuda.current_stream(eng.device).synchronize()
     tallied_from = opts.sa_burnin + opts.burnin
-    nbr = None
+    builds = set(knn_builds(opts))
+    nbr = table = None
     for g in range(opts.generations):
-        if opts.knn and nbr is None and g >= opts.cluster_start:
-            nbr = eng.knn(opts.knn)
+        if g in builds:
+            table = eng.knn(opts.knn)
+        # the table is the sampler from cluster_start on
+        nbr = table if opts.knn and g >= opts.cluster_start else None
         pen = float(anneal_pen(g, opts.sa_burnin))
         a = eng.args(None, None, pen, opts.seed, g, neighbors=nbr,
                      kick_first=opts.kick_first and eng.H > 2 * N)

@@ -120,3 +120,21 @@ def test_panel_phasing_matches_oracle(oracle_lib, kick):
     want_prob, want_haps = oracle_phase(oracle_lib, m, haps, opts)
     assert np.array_equal(final, want_haps)
     assert np.array_equal(prob, want_prob)
+
+
+def test_knn_recluster_matches_oracle(oracle_lib):
+    """The kNN sampler (K = 40 from generation 3) rebuilt from the current
+    haplotypes every 2 generations after the 10 burn-in generations (the
+    reference's -r, insti.cpp:1675-1684): the device loop -- device-built
+    tables, in-kernel draws -- equals the oracle loop with the oracle's
+    KNN::ClusterHaps restatement bit for bit."""
+    from phase_oracle import oracle_phase
+    ds, pos, gmap, truth = cohort()
+    opts = ph.PhaseOptions(sa_burnin=5, burnin=5, sampling=12, cycles=60, seed=3, knn=40,
+                           cluster_start=3, recluster=2)
+    assert ph.knn_builds(opts) == [3, 12, 14, 16, 18, 20]
+    m, haps = ph.prepare(ds.gl_het_alt, pos, gmap, seed=opts.seed)
+    prob, final = ph.phase(m, haps, opts)
+    want_prob, want_haps = oracle_phase(oracle_lib, m, haps, opts)
+    assert np.array_equal(final, want_haps)
+    assert np.array_equal(prob, want_prob)
