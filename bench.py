@@ -162,16 +162,16 @@ def accuracy(w, m, haps, ds, seed, device, recluster=0):
 
 
 # DRAM bytes (read + write) of one generation_kernel launch measured by ncu on
-# the batched workload at S = 1,024 (N = 10,000, C = 100, 8 lanes, float
-# emission); the traffic grows in proportion to S (emission rows per scored
-# site), so the full-size figure is this one scaled by S / 1,024.
-NCU_TRAFFIC_S1024 = 1.426213e9 + 0.003265e9
+# the batched workload itself (N = 10,000, S = 4,096, C = 100, 8 lanes, float
+# emission), one launch, no scaling: every speculative round streams its
+# sample's emission row again, mostly from DRAM.
+NCU_TRAFFIC_BATCHED = 18.750250240e9 + 0.004036096e9
 
 
 def traffic_per_launch(N, S, C, args):
-    if N != 10000 or C != 100 or args.vq or args.config != "batched":
+    if (N, S, C) != (10000, 4096, 100) or args.vq or args.config != "batched":
         return None
-    return NCU_TRAFFIC_S1024 * S / 1024
+    return NCU_TRAFFIC_BATCHED
 
 
 def hbm_roofline(N, S, H, wn, kernel_ms, traffic, args):
@@ -194,10 +194,16 @@ def hbm_roofline(N, S, H, wn, kernel_ms, traffic, args):
         src = "measured"
     algo = N * S * 16 + H * wn * 8
     achieved = algo / (kernel_ms * 1e-3) / 1e9
-    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": traffic,
-            "note": f"compulsory bytes {algo} per launch; peak = {src} HBM copy bandwidth; "
-                    "far below it: the kernel is bound by FP32 issue (roofline)"}
+    out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "traffic": traffic,
+           "note": f"achieved = compulsory bytes ({algo} per launch) over the kernel time; "
+                   f"peak = {src} HBM copy bandwidth; traffic = measured DRAM bytes of one "
+                   "launch (every speculative round streams its sample's emission row "
+                   "again); the kernel is bound by instruction issue (roofline)"}
+    if traffic:
+        out["traffic_gbs"] = traffic / (kernel_ms * 1e-3) / 1e9
+        out["traffic_frac"] = out["traffic_gbs"] / peak
+    return out
 
 
 def pen_for(gen, burnin):
@@ -513,8 +519,8 @@ def run_ours(args):
                          "note": "29 algorithmic FP32 flops per update over the generation "
                                  "kernel's CUDA-event time; peak = FP32 FMA rate measured on "
                                  "this GPU (glp_measure_fp32_peak, dependent-free FMA chains on "
-                                 "every SM); traffic = DRAM bytes per launch from one ncu "
-                                 "capture at S=1024 scaled by S"},
+                                 "every SM); traffic = DRAM bytes of one launch of this "
+                                 "workload from one ncu capture"},
             "roofline_hbm": hbm_roofline(N, S, H, wn, kernel_ms, traffic_per_launch(N, S, C, args),
                                          args),
             "clocks": ck,
