@@ -48,11 +48,12 @@ namespace glp {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-// Resident blocks per SM the one-evaluation-per-lane generation kernels are
-// compiled for: a register cap of 128 per thread keeps 16 warps per SM
-// (faster than 168 registers and 12 warps; at 96 registers the loop spills).
+// Resident blocks per SM the generation kernels are compiled for: 3 (12
+// warps per SM, up to 168 registers a thread) measured 1.2 % faster than 4
+// (16 warps, a cap of 128) on 10,000 samples x 4,096 sites; 5 (a cap of 96)
+// was 16 % slower.
 #ifndef GLP_MIN_BLOCKS
-#define GLP_MIN_BLOCKS 4
+#define GLP_MIN_BLOCKS 3
 #endif
 constexpr int kMinBlocks = GLP_MIN_BLOCKS;
 constexpr uint32_t kNone = 0xffffffffu;
