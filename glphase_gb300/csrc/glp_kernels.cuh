@@ -48,10 +48,11 @@ namespace glp {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-// Resident blocks per SM the generation kernels are compiled for: 3 (12
-// warps per SM, up to 168 registers a thread) measured 1.2 % faster than 4
-// (16 warps, a cap of 128) on 10,000 samples x 4,096 sites; 5 (a cap of 96)
-// was 16 % slower.
+// Resident blocks per SM the generation kernels are compiled for (the
+// launch bound's minimum): with 3 the compiler may use up to 168 registers
+// a thread and schedules the loop in 119-127, so 4 blocks (16 warps) still
+// fit; measured 1.2 % faster than the bound of 4 (a cap of 128) on 10,000
+// samples x 4,096 sites.  5 (a cap of 96) was 16 % slower.
 #ifndef GLP_MIN_BLOCKS
 #define GLP_MIN_BLOCKS 3
 #endif
