@@ -242,19 +242,23 @@ int set_tran(glp_problem *pb, const float *tran, uint32_t S) {
     return fail(c, GLP_ERR_ARG, "tran must be non-null with num_sites > 0");
   // rows 0 and S are the identity: row 0 is unused by the reference's
   // recursion (the forward pass starts from it), row S ends the backward pass
-  std::vector<float4> t4(S + 1);
+  // followed by the same rows as (t1, t2, t0 - t2, t0 - t2) for the blocked
+  // recursion
+  std::vector<float4> t4(2 * (size_t)(S + 1));
   t4[0] = make_float4(1.f, 0.f, 0.f, 1.f);
   for (uint32_t m = 1; m < S; ++m)
     t4[m] = make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
                         tran[3 * m] - tran[3 * m + 2]);
   t4[S] = make_float4(1.f, 0.f, 0.f, 1.f);
+  for (uint32_t m = 0; m <= S; ++m)
+    t4[S + 1 + m] = make_float4(t4[m].y, t4[m].z, t4[m].w, t4[m].w);
   if (pb->S != S) {
     release(pb->d_tran4);
     pb->S = 0;
-    GLP_CUDA(c, cudaMalloc((void **)&pb->d_tran4, sizeof(float4) * (S + 1)));
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_tran4, sizeof(float4) * t4.size()));
     pb->S = S;
   }
-  GLP_CUDA(c, cudaMemcpy(pb->d_tran4, t4.data(), sizeof(float4) * (S + 1),
+  GLP_CUDA(c, cudaMemcpy(pb->d_tran4, t4.data(), sizeof(float4) * t4.size(),
                          cudaMemcpyHostToDevice));
   return GLP_OK;
 }
@@ -512,6 +516,7 @@ int make_params(glp_ctx *c, glp_problem *pb, const glp_generation_args *a,
   p->emit = pb->d_emit;
   p->prob = pb->d_prob;
   p->tran4 = pb->d_tran4;
+  p->tranp = pb->d_tran4 + (S + 1);
   p->packed = pb->d_packed;
   p->vq_table = vq ? pb->d_vq : nullptr;
   p->quad_in = a->hap_idxs_in;
@@ -1724,14 +1729,18 @@ int noalloc_setup(NoallocSetup *out) {
 // Kernel layout of the reference's tran [S][3] (row 0 unused,
 // hmmLike.cu:325): S + 1 rows, rows 0 and S the identity (the forward pass
 // starts from row 0 so that the first step reproduces l = e / 4; the backward
-// pass starts from row S); the fourth component is t0 - t2.
+// pass starts from row S); the fourth component is t0 - t2.  The same rows
+// follow as (t1, t2, t0 - t2, t0 - t2) for the blocked recursion.
 __global__ void tran4_kernel(const float *__restrict__ tran, uint32_t S,
                              float4 *__restrict__ out) {
   const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m <= S)
-    out[m] = (m && m < S) ? make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
-                                        __fsub_rn(tran[3 * m], tran[3 * m + 2]))
-                          : make_float4(1.f, 0.f, 0.f, 1.f);
+  if (m <= S) {
+    const float4 r = (m && m < S) ? make_float4(tran[3 * m], tran[3 * m + 1], tran[3 * m + 2],
+                                                __fsub_rn(tran[3 * m], tran[3 * m + 2]))
+                                  : make_float4(1.f, 0.f, 0.f, 1.f);
+    out[m] = r;
+    out[S + 1 + m] = make_float4(r.y, r.z, r.w, r.w);
+  }
 }
 
 size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -1769,7 +1778,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   const bool kick_first = (a->flags & GLP_GEN_KICK_FIRST) != 0;
   if (kick_first && draws && C && H < 2 * N + 1)  // as make_params
     return GLP_ERR_ARG;
-  const size_t tran_off = 256, beta_off = tran_off + round256((size_t)16 * (S + 1));
+  const size_t tran_off = 256, beta_off = tran_off + round256((size_t)32 * (S + 1));
   const size_t need = beta_off + (work ? (size_t)16 * N * S : 0);
   if (need > GLP_NOALLOC_SCRATCH_BYTES)
     return GLP_ERR_TOO_LARGE;
@@ -1795,6 +1804,7 @@ extern "C" int glp_run_generation_noalloc(const glp_generation_args *a, const fl
   p.emit = reinterpret_cast<const float4 *>(emit);
   p.prob = prob;
   p.tran4 = reinterpret_cast<const float4 *>(base + tran_off);
+  p.tranp = p.tran4 + (S + 1);
   p.quad_in = a->hap_idxs_in;
   p.quad_out = a->hap_idxs_out;
   p.props = a->props;

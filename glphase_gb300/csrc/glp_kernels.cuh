@@ -36,6 +36,8 @@
 //   emit       float4 [N][S]              (streamed, shared by a group)
 //   packed     uint32 [ceil(S/8)][N]      (VQ codes; 16-entry table in smem)
 //   tran4      float4 [S + 1]             (t0, t1, t2, t0 - t2); rows 0 and S = identity
+//   tranp      float4 [S + 1]             (t1, t2, t0 - t2, t0 - t2), the pair rows the
+//                                         blocked recursion stages (follows tran4)
 //   beta       float4 [N][S]              (hmm_work scratch)
 #pragma once
 
@@ -73,6 +75,7 @@ struct GenParams {
   const float4 *__restrict__ emit;
   const float *__restrict__ prob;
   const float4 *__restrict__ tran4;
+  const float4 *__restrict__ tranp;  // tran4's rows as (t1, t2, t0 - t2, t0 - t2)
   const uint32_t *__restrict__ packed;
   const float4 *__restrict__ vq_table;
   const uint32_t *__restrict__ quad_in;
@@ -269,10 +272,20 @@ struct EmitVQ {
 // meet at L = alpha_h . (T_{h+1} v_{h+1}).  T is symmetric, so this is the
 // reference's likelihood; one code path serves both halves.
 
+// The state in register pairs for the packed binary32 instructions of
+// sm_100+ (__ffma2_rn and friends round each component as the scalar
+// instruction does): X = (l00, l01), Y = (l11, l10), P = (p2, p1) with
+// p1 = l01 + l10 and p2 = l00 + l11, so that X + Y = P.
 struct FState {
-  float l00, l01, l10, l11, p1, p2;
+  float2 X, Y, P;
   int k;
 };
+
+__device__ __forceinline__ void fstate_fill(FState &f, float l, int k) {
+  f.X = f.Y = make_float2(l, l);
+  f.P = make_float2(l + l, l + l);
+  f.k = k;
+}
 
 __device__ __forceinline__ void select4(const float4 e, bool a0, bool a1, bool c0,
                                         bool c1, float &s00, float &s01, float &s10,
@@ -285,26 +298,27 @@ __device__ __forceinline__ void select4(const float4 e, bool a0, bool a1, bool c
   s11 = c1 ? hi1 : lo1;
 }
 
-// One step with per-site power-of-two rescaling (the site-by-site pass).
+__device__ __forceinline__ void fstate_scale(FState &f, float sc) {
+  const float2 s2 = make_float2(sc, sc);
+  f.X = __fmul2_rn(f.X, s2);
+  f.Y = __fmul2_rn(f.Y, s2);
+  f.P = __fmul2_rn(f.P, s2);
+}
+
+// One step with per-site power-of-two rescaling (the site-by-site pass), for
+// t = (x, y, z, x - z).
 __device__ __forceinline__ void fwd_step(FState &f, const float4 t, float s00, float s01,
                                          float s10, float s11) {
-  const float b00 = fmaf(f.l11, t.z, fmaf(f.p1, t.y, f.l00 * t.x));
-  const float b01 = fmaf(f.l10, t.z, fmaf(f.p2, t.y, f.l01 * t.x));
-  const float b10 = fmaf(f.l01, t.z, fmaf(f.p2, t.y, f.l10 * t.x));
-  const float b11 = fmaf(f.l00, t.z, fmaf(f.p1, t.y, f.l11 * t.x));
-  f.l00 = b00 * s00;
-  f.l01 = b01 * s01;
-  f.l10 = b10 * s10;
-  f.l11 = b11 * s11;
-  f.p1 = f.l01 + f.l10;
-  f.p2 = f.l00 + f.l11;
-  if (f.p1 + f.p2 < kTiny) {
-    f.l00 *= kHuge;
-    f.l01 *= kHuge;
-    f.l10 *= kHuge;
-    f.l11 *= kHuge;
-    f.p1 *= kHuge;
-    f.p2 *= kHuge;
+  const float l00 = f.X.x, l01 = f.X.y, l10 = f.Y.y, l11 = f.Y.x, p1 = f.P.y, p2 = f.P.x;
+  const float b00 = fmaf(l11, t.z, fmaf(p1, t.y, l00 * t.x));
+  const float b01 = fmaf(l10, t.z, fmaf(p2, t.y, l01 * t.x));
+  const float b10 = fmaf(l01, t.z, fmaf(p2, t.y, l10 * t.x));
+  const float b11 = fmaf(l00, t.z, fmaf(p1, t.y, l11 * t.x));
+  f.X = make_float2(b00 * s00, b01 * s01);
+  f.Y = make_float2(b11 * s11, b10 * s10);
+  f.P = __fadd2_rn(f.X, f.Y);
+  if (f.P.x + f.P.y < kTiny) {
+    fstate_scale(f, kHuge);
     f.k -= 64;
   }
 }
@@ -313,28 +327,26 @@ __device__ __forceinline__ void fwd_step(FState &f, const float4 t, float s00, f
 // p1 = l01 + l10 and p2 = l00 + l11,
 //   (T l)_00 = (x - z) l00 + c1,  (T l)_11 = (x - z) l11 + c1,  c1 = y p1 + z p2
 //   (T l)_01 = (x - z) l01 + c2,  (T l)_10 = (x - z) l10 + c2,  c2 = y p2 + z p1
-// for t = (x, y, z, x - z): 14 operations a site instead of 18.  The caller
-// keeps the state in range by normalising at 8-site block boundaries.
-__device__ __forceinline__ void fwd_fast(FState &f, const float4 t, float s00, float s01,
-                                         float s10, float s11) {
-  const float c1 = fmaf(t.z, f.p2, t.y * f.p1);
-  const float c2 = fmaf(t.z, f.p1, t.y * f.p2);
-  f.l00 = fmaf(t.w, f.l00, c1) * s00;
-  f.l01 = fmaf(t.w, f.l01, c2) * s01;
-  f.l10 = fmaf(t.w, f.l10, c2) * s10;
-  f.l11 = fmaf(t.w, f.l11, c1) * s11;
-  f.p1 = f.l01 + f.l10;
-  f.p2 = f.l00 + f.l11;
+// so that X <- (w X + c) * sx and Y <- (w Y + c) * sy for c = (c1, c2),
+// w = x - z: four scalar and five packed instructions a site.  t is a row of
+// the pair table, (y, z, w, w), whose last two components form the pair
+// (w, w).  The caller keeps the state in range by normalising at block
+// boundaries.
+__device__ __forceinline__ void fwd_fast(FState &f, const float4 t, float2 sx, float2 sy) {
+  const float2 c = make_float2(fmaf(t.y, f.P.x, t.x * f.P.y), fmaf(t.y, f.P.y, t.x * f.P.x));
+  const float2 w = make_float2(t.z, t.w);
+  f.X = __fmul2_rn(__ffma2_rn(w, f.X, c), sx);
+  f.Y = __fmul2_rn(__ffma2_rn(w, f.Y, c), sy);
+  f.P = __fadd2_rn(f.X, f.Y);
 }
 
-// x <- T x alone (the backward half's last step, T_{h+1} v_{h+1}).
+// x <- T x alone (the backward half's last step, T_{h+1} v_{h+1}), for
+// t = (x, y, z, x - z).
 __device__ __forceinline__ void apply_tran(FState &f, const float4 t) {
-  const float c1 = fmaf(t.z, f.p2, t.y * f.p1);
-  const float c2 = fmaf(t.z, f.p1, t.y * f.p2);
-  f.l00 = fmaf(t.w, f.l00, c1);
-  f.l01 = fmaf(t.w, f.l01, c2);
-  f.l10 = fmaf(t.w, f.l10, c2);
-  f.l11 = fmaf(t.w, f.l11, c1);
+  const float2 c = make_float2(fmaf(t.z, f.P.x, t.y * f.P.y), fmaf(t.z, f.P.y, t.y * f.P.x));
+  const float2 w = make_float2(t.w, t.w);
+  f.X = __ffma2_rn(w, f.X, c);
+  f.Y = __ffma2_rn(w, f.Y, c);
 }
 
 // Exact power-of-two normalisation at a block boundary: scales the state so
@@ -346,14 +358,8 @@ __device__ __forceinline__ void apply_tran(FState &f, const float4 t) {
 // in the block just computed (the scale is then meaningless too) and the
 // evaluation must be redone with per-site rescaling.
 __device__ __forceinline__ uint32_t fwd_norm(FState &f) {
-  const uint32_t eb = __float_as_uint(f.p1 + f.p2) & 0x7f800000u;
-  const float sc = __uint_as_float(0x9e000000u - eb);  // 2^(189 - e)
-  f.l00 *= sc;
-  f.l01 *= sc;
-  f.l10 *= sc;
-  f.l11 *= sc;
-  f.p1 *= sc;
-  f.p2 *= sc;
+  const uint32_t eb = __float_as_uint(f.P.x + f.P.y) & 0x7f800000u;
+  fstate_scale(f, __uint_as_float(0x9e000000u - eb));  // 2^(189 - e)
   const int e = (int)(eb >> 23);
   f.k += e - 189;
   return (uint32_t)(e - 65);
@@ -361,27 +367,16 @@ __device__ __forceinline__ uint32_t fwd_norm(FState &f) {
 // The same for a state kept in range site by site (any sum down to 2^-65 is
 // legitimate there): the exponent is clamped so the scale stays a normal float.
 __device__ __forceinline__ void fwd_renorm(FState &f) {
-  const int e = (int)((__float_as_uint(f.p1 + f.p2) >> 23) & 0xffu);
+  const int e = (int)((__float_as_uint(f.P.x + f.P.y) >> 23) & 0xffu);
   const int ec = max(e, 62);
-  const float sc = __uint_as_float((uint32_t)(316 - ec) << 23);  // 2^(189 - ec)
-  f.l00 *= sc;
-  f.l01 *= sc;
-  f.l10 *= sc;
-  f.l11 *= sc;
-  f.p1 *= sc;
-  f.p2 *= sc;
+  fstate_scale(f, __uint_as_float((uint32_t)(316 - ec) << 23));  // 2^(189 - ec)
   f.k += ec - 189;
 }
 
 // Overflow guard of the site-by-site pass (emissions above 1 could grow it).
 __device__ __forceinline__ void fwd_guard(FState &f) {
-  if (f.p1 + f.p2 > kHuge) {
-    f.l00 *= kTiny;
-    f.l01 *= kTiny;
-    f.l10 *= kTiny;
-    f.l11 *= kTiny;
-    f.p1 *= kTiny;
-    f.p2 *= kTiny;
+  if (f.P.x + f.P.y > kHuge) {
+    fstate_scale(f, kTiny);
     f.k += 64;
   }
 }
@@ -433,12 +428,13 @@ __device__ __forceinline__ Bits32 half_words(const Parents &pw, uint32_t h) {
   return r;
 }
 
+// The emissions of one site as the pairs (s00, s01) and (s11, s10) that
+// multiply X and Y.
 __device__ __forceinline__ void site_emission(const float4 e, const Bits32 &bw, uint32_t j,
-                                              float &s00, float &s01, float &s10,
-                                              float &s11) {
+                                              float2 &sx, float2 &sy) {
   const uint32_t bit = 1u << j;  // j is a compile-time constant in the unrolled block
   select4(e, (bw.f0 & bit) != 0u, (bw.f1 & bit) != 0u, (bw.m0 & bit) != 0u,
-          (bw.m1 & bit) != 0u, s00, s01, s10, s11);
+          (bw.m1 & bit) != 0u, sx.x, sx.y, sy.y, sy.x);
 }
 
 // One staged block of 8 sites: row j of the slot (transition rows first,
@@ -451,9 +447,9 @@ __device__ __forceinline__ void block8(FState &x, const E &em, const float4 *slo
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
     const float4 e = em.at(eb, j), t = slot[j];
-    float s00, s01, s10, s11;
-    site_emission(e, bw, 8 * B + j, s00, s01, s10, s11);
-    fwd_fast(x, t, s00, s01, s10, s11);
+    float2 sx, sy;
+    site_emission(e, bw, 8 * B + j, sx, sy);
+    fwd_fast(x, t, sx, sy);
     if (kSub == 2 && j == 3)
       eacc |= fwd_norm(x);
   }
@@ -470,9 +466,7 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
                                             uint32_t S, const float4 *__restrict__ tran4,
                                             const E em, uint4 q) {
   FState f;
-  f.l00 = f.l01 = f.l10 = f.l11 = 0.25f;
-  f.p1 = f.p2 = 0.5f;
-  f.k = 0;
+  fstate_fill(f, 0.25f, 0);
   for (uint32_t w = 0; w < wn; ++w) {
     const Parents pw = load_parents(haps, wn, q, w);
     const uint32_t end = min(S, (w + 1) * 64);
@@ -485,7 +479,7 @@ __device__ __noinline__ double like_forward(const uint64_t *__restrict__ haps, u
     }
     fwd_guard(f);
   }
-  const double sum = (((double)f.l00 + (double)f.l01) + (double)f.l10) + (double)f.l11;
+  const double sum = (((double)f.X.x + (double)f.X.y) + (double)f.Y.y) + (double)f.Y.x;
   return log(sum) + (double)f.k * 0.69314718055994530942;
 }
 
@@ -520,8 +514,8 @@ __device__ __forceinline__ double log_scaled(double dot, int k) {
 // by the even lane.  The pair joins with two exact-product shuffles, so both
 // lanes return the same value.  All P lanes of the group call this together;
 // gmask names the lanes that synchronise at each step (the group, or the
-// whole warp when every group runs the same loop).  tran4 holds S + 1 rows,
-// rows 0 and S the identity.
+// whole warp when every group runs the same loop).  tran4 and tranp hold
+// S + 1 rows, rows 0 and S the identity; the ring stages tranp's.
 // kFull: every lane of the warp takes part (gmask is the full mask, known to
 // the compiler).
 template <int kMaxRows, class E, int kSub = 1, bool kFull = false>
@@ -530,16 +524,14 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
                                             unsigned gmask_in) {
   const unsigned gmask = kFull ? 0xffffffffu : gmask_in;
   const uint32_t S = p.S, wn = p.wn;
-  const float4 *tran4 = p.tran4;
+  const float4 *tran4 = p.tran4, *tranp = p.tranp;
   const bool bwd = (li & 1u) != 0;
   const uint32_t nw = S >> 6, wf = (nw + 1) >> 1, wb = nw - wf;
   const uint32_t nbf = 8 * wf, nbb = 8 * wb, top = 8 * nw - 1;  // blocks per direction
   // block-normalised states start at sum 2^62: the forward state 1/4 scaled
   // by 2^62, the backward state 1 scaled by 2^60
   FState x;
-  x.l00 = x.l01 = x.l10 = x.l11 = 0x1p60f;
-  x.p1 = x.p2 = 0x1p61f;
-  x.k = bwd ? -60 : -62;
+  fstate_fill(x, 0x1p60f, bwd ? -60 : -62);
   uint32_t eacc = 0;  // OR of the blocks' range codes (fwd_norm)
   if (bwd && (S & 63u)) {
     const Parents pw = load_parents(p.haps, wn, q, nw);
@@ -563,11 +555,11 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
   auto issue = [&](uint32_t t0, uint32_t d) {
     const uint32_t t = t0 + d, slot = d & 3u;
     if (t < nbf) {
-      stage8<kMaxRows>(stF + slot * kSlotF4, tran4 + 8 * (size_t)t0 + 8 * d, rows);
+      stage8<kMaxRows>(stF + slot * kSlotF4, tranp + 8 * (size_t)t0 + 8 * d, rows);
       em.template stage<kMaxRows>(stF + slot * kSlotF4 + 8, t, rows);
     }
     if (t < nbb) {
-      stage8_rev<kMaxRows>(stB + slot * kSlotF4, tran4 + 8 * (size_t)(top - t0) + 1 - 8 * d,
+      stage8_rev<kMaxRows>(stB + slot * kSlotF4, tranp + 8 * (size_t)(top - t0) + 1 - 8 * d,
                            rows);
       em.template stage_rev<kMaxRows>(stB + slot * kSlotF4 + 8, top - t, rows);
     }
@@ -614,13 +606,13 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
   }
   if (bwd)  // beta_{64 wf - 1} = T_{64 wf} v_{64 wf} (row S is the identity)
     apply_tran(x, __ldg(tran4 + 64 * (size_t)wf));
-  const float y00 = __shfl_xor_sync(gmask, x.l00, 1), y01 = __shfl_xor_sync(gmask, x.l01, 1),
-              y10 = __shfl_xor_sync(gmask, x.l10, 1), y11 = __shfl_xor_sync(gmask, x.l11, 1);
+  const float y00 = __shfl_xor_sync(gmask, x.X.x, 1), y01 = __shfl_xor_sync(gmask, x.X.y, 1),
+              y10 = __shfl_xor_sync(gmask, x.Y.y, 1), y11 = __shfl_xor_sync(gmask, x.Y.x, 1);
   const int yk = __shfl_xor_sync(gmask, x.k, 1);
   const uint32_t bad = (eacc | __shfl_xor_sync(gmask, eacc, 1)) & ~127u;
   // alpha . beta on both lanes: the same exact products in the same order
-  const double dot = (double)x.l00 * (double)y00 + (double)x.l01 * (double)y01 +
-                     (double)x.l10 * (double)y10 + (double)x.l11 * (double)y11;
+  const double dot = (double)x.X.x * (double)y00 + (double)x.X.y * (double)y01 +
+                     (double)x.Y.y * (double)y10 + (double)x.Y.x * (double)y11;
   double L = log_scaled(dot, x.k + yk);
   if (__any_sync(gmask, bad != 0u)) {
     double Lf = L;

@@ -385,7 +385,7 @@ int glp_result(glp_ctx *ctx, const uint32_t *hsum, uint32_t num_samples, uint32_
  * kernel layout and the hmm_work rows -- in one fixed array of
  * GLP_NOALLOC_SCRATCH_BYTES (32 MiB) of device memory that every GPU loading
  * this library holds until the process exits.  It needs
- * 256 + 16*ceil((S+1)/16)*16 + 16*N*S bytes of it and returns GLP_ERR_TOO_LARGE
+ * 256 + 32*ceil((S+1)/8)*8 + 16*N*S bytes of it and returns GLP_ERR_TOO_LARGE
  * beyond that (about N*S <= 2.0e6 site-samples).
  *
  * All array arguments are DEVICE pointers except pc16 (host, row-major
