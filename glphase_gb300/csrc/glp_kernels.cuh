@@ -48,8 +48,11 @@
 
 namespace glp {
 
-constexpr int kThreads = 128;
-constexpr int kWarps = kThreads / 32;
+#ifndef GLP_GEN_WARPS
+#define GLP_GEN_WARPS 4
+#endif
+constexpr int kWarps = GLP_GEN_WARPS;  // warps per generation block
+constexpr int kThreads = 32 * kWarps;
 // Resident blocks per SM the generation kernels are compiled for (the
 // launch bound's minimum): with 3 the compiler may use up to 168 registers
 // a thread and schedules the loop in 119-127, so 4 blocks (16 warps) still
@@ -1167,14 +1170,15 @@ __device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s
   }
 }
 
-// Pass 2 of hmm_work: the sampling of impute.cpp:453-484 for sites m0 + lane
-// and m0 + 32 + lane of sample s (one warp per sample and 64-site word),
-// from p_m (pass 1), the genotype probabilities, the mutation-matrix rows pcr
-// (pc[i][0..3] as float4) and the reference's 4-site draws.  Returns the two
-// haplotype bits of the site as bits 0 and 1 (0 for sites past S).
+// Pass 2 of hmm_work: the sampling of impute.cpp:453-484 for site m of
+// sample s, from p_m (pass 1), the genotype probabilities, the
+// mutation-matrix rows pcr (pc[i][0..3] as float4) and the site's uniform
+// u_bits (the draw's 32 bits; the trace's value when one is given).  Returns
+// the two haplotype bits of the site as bits 0 and 1 (0 for sites past S).
 __device__ __forceinline__ uint32_t work_sample_site(const GenParams &p, const float4 *pcr,
                                                      uint32_t s, uint32_t m, uint64_t A0,
-                                                     uint64_t A1, uint64_t C0, uint64_t C1) {
+                                                     uint64_t A1, uint64_t C0, uint64_t C1,
+                                                     uint32_t u_bits) {
   const uint32_t S = p.S;
   if (m >= S)
     return 0;
@@ -1198,13 +1202,7 @@ __device__ __forceinline__ uint32_t work_sample_site(const GenParams &p, const f
     for (int k = 0; k < 4; ++k)
       c[k] = powf(c[k], p.pen);
   }
-  float u;
-  if (p.tr_work) {
-    u = __ldg(p.tr_work + (size_t)s * S + m);
-  } else {
-    const glp_u32x4 ux = glp_draw(p.seed, p.generation, s, m >> 2, GLP_TAG_WORK);
-    u = glp_u24(ux.v[m & 3u]);
-  }
+  const float u = p.tr_work ? __ldg(p.tr_work + (size_t)s * S + m) : glp_u24(u_bits);
   const float c01 = __fadd_rn(c[0], c[1]);
   const float c012 = __fadd_rn(c01, c[2]);
   const float r = __fmul_rn(u, __fadd_rn(c012, c[3]));
@@ -1217,26 +1215,42 @@ __device__ __forceinline__ uint32_t work_sample_site(const GenParams &p, const f
   return 3u;    // (1, 1)
 }
 
-// Pass 2 for all words of sample s (called by a whole warp): bits of sites
-// w*64 + lane and w*64 + 32 + lane, gathered into the two new haplotype words
-// with ballots.
+// Pass 2 for all words of sample s (called by a whole warp), two words at a
+// time: lane l draws the four uniforms of the l-th 4-site group of the
+// 128-site span (one draw per group, as the reference draws them) into
+// u[4 l .. 4 l + 3], so u[o] is the uniform of span site o; then the bits
+// of sites w*64 + lane and w*64 + 32 + lane of each word are gathered into
+// the two new haplotype words with ballots.
 __device__ __forceinline__ void work_sample(const GenParams &p, const float4 *pcr, uint32_t s,
-                                            uint4 q, uint32_t lane) {
+                                            uint4 q, uint32_t lane, uint32_t *u) {
   const uint32_t wn = p.wn;
   const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
                  *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
   uint64_t *ha = p.hnew + (size_t)2 * s * wn, *hb = ha + wn;
-  for (uint32_t w = 0; w < wn; ++w) {
-    const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
-                   C1 = __ldg(m1 + w);
-    const uint32_t lo = work_sample_site(p, pcr, s, w * 64 + lane, A0, A1, C0, C1);
-    const uint32_t hi = work_sample_site(p, pcr, s, w * 64 + 32 + lane, A0, A1, C0, C1);
-    const uint32_t alo = __ballot_sync(0xffffffffu, lo & 1u), ahi = __ballot_sync(0xffffffffu, hi & 1u);
-    const uint32_t blo = __ballot_sync(0xffffffffu, lo & 2u), bhi = __ballot_sync(0xffffffffu, hi & 2u);
-    if (lane == 0) {
-      ha[w] = ((uint64_t)ahi << 32) | alo;
-      hb[w] = ((uint64_t)bhi << 32) | blo;
+  for (uint32_t w2 = 0; w2 < wn; w2 += 2) {
+    if (!p.tr_work) {
+      const glp_u32x4 ux = glp_draw(p.seed, p.generation, s, 16 * w2 + lane, GLP_TAG_WORK);
+      reinterpret_cast<uint4 *>(u)[lane] = make_uint4(ux.v[0], ux.v[1], ux.v[2], ux.v[3]);
     }
+    __syncwarp();
+    for (uint32_t t = 0; t < 2 && w2 + t < wn; ++t) {
+      const uint32_t w = w2 + t;
+      const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
+                     C1 = __ldg(m1 + w);
+      const uint32_t lo = work_sample_site(p, pcr, s, w * 64 + lane, A0, A1, C0, C1,
+                                           u[64 * t + lane]);
+      const uint32_t hi = work_sample_site(p, pcr, s, w * 64 + 32 + lane, A0, A1, C0, C1,
+                                           u[64 * t + 32 + lane]);
+      const uint32_t alo = __ballot_sync(0xffffffffu, lo & 1u),
+                     ahi = __ballot_sync(0xffffffffu, hi & 1u);
+      const uint32_t blo = __ballot_sync(0xffffffffu, lo & 2u),
+                     bhi = __ballot_sync(0xffffffffu, hi & 2u);
+      if (lane == 0) {
+        ha[w] = ((uint64_t)ahi << 32) | alo;
+        hb[w] = ((uint64_t)bhi << 32) | blo;
+      }
+    }
+    __syncwarp();  // u is redrawn next span
   }
 }
 
@@ -1664,6 +1678,7 @@ __device__ __forceinline__ void chains_body(const Src &src) {
 template <class Src>
 __device__ __forceinline__ void sample_body(const Src &src) {
   __shared__ float4 s_pcr[kWorkThreads / 32][4];  // the warp's mutation-matrix rows
+  __shared__ __align__(16) uint32_t s_u[kWorkThreads / 32][128];  // a span's uniforms
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const uint32_t g = blockIdx.x * (blockDim.x >> 5) + wib;  // one sample per warp
   if (g >= src.total())
@@ -1677,7 +1692,7 @@ __device__ __forceinline__ void sample_body(const Src &src) {
     s_pcr[wib][lane] = make_float4(p.pc[4 * lane], p.pc[4 * lane + 1], p.pc[4 * lane + 2],
                                    p.pc[4 * lane + 3]);
   __syncwarp();
-  work_sample(p, s_pcr[wib], s, final_quad(src, p, s), lane);
+  work_sample(p, s_pcr[wib], s, final_quad(src, p, s), lane, s_u[wib]);
 }
 
 template <int = 0>
