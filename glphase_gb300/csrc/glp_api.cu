@@ -349,13 +349,13 @@ cudaError_t allow_chain_smem() {
   return e;
 }
 void launch_work(const glp::GenParams &p, uint64_t samples, cudaStream_t st) {
-  glp::work_chains_kernel<><<<(unsigned)((samples + 31) / 32), glp::kChainThreads,
-                              glp::kChainSmem, st>>>(p);
+  glp::work_chains_kernel<><<<(unsigned)((samples + glp::kPairRows - 1) / glp::kPairRows),
+                              glp::kChainThreads, glp::kChainSmem, st>>>(p);
   glp::work_sample_kernel<><<<(unsigned)samples, 32, 0, st>>>(p);
 }
 void launch_work(const glp::MultiParams &mp, uint64_t samples, cudaStream_t st) {
-  glp::work_chains_multi_kernel<><<<(unsigned)((samples + 31) / 32), glp::kChainThreads,
-                                    glp::kChainSmem, st>>>(mp);
+  glp::work_chains_multi_kernel<><<<(unsigned)((samples + glp::kPairRows - 1) / glp::kPairRows),
+                                    glp::kChainThreads, glp::kChainSmem, st>>>(mp);
   glp::work_sample_multi_kernel<><<<(unsigned)samples, 32, 0, st>>>(mp);
 }
 

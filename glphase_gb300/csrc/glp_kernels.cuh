@@ -759,8 +759,9 @@ __device__ __forceinline__ void work_fwd_step(float &l00, float &l01, float &l10
 // bits, so (1) the two sequential recursions -- the backward vectors beta_m
 // (impute.cpp:389-414) and the forward l_m -- run per sample and leave
 // p_m = l_m * beta_m (the products of impute.cpp:449-452) in the scratch:
-// work_chains_split runs them at the same time on two warps, work_chains one
-// after the other on one thread (chunks mixed within a warp); (2) the
+// work_chains_pair runs them at the same time on two warps (a lane pair per
+// recursion), work_chains one after the other on one thread (chunks mixed
+// within a warp); (2) the
 // sampling of impute.cpp:453-484 then runs for every site in parallel, one
 // warp per sample and 32 sites per instruction.
 
@@ -909,52 +910,111 @@ __device__ __forceinline__ void work_chains(const GenParams &p, uint32_t s, uint
   }
 }
 
-// The four parent words of one 64-site word index, with the next word in the
-// traversal direction already loaded (a word lasts four 16-site tiles).
-struct ParentWords {
-  uint64_t cur[4], nxt[4];
-  uint32_t w;
-};
-__device__ __forceinline__ void load_words(uint64_t (&d)[4], const uint64_t *f0,
-                                           const uint64_t *f1, const uint64_t *m0,
-                                           const uint64_t *m1, uint32_t w) {
-  d[0] = __ldg(f0 + w);
-  d[1] = __ldg(f1 + w);
-  d[2] = __ldg(m0 + w);
-  d[3] = __ldg(m1 + w);
-}
-
-// Staging of pass 1 for the 32 samples of a warp that share one chunk: each
-// 16-site tile of the 32 per-sample rows (emission, and stored vectors) is
-// copied into shared memory by the whole warp, one 256-byte row segment per
-// half-warp instruction (cp.async, one tile in flight ahead), so every lane
-// then reads its own row from shared memory.
+// Staging of pass 1 for the 16 samples of a warp that share one chunk (two
+// lanes a sample): each 16-site tile of the 16 per-sample rows (emission,
+// and stored vectors) is copied into shared memory by the whole warp, one
+// 256-byte row segment per half-warp instruction (cp.async, one tile in
+// flight ahead), so every lane then reads its sample's row from shared
+// memory.
 constexpr int kTile = 16;
 constexpr int kTileStrideF4 = kTile + 1;  // odd number of 16-byte units: no bank conflicts
+constexpr int kPairRows = 16;             // samples per warp of pass 1
 
 struct ChainTiles {
-  float4 e[2][32 * kTileStrideF4];
-  float4 b[2][32 * kTileStrideF4];
+  float4 e[2][kPairRows * kTileStrideF4];
+  float4 b[2][kPairRows * kTileStrideF4];
   float4 t[2][kTile];
-  const float4 *erow[32];
-  float4 *brow[32];
+  const float4 *erow[kPairRows];
+  float4 *brow[kPairRows];
 };
 
 // Copy sites [base, base + kTile) of every row (rows with a null pointer are
-// skipped) and of the transition table; indices are clamped to [0, S).
+// skipped); indices are clamped to [0, S).
 __device__ __forceinline__ void stage_tile(float4 *dst, const float4 *const *rows, int base,
                                            uint32_t S, uint32_t lane) {
   const uint32_t half = lane >> 4, j = lane & 15u;
   const uint32_t m = clamp_site(base + (int)j, S);
-#pragma unroll 4
-  for (uint32_t r = 0; r < 32; r += 2) {
+#pragma unroll
+  for (uint32_t r = 0; r < (uint32_t)kPairRows; r += 2) {
     const float4 *row = rows[r + half];
     if (row)
       cp_async16(dst + (r + half) * kTileStrideF4 + j, row + m);
   }
 }
 
-// Pass 1 split over two warps that share the same 32 samples (one thread per
+// The emission e[(abit << 1) | cbit] of impute.cpp:338-342 for bit j of the
+// father word a and the mother word c.
+__device__ __forceinline__ float pick_bits(const float4 e, uint32_t a, uint32_t c, int j) {
+  const bool ab = (a >> j) & 1u, cb = (c >> j) & 1u;
+  return ab ? (cb ? e.w : e.z) : (cb ? e.y : e.x);
+}
+
+// Pass 1 on lane pairs.  A generation has only 2N recursions of S
+// sequential steps, so one lane a recursion leaves about one warp a
+// scheduler, which then waits on each step's latency; here two lanes share a
+// recursion, which doubles the warps.  Lane role 0 owns the states 00 and
+// 11, role 1 the states 01 and 10: each lane computes the reference's
+// formula for its own two states (impute.cpp:389-414 backward, 416-447
+// forward) in the reference's binary32 operation order, one shuffle hands
+// the pair the other two, and both lanes form the normalising sum in the
+// reference's order, so both hold the same, bit-identical vector.
+//
+// The backward state is kept relative to the lane: (o1, o2) its own states,
+// (p1, p2) the partner's -- role 0: (b0, b3, b1, b2), role 1: (b1, b2, b0,
+// b3).  With the mother words of role 1 swapped (cf, cs), own state k picks
+// its emission from (father word k, cf) for k = 1 and (father word 2, cs)
+// for k = 2, and the partner's from the opposite mother word.
+struct PairBwd {
+  float o1, o2, p1, p2;
+  __device__ __forceinline__ void step(float e_o1, float e_o2, float e_p1, float e_p2,
+                                       const float4 t, bool r0) {
+    const float xo1 = __fmul_rn(o1, e_o1), xo2 = __fmul_rn(o2, e_o2);
+    const float pair = __fadd_rn(__fmul_rn(p1, e_p1), __fmul_rn(p2, e_p2));
+    const float py = __fmul_rn(pair, t.y);
+    const float A = __fadd_rn(__fadd_rn(__fmul_rn(xo1, t.x), py), __fmul_rn(xo2, t.z));
+    const float B = __fadd_rn(__fadd_rn(__fmul_rn(xo2, t.x), py), __fmul_rn(xo1, t.z));
+    const float pA = __shfl_xor_sync(0xffffffffu, A, 1), pB = __shfl_xor_sync(0xffffffffu, B, 1);
+    // ((b0 + b1) + b2) + b3: role 0 holds b0 = A, b3 = B; role 1 b1 = A, b2 = B
+    const float sum = __fadd_rn(__fadd_rn(__fadd_rn(A, pA), r0 ? pB : B), r0 ? B : pB);
+    const float inv = recip_rn(sum);
+    o1 = __fmul_rn(A, inv);
+    o2 = __fmul_rn(B, inv);
+    p1 = __fmul_rn(pA, inv);
+    p2 = __fmul_rn(pB, inv);
+  }
+  // (b0, b1, b2, b3) for role 0
+  __device__ __forceinline__ float4 vec() const { return make_float4(o1, p1, p2, o2); }
+};
+
+// The forward state is the reference's (l00, l01, l10, l11) in both lanes.
+// Role 0 computes c00 and c11, role 1 c01 and c10 (the coefficient rows of
+// T for those states), each times its own emission.
+struct PairFwd {
+  float l00, l01, l10, l11;
+  __device__ __forceinline__ void finish(float A, float B, bool r0) {
+    const float pA = __shfl_xor_sync(0xffffffffu, A, 1), pB = __shfl_xor_sync(0xffffffffu, B, 1);
+    const float n00 = r0 ? A : pA, n01 = r0 ? pA : A, n10 = r0 ? pB : B, n11 = r0 ? B : pB;
+    const float inv = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(n00, n01), n10), n11));
+    l00 = __fmul_rn(n00, inv);
+    l01 = __fmul_rn(n01, inv);
+    l10 = __fmul_rn(n10, inv);
+    l11 = __fmul_rn(n11, inv);
+  }
+  __device__ __forceinline__ void step(float e_o1, float e_o2, const float4 t, bool r0) {
+    // role 0: c00 (x, y, y, z), c11 (z, y, y, x); role 1: c01 (y, x, z, y), c10 (y, z, x, y)
+    const float cA = fma3_rn(l00, r0 ? t.x : t.y, l01, r0 ? t.y : t.x, l10, r0 ? t.y : t.z, l11,
+                             r0 ? t.z : t.y);
+    const float cB = fma3_rn(l00, r0 ? t.z : t.y, l01, r0 ? t.y : t.z, l10, r0 ? t.y : t.x, l11,
+                             r0 ? t.x : t.y);
+    finish(__fmul_rn(cA, e_o1), __fmul_rn(cB, e_o2), r0);
+  }
+  __device__ __forceinline__ void first(float e_o1, float e_o2, bool r0) {
+    finish(__fmul_rn(0.25f, e_o1), __fmul_rn(0.25f, e_o2), r0);
+  }
+  __device__ __forceinline__ float4 vec() const { return make_float4(l00, l01, l10, l11); }
+};
+
+// Pass 1 split over two warps that share the same 16 samples (two lanes per
 // sample in each): warp 0 runs the backward recursion from the top site and
 // warp 1 the forward recursion from site 0, at the same time.  Neither
 // depends on the other until p_m = l_m * beta_m, so each runs to the middle
@@ -964,20 +1024,27 @@ __device__ __forceinline__ void stage_tile(float4 *dst, const float4 *const *row
 // half reading what the other stored and writing p there: the backward warp
 // p_m for m <= mid-2 (beta_m fresh, l_m stored), the forward warp p_{mid-1}
 // and p_m for m >= mid (l_m fresh, beta_m stored).  The operations on every
-// vector are those of work_chains, so p is bit-identical; the sequential
-// chain per thread is half as long, which is what bounds the pass when a
-// generation has few samples.  Both warps call this together.
-__device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s, uint4 q,
-                                                  bool valid, uint32_t lane, bool fwd,
-                                                  ChainTiles &sm) {
+// vector are those of work_chains, so p is bit-identical.  Role-0 lanes store
+// the vectors.  Both warps call this together, every lane (lanes of samples
+// past the end compute on whatever their rows hold and store nothing).
+__device__ __forceinline__ void work_chains_pair(const GenParams &p, uint32_t s, uint4 q,
+                                                 bool valid, uint32_t lane, bool fwd,
+                                                 ChainTiles &sm) {
   const uint32_t S = p.S, wn = p.wn;
   const float4 *tr = p.tran4;
+  const bool r0 = (lane & 1u) == 0;
+  const bool writer = valid && r0;
+  const uint32_t row = lane >> 1;
   const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
                  *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
+  // role 1 owns 01 and 10: its first own state takes the second mother word
+  const uint64_t *mf = r0 ? m0 : m1, *ms = r0 ? m1 : m0;
   float4 *beta = p.beta + (size_t)s * S;
-  sm.erow[lane] = valid ? p.emit + (size_t)s * S : nullptr;
-  sm.brow[lane] = valid ? beta : nullptr;
-  if (!fwd && valid)
+  if (r0) {
+    sm.erow[row] = valid ? p.emit + (size_t)s * S : nullptr;
+    sm.brow[row] = valid ? beta : nullptr;
+  }
+  if (!fwd && writer)
     beta[S - 1] = make_float4(1.f, 1.f, 1.f, 1.f);
   __syncwarp();
   const int ntiles = (int)((S + kTile - 1) / kTile);
@@ -996,20 +1063,28 @@ __device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s
       cp_async16(&sm.t[buf][lane], tr + clamp_site(base + (int)lane, S));
     cp_async_commit();
   };
-  float v0 = 1.f, v1 = 1.f, v2 = 1.f, v3 = 1.f;  // beta (backward) or l (forward)
-  ParentWords pw;
+  PairBwd vb;
+  vb.o1 = vb.o2 = vb.p1 = vb.p2 = 1.f;
+  PairFwd vf;
+  vf.l00 = vf.l01 = vf.l10 = vf.l11 = 0.f;
+  // the four parent words of the current 64-site word, mother words by role
+  uint64_t wa0 = 0, wa1 = 0, wcf = 0, wcs = 0;
+  int wcur = -1;
+  auto words = [&](uint32_t w) {
+    if ((int)w != wcur) {
+      wa0 = __ldg(f0 + w);
+      wa1 = __ldg(f1 + w);
+      wcf = __ldg(mf + w);
+      wcs = __ldg(ms + w);
+      wcur = (int)w;
+    }
+  };
 
   // backward (impute.cpp:389-414) over n tiles from the tile at first down;
   // comb: store p_{m-1} = l_{m-1} * beta_{m-1} (l staged one site lower)
   auto run_bwd = [&](int first, int n, bool comb) {
     if (n <= 0)
       return;
-    pw.w = (uint32_t)first >> 6;
-    if (valid) {
-      load_words(pw.cur, f0, f1, m0, m1, pw.w);
-      if (pw.w >= 1)
-        load_words(pw.nxt, f0, f1, m0, m1, pw.w - 1);
-    }
     stage(0, first, comb, first - 1);
     for (int i = 0; i < n; ++i) {
       const int base = first - kTile * i, buf = i & 1;
@@ -1017,59 +1092,40 @@ __device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s
         stage(buf ^ 1, base - kTile, comb, base - kTile - 1);
       else
         cp_async_commit();
+      words((uint32_t)base >> 6);
+      const uint32_t A0 = (uint32_t)(wa0 >> (base & 63)), A1 = (uint32_t)(wa1 >> (base & 63)),
+                     CF = (uint32_t)(wcf >> (base & 63)), CS = (uint32_t)(wcs >> (base & 63));
       cp_async_wait<1>();
       __syncwarp();
-      if (valid) {
-        const uint32_t w = (uint32_t)base >> 6;
-        if (w != pw.w) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            pw.cur[k] = pw.nxt[k];
-          pw.w = w;
-          if (w >= 1)
-            load_words(pw.nxt, f0, f1, m0, m1, w - 1);
-        }
-        const uint32_t A0 = (uint32_t)(pw.cur[0] >> (base & 63)),
-                       A1 = (uint32_t)(pw.cur[1] >> (base & 63)),
-                       C0 = (uint32_t)(pw.cur[2] >> (base & 63)),
-                       C1 = (uint32_t)(pw.cur[3] >> (base & 63));
-        const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
-        const float4 *lrow = sm.b[buf] + lane * kTileStrideF4;
-        auto store = [&](int j) {  // beta_{m-1} (or p_{m-1}) for site m = base + j
-          if (comb) {
-            const float4 l = lrow[j];
-            beta[base + j - 1] = make_float4(__fmul_rn(l.x, v0), __fmul_rn(l.y, v1),
-                                             __fmul_rn(l.z, v2), __fmul_rn(l.w, v3));
-          } else {
-            beta[base + j - 1] = make_float4(v0, v1, v2, v3);
-          }
-        };
-        if (base >= 1 && base + kTile - 1 <= (int)S - 1) {
-          float4 pk[kTile], tt[kTile];
-#pragma unroll
-          for (int j = 0; j < kTile; ++j) {
-            const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
-                           c1b = (C1 >> j) & 1u;
-            pk[j] = pick4(erow[j], (a0 << 1) | c0b, (a0 << 1) | c1b, (a1 << 1) | c0b,
-                          (a1 << 1) | c1b);
-            tt[j] = sm.t[buf][j];
-          }
-#pragma unroll
-          for (int j = kTile - 1; j >= 0; --j) {
-            work_bwd_math(v0, v1, v2, v3, pk[j], tt[j]);
-            store(j);
-          }
+      const float4 *erow = sm.e[buf] + row * kTileStrideF4;
+      const float4 *lrow = sm.b[buf] + row * kTileStrideF4;
+      auto store = [&](int j) {  // beta_{m-1} (or p_{m-1}) for site m = base + j
+        if (!writer)
+          return;
+        const float4 v = vb.vec();
+        if (comb) {
+          const float4 l = lrow[j];
+          beta[base + j - 1] = make_float4(__fmul_rn(l.x, v.x), __fmul_rn(l.y, v.y),
+                                           __fmul_rn(l.z, v.z), __fmul_rn(l.w, v.w));
         } else {
-#pragma unroll 1
-          for (int j = kTile - 1; j >= 0; --j)
-            if (base + j >= 1 && base + j <= (int)S - 1) {
-              const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
-                             c1b = (C1 >> j) & 1u;
-              work_bwd_step(v0, v1, v2, v3, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
-                            (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b);
-              store(j);
-            }
+          beta[base + j - 1] = v;
         }
+      };
+      auto one = [&](int j) {
+        const float4 e = erow[j];
+        vb.step(pick_bits(e, A0, CF, j), pick_bits(e, A1, CS, j), pick_bits(e, A0, CS, j),
+                pick_bits(e, A1, CF, j), sm.t[buf][j], r0);
+        store(j);
+      };
+      if (base >= 1 && base + kTile - 1 <= (int)S - 1) {
+#pragma unroll
+        for (int j = kTile - 1; j >= 0; --j)
+          one(j);
+      } else {
+#pragma unroll 1
+        for (int j = kTile - 1; j >= 0; --j)
+          if (base + j >= 1 && base + j <= (int)S - 1)
+            one(j);
       }
       __syncwarp();  // the buffer is refilled next iteration
     }
@@ -1080,12 +1136,6 @@ __device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s
   auto run_fwd = [&](int first, int n, bool comb) {
     if (n <= 0)
       return;
-    pw.w = (uint32_t)first >> 6;
-    if (valid) {
-      load_words(pw.cur, f0, f1, m0, m1, pw.w);
-      if (pw.w + 1 < wn)
-        load_words(pw.nxt, f0, f1, m0, m1, pw.w + 1);
-    }
     stage(0, first, comb, first);
     for (int i = 0; i < n; ++i) {
       const int base = first + kTile * i, buf = i & 1;
@@ -1093,60 +1143,44 @@ __device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s
         stage(buf ^ 1, base + kTile, comb, base + kTile);
       else
         cp_async_commit();
+      words((uint32_t)base >> 6);
+      const uint32_t A0 = (uint32_t)(wa0 >> (base & 63)), A1 = (uint32_t)(wa1 >> (base & 63)),
+                     CF = (uint32_t)(wcf >> (base & 63)), CS = (uint32_t)(wcs >> (base & 63));
       cp_async_wait<1>();
       __syncwarp();
-      if (valid) {
-        const uint32_t w = (uint32_t)base >> 6;
-        if (w != pw.w) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            pw.cur[k] = pw.nxt[k];
-          pw.w = w;
-          if (w + 1 < wn)
-            load_words(pw.nxt, f0, f1, m0, m1, w + 1);
+      const float4 *erow = sm.e[buf] + row * kTileStrideF4;
+      const float4 *brow = sm.b[buf] + row * kTileStrideF4;
+      auto store = [&](int j) {  // l_m (or p_m) for site m = base + j
+        const int m = base + j;
+        if (!writer)
+          return;
+        const float4 v = vf.vec();
+        if (comb) {
+          const float4 bb = brow[j];
+          beta[m] = make_float4(__fmul_rn(v.x, bb.x), __fmul_rn(v.y, bb.y),
+                                __fmul_rn(v.z, bb.z), __fmul_rn(v.w, bb.w));
+        } else if (m <= mid - 2) {
+          beta[m] = v;
         }
-        const uint32_t A0 = (uint32_t)(pw.cur[0] >> (base & 63)),
-                       A1 = (uint32_t)(pw.cur[1] >> (base & 63)),
-                       C0 = (uint32_t)(pw.cur[2] >> (base & 63)),
-                       C1 = (uint32_t)(pw.cur[3] >> (base & 63));
-        const float4 *erow = sm.e[buf] + lane * kTileStrideF4;
-        const float4 *brow = sm.b[buf] + lane * kTileStrideF4;
-        auto store = [&](int j) {  // l_m (or p_m) for site m = base + j
-          const int m = base + j;
-          if (comb) {
-            const float4 bb = brow[j];
-            beta[m] = make_float4(__fmul_rn(v0, bb.x), __fmul_rn(v1, bb.y),
-                                  __fmul_rn(v2, bb.z), __fmul_rn(v3, bb.w));
-          } else if (m <= mid - 2) {
-            beta[m] = make_float4(v0, v1, v2, v3);
-          }
-        };
-        if (base >= 1 && base + kTile <= (int)S) {
-          float4 pk[kTile], tt[kTile];
+      };
+      auto one = [&](int j) {
+        const float4 e = erow[j];
+        const float e1 = pick_bits(e, A0, CF, j), e2 = pick_bits(e, A1, CS, j);
+        if (base + j == 0)
+          vf.first(e1, e2, r0);
+        else
+          vf.step(e1, e2, sm.t[buf][j], r0);
+        store(j);
+      };
+      if (base >= 1 && base + kTile <= (int)S) {
 #pragma unroll
-          for (int j = 0; j < kTile; ++j) {
-            const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
-                           c1b = (C1 >> j) & 1u;
-            pk[j] = pick4(erow[j], (a0 << 1) | c0b, (a0 << 1) | c1b, (a1 << 1) | c0b,
-                          (a1 << 1) | c1b);
-            tt[j] = sm.t[buf][j];
-          }
-#pragma unroll
-          for (int j = 0; j < kTile; ++j) {
-            work_fwd_math(v0, v1, v2, v3, pk[j], tt[j], false);
-            store(j);
-          }
-        } else {
+        for (int j = 0; j < kTile; ++j)
+          one(j);
+      } else {
 #pragma unroll 1
-          for (int j = 0; j < kTile; ++j)
-            if (base + j < (int)S) {
-              const uint32_t a0 = (A0 >> j) & 1u, a1 = (A1 >> j) & 1u, c0b = (C0 >> j) & 1u,
-                             c1b = (C1 >> j) & 1u;
-              work_fwd_step(v0, v1, v2, v3, erow[j], sm.t[buf][j], (a0 << 1) | c0b,
-                            (a0 << 1) | c1b, (a1 << 1) | c0b, (a1 << 1) | c1b, base + j == 0);
-              store(j);
-            }
-        }
+        for (int j = 0; j < kTile; ++j)
+          if (base + j < (int)S)
+            one(j);
       }
       __syncwarp();
     }
@@ -1159,10 +1193,11 @@ __device__ __forceinline__ void work_chains_split(const GenParams &p, uint32_t s
   // both halves' vectors are stored (block barrier: the two warps)
   __syncthreads();
   if (fwd) {
-    if (valid && mid >= 1) {  // p_{mid-1}: l_{mid-1} still in registers
+    if (writer && mid >= 1) {  // p_{mid-1}: l_{mid-1} still in registers
       const float4 bb = beta[mid - 1];
-      beta[mid - 1] = make_float4(__fmul_rn(v0, bb.x), __fmul_rn(v1, bb.y),
-                                  __fmul_rn(v2, bb.z), __fmul_rn(v3, bb.w));
+      const float4 v = vf.vec();
+      beta[mid - 1] = make_float4(__fmul_rn(v.x, bb.x), __fmul_rn(v.y, bb.y),
+                                  __fmul_rn(v.z, bb.z), __fmul_rn(v.w, bb.w));
     }
     run_fwd(mid, n_hi, true);
   } else {
@@ -1632,10 +1667,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 }
 
 // hmm_work after the generation kernel, over the published final
-// quadruples.  Pass 1: blocks of two warps over 32 samples, one thread per
-// sample and recursion direction in each warp (work_chains_split), so the
-// few hundred blocks of a generation spread over every SM.  Pass 2: one warp
-// per sample samples all sites.  Chunks without hmm_work skip both.
+// quadruples.  Pass 1: blocks of two warps over 16 samples, a lane pair per
+// sample and recursion direction in each warp (work_chains_pair), so the
+// thousand-odd blocks of a generation spread over every SM.  Pass 2: one
+// warp per sample samples all sites.  Chunks without hmm_work skip both.
 constexpr int kWorkThreads = 32;
 constexpr int kChainThreads = 64;
 constexpr size_t kChainSmem = 2 * sizeof(ChainTiles);  // dynamic: one per warp
@@ -1652,7 +1687,8 @@ __device__ __forceinline__ void chains_body(const Src &src) {
   extern __shared__ __align__(16) unsigned char glp_chain_smem[];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   ChainTiles &s_tiles = reinterpret_cast<ChainTiles *>(glp_chain_smem)[warp];
-  const uint32_t g = blockIdx.x * 32u + lane;  // both warps: the block's 32 samples
+  // both warps: the block's 16 samples, two lanes each
+  const uint32_t g = blockIdx.x * (uint32_t)kPairRows + (lane >> 1);
   const uint32_t total = src.total();
   uint32_t c = 0, s = 0;
   if (g < total)
@@ -1663,14 +1699,14 @@ __device__ __forceinline__ void chains_body(const Src &src) {
   const bool valid = g < total && p.do_work;
   // the warps stage rows together when all their lanes share one chunk (the
   // two warps see the same samples, so they take the same branch and either
-  // both or neither reach the barrier in work_chains_split)
+  // both or neither reach the barrier in work_chains_pair)
   int same = 0;
   __match_all_sync(0xffffffffu, c, &same);
   if (same) {
     if (__any_sync(0xffffffffu, valid))
-      work_chains_split(p, s, valid ? final_quad(src, p, s) : make_uint4(0, 0, 0, 0), valid,
-                        lane, warp == 1, s_tiles);
-  } else if (valid && warp == 0) {
+      work_chains_pair(p, s, valid ? final_quad(src, p, s) : make_uint4(0, 0, 0, 0), valid,
+                       lane, warp == 1, s_tiles);
+  } else if (valid && warp == 0 && (lane & 1u) == 0) {
     work_chains(p, s, final_quad(src, p, s));
   }
 }
