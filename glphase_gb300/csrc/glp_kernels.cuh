@@ -1268,8 +1268,11 @@ __device__ __forceinline__ void work_sample(const GenParams &p, const float4 *pc
       reinterpret_cast<uint4 *>(u)[lane] = make_uint4(ux.v[0], ux.v[1], ux.v[2], ux.v[3]);
     }
     __syncwarp();
-    for (uint32_t t = 0; t < 2 && w2 + t < wn; ++t) {
+#pragma unroll
+    for (uint32_t t = 0; t < 2; ++t) {
       const uint32_t w = w2 + t;
+      if (w >= wn)
+        break;
       const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
                      C1 = __ldg(m1 + w);
       const uint32_t lo = work_sample_site(p, pcr, s, w * 64 + lane, A0, A1, C0, C1,
