@@ -165,7 +165,7 @@ def accuracy(w, m, haps, ds, seed, device, recluster=0):
 # the batched workload itself (N = 10,000, S = 4,096, C = 100, 8 lanes, float
 # emission), one launch, no scaling: every speculative round streams its
 # sample's emission row again, mostly from DRAM.
-NCU_TRAFFIC_BATCHED = 18.750250240e9 + 0.004036096e9
+NCU_TRAFFIC_BATCHED = 18.977837568e9 + 0.004564480e9
 
 
 def traffic_per_launch(N, S, C, args):
