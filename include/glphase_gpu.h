@@ -401,9 +401,9 @@ int glp_result(glp_ctx *ctx, const uint32_t *hsum, uint32_t num_samples, uint32_
  * sets the kernels' launch attributes; later calls in the same context reuse
  * that set-up.  Any context is supported: the set-up is kept per context id,
  * so a context made after cudaDeviceReset or with the driver API gets its
- * own.  Make the first call in a context before any stream capture begins.
- * Every call copies the device error flag back and synchronizes `stream`
- * before it returns.  Calls share the one array, which keeps what the last
+ * own.  Every call copies the device error flag back into host memory and
+ * synchronizes `stream` before it returns, so no call may be made while a
+ * stream is capturing (a CUDA graph cannot hold it).  Calls share the one array, which keeps what the last
  * call left there (each call clears the counters and flag it reads): calls
  * that overlap on the GPU (other host threads, other streams) race and must
  * be serialized by the caller. */
