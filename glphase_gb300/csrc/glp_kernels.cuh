@@ -630,7 +630,7 @@ __device__ __forceinline__ double eval_pair(const GenParams &p, const E &em, uin
 }
 
 // ---------------------------------------------------------------------------
-// hmm_work, one sample per lane, binary32 in the reference's operation order
+// hmm_work, binary32 in the reference's operation order
 // (impute.cpp:380-485): explicit _rn intrinsics keep nvcc from contracting
 // products and sums into FMAs, so results are bit-identical to the CPU code.
 
@@ -651,108 +651,6 @@ __device__ __forceinline__ float fma3_rn(float a0, float b0, float a1, float b1,
 // correctly rounded reciprocal, which is what __frcp_rn returns for every
 // input, with a shorter dependency chain than the general division.
 __device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
-
-// One backward step of impute.cpp:389-414: b <- normalise(T (b * e)), with
-// the emission picks i_ab = (father bit << 1) | mother bit of the site.
-__device__ __forceinline__ float4 pick4(const float4 em, uint32_t i00, uint32_t i01,
-                                        uint32_t i10, uint32_t i11) {
-  return make_float4(pick(em, i00), pick(em, i01), pick(em, i10), pick(em, i11));
-}
-
-// The same step with the four emission values already picked (e = pick4(...)).
-__device__ __forceinline__ void work_bwd_math(float &b0, float &b1, float &b2, float &b3,
-                                              const float4 e, const float4 t) {
-  const float b00 = __fmul_rn(b0, e.x);
-  const float b01 = __fmul_rn(b1, e.y);
-  const float b10 = __fmul_rn(b2, e.z);
-  const float b11 = __fmul_rn(b3, e.w);
-  b0 = __fadd_rn(__fadd_rn(__fmul_rn(b00, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
-                 __fmul_rn(b11, t.z));
-  b1 = __fadd_rn(__fadd_rn(__fmul_rn(b01, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
-                 __fmul_rn(b10, t.z));
-  b2 = __fadd_rn(__fadd_rn(__fmul_rn(b10, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
-                 __fmul_rn(b01, t.z));
-  b3 = __fadd_rn(__fadd_rn(__fmul_rn(b11, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
-                 __fmul_rn(b00, t.z));
-  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(b0, b1), b2), b3));
-  b0 = __fmul_rn(b0, sum);
-  b1 = __fmul_rn(b1, sum);
-  b2 = __fmul_rn(b2, sum);
-  b3 = __fmul_rn(b3, sum);
-}
-
-__device__ __forceinline__ void work_fwd_math(float &l00, float &l01, float &l10, float &l11,
-                                              const float4 e, const float4 t, bool first) {
-  if (!first) {
-    const float c00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
-    const float c01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
-    const float c10 = fma3_rn(l00, t.y, l01, t.z, l10, t.x, l11, t.y);
-    const float c11 = fma3_rn(l00, t.z, l01, t.y, l10, t.y, l11, t.x);
-    l00 = __fmul_rn(c00, e.x);
-    l01 = __fmul_rn(c01, e.y);
-    l10 = __fmul_rn(c10, e.z);
-    l11 = __fmul_rn(c11, e.w);
-  } else {
-    l00 = __fmul_rn(0.25f, e.x);
-    l01 = __fmul_rn(0.25f, e.y);
-    l10 = __fmul_rn(0.25f, e.z);
-    l11 = __fmul_rn(0.25f, e.w);
-  }
-  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(l00, l01), l10), l11));
-  l00 = __fmul_rn(l00, sum);
-  l01 = __fmul_rn(l01, sum);
-  l10 = __fmul_rn(l10, sum);
-  l11 = __fmul_rn(l11, sum);
-}
-
-__device__ __forceinline__ void work_bwd_step(float &b0, float &b1, float &b2, float &b3,
-                                              const float4 em, const float4 t, uint32_t i00,
-                                              uint32_t i01, uint32_t i10, uint32_t i11) {
-  const float b00 = __fmul_rn(b0, pick(em, i00));
-  const float b01 = __fmul_rn(b1, pick(em, i01));
-  const float b10 = __fmul_rn(b2, pick(em, i10));
-  const float b11 = __fmul_rn(b3, pick(em, i11));
-  b0 = __fadd_rn(__fadd_rn(__fmul_rn(b00, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
-                 __fmul_rn(b11, t.z));
-  b1 = __fadd_rn(__fadd_rn(__fmul_rn(b01, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
-                 __fmul_rn(b10, t.z));
-  b2 = __fadd_rn(__fadd_rn(__fmul_rn(b10, t.x), __fmul_rn(__fadd_rn(b00, b11), t.y)),
-                 __fmul_rn(b01, t.z));
-  b3 = __fadd_rn(__fadd_rn(__fmul_rn(b11, t.x), __fmul_rn(__fadd_rn(b01, b10), t.y)),
-                 __fmul_rn(b00, t.z));
-  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(b0, b1), b2), b3));
-  b0 = __fmul_rn(b0, sum);
-  b1 = __fmul_rn(b1, sum);
-  b2 = __fmul_rn(b2, sum);
-  b3 = __fmul_rn(b3, sum);
-}
-
-// One forward step of impute.cpp:416-447 (site 0 when first).
-__device__ __forceinline__ void work_fwd_step(float &l00, float &l01, float &l10, float &l11,
-                                              const float4 em, const float4 t, uint32_t i00,
-                                              uint32_t i01, uint32_t i10, uint32_t i11,
-                                              bool first) {
-  if (!first) {
-    const float c00 = fma3_rn(l00, t.x, l01, t.y, l10, t.y, l11, t.z);
-    const float c01 = fma3_rn(l00, t.y, l01, t.x, l10, t.z, l11, t.y);
-    const float c10 = fma3_rn(l00, t.y, l01, t.z, l10, t.x, l11, t.y);
-    const float c11 = fma3_rn(l00, t.z, l01, t.y, l10, t.y, l11, t.x);
-    l00 = __fmul_rn(c00, pick(em, i00));
-    l01 = __fmul_rn(c01, pick(em, i01));
-    l10 = __fmul_rn(c10, pick(em, i10));
-    l11 = __fmul_rn(c11, pick(em, i11));
-  } else {
-    l00 = __fmul_rn(0.25f, pick(em, i00));
-    l01 = __fmul_rn(0.25f, pick(em, i01));
-    l10 = __fmul_rn(0.25f, pick(em, i10));
-    l11 = __fmul_rn(0.25f, pick(em, i11));
-  }
-  const float sum = recip_rn(__fadd_rn(__fadd_rn(__fadd_rn(l00, l01), l10), l11));
-  l00 = __fmul_rn(l00, sum);
-  l01 = __fmul_rn(l01, sum);
-  l10 = __fmul_rn(l10, sum);
-  l11 = __fmul_rn(l11, sum);
-}
 
 // hmm_work is split in two passes with the reference's arithmetic unchanged.
 // The forward state l_m of impute.cpp:416-447 does not depend on the sampled
