@@ -395,9 +395,16 @@ def run_ours(args):
     H, wn = haps.shape
     packed = codebook = None
     if args.vq:
+        # the codebook trained and the codes packed by the device codec (bit
+        # for bit the host GLPack's result, in a fraction of a second)
         from glphase_gb300.glpack import GLPack
-        gp = GLPack(m.t, np.random.default_rng(1))
-        packed, codebook = gp.packed_gls(), gp.code_book()
+        from glphase_gb300.hmmlike import HMMLikeCUDA
+        codec = HMMLikeCUDA(local)
+        try:
+            gp = GLPack(m.t, np.random.default_rng(1), device=codec)
+            packed, codebook = gp.packed_gls(), gp.code_book()
+        finally:
+            codec.cleanup()
     eng = Engine(m.emit, m.t, m.tran, m.pc, haps, C, device=local, lanes=args.lanes,
                  packed=packed, codebook=codebook,
                  block_sites=args.block_sites)

@@ -11,7 +11,8 @@ checked against the CPU oracle at the sizes the benchmark runs:
   * batched: 10,000 samples x 4,096 sites, C = 100, surrogates from the
     device-built K = 200 Hamming-neighbour table (KNN::ClusterHaps,
     kNN.cpp:99-206), one generation in the annealing ramp and one at full
-    penalty; a seeded subset of 256 samples replayed on the oracle;
+    penalty; a seeded subset of 256 samples replayed on the oracle; and the
+    same shape scored from 4-bit VQ GL codes;
   * panel: 2,000 samples + 10,000 panel haplotypes x 8,192 sites; generation 0
     draws its surrogates from the panel only (the kick-start), generation 1
     from panel and samples with every chain's first proposal from the panel
@@ -128,6 +129,42 @@ def test_batched_config_shape(oracle_lib):
     finally:
         eng.dev.cleanup()
     report("batched 10000x4096 C=100 kNN K=200", worst, worst64, checked)
+
+
+def test_batched_vq_config_shape(oracle_lib):
+    """10,000 x 4,096, C = 100, K = 200 device kNN surrogates, likelihoods
+    from 4-bit VQ GL codes (GLPack / GLVQ, trained and packed by the device
+    codec): 256 seeded samples of a full-penalty generation replayed on the
+    oracle's VQ emission."""
+    from glphase_gb300.glpack import GLPack
+    from glphase_gb300.hmmlike import Engine, HMMLikeCUDA
+    O = oracle_lib
+    w = synth.CONFIGS["batched"]
+    ds = synth.generate(w)
+    m, haps = synth.initial_state(ds)
+    codec = HMMLikeCUDA(0)
+    try:
+        gp = GLPack(m.t, np.random.default_rng(1), device=codec)
+        packed, cb = gp.packed_gls(), gp.code_book()
+    finally:
+        codec.cleanup()
+    eng = Engine(m.emit, m.t, m.tran, m.pc, haps, w.cycles, packed=packed, codebook=cb)
+    try:
+        nbr = eng.knn(w.knn)
+        eng.finish()
+        nbr_host = np.ascontiguousarray(nbr.cpu().numpy().view(np.uint32)[:m.N])
+        gen = 9
+        pen = float(anneal_pen(gen, w.burnin))
+        h_in, out = _engine_generation(eng, pen, 31, gen, nbr=nbr)
+        quad, props = O.sample_surrogates(31, gen, m.N, w.cycles, 0, h_in.shape[0],
+                                          nbr=nbr_host)
+        sub = _subset(m.N, 256, 77)
+        worst, worst64 = check_samples(O, m.emit, m.t, m.tran, m.pc, h_in, quad, props, pen,
+                                       out, sub, 31, gen, vq=(packed, cb))
+        assert np.isfinite(out["evals"][:, 0]).all()
+    finally:
+        eng.dev.cleanup()
+    report("batched VQ 10000x4096 C=100 kNN K=200", worst, worst64, len(sub))
 
 
 def test_panel_config_shape(oracle_lib):
