@@ -115,6 +115,7 @@ struct glp_ctx {
   // generation recomputes more than 0.1 % of its evaluations site by site,
   // then 4 for the rest of the context's life
   uint32_t block_sites = 0;
+  int knn_metric = GLP_KNN_HAMMING;  // glp_set_knn_metric
   bool short_blocks = false;
   // resident threads per lane width (1 .. 32), per [multi-chunk][VQ] kernel
   double resident[2][2][6] = {};
@@ -1221,6 +1222,15 @@ int glp_set_evals_per_lane(glp_ctx *c, uint32_t evals) {
   return GLP_OK;
 }
 
+int glp_set_knn_metric(glp_ctx *c, int metric) {
+  if (!c)
+    return GLP_ERR_ARG;
+  if (metric != GLP_KNN_HAMMING && metric != GLP_KNN_TRACT)
+    return fail(c, GLP_ERR_ARG, "kNN metric must be GLP_KNN_HAMMING or GLP_KNN_TRACT");
+  c->knn_metric = metric;
+  return GLP_OK;
+}
+
 int glp_set_block_sites(glp_ctx *c, uint32_t sites) {
   if (!c)
     return GLP_ERR_ARG;
@@ -1552,7 +1562,7 @@ int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, 
   GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
   glp::knn_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask, half,
-                                                                 S, neighbors);
+                                                                 S, c->knn_metric, neighbors);
   GLP_CUDA(c, cudaGetLastError());
   return GLP_OK;
 }

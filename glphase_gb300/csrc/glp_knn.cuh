@@ -1,6 +1,8 @@
 // glp_knn.cuh -- kNN surrogate restriction on the device: the reference's
 // KNN::ClusterHaps (src/kNN.cpp:123-206) with the Hamming metric
-// (src/haplotype.cpp:35-60) over the common sites of KNN::CutDownHaps
+// (src/haplotype.cpp:35-60) or the tract-length metric (insti -T: the number
+// of common sites minus Haplotype::MaxTractLen, src/haplotype.cpp:62-90,
+// kNN.cpp:157-164) over the common sites of KNN::CutDownHaps
 // (src/kNN.cpp:216-257).
 //
 // For each sample s of the H/2 samples: the ceil(K/2) haplotypes nearest to
@@ -12,7 +14,10 @@
 //
 // One CTA per sample.  Distances of both haplotypes to all H haplotypes sit
 // in shared memory as uint16 (H <= kKnnMaxHaps); every warp scores one
-// haplotype at a time with coalesced word loads and a shuffle reduction.  The
+// haplotype at a time with coalesced word loads and a shuffle reduction (for
+// the tract length an ordered one: each word's runs of agreeing common sites
+// -- before its first disagreement, after its last, the longest between --
+// combine left to right).  The
 // ceil(K/2) nearest are found by binary search on the distance threshold,
 // ties at the threshold are taken in index order through a block scan, and
 // the chosen list is put in (distance, index) order by a bitonic sort.
@@ -54,6 +59,65 @@ __global__ void common_sites_kernel(const uint64_t *__restrict__ haps, uint32_t 
   __syncthreads();
   if (lane == 0)
     mask[w] = (uint64_t)lo | ((uint64_t)hi_bits << 32);
+}
+
+// Runs of agreeing common sites in a stretch of words: len common sites, pre
+// of them before the first disagreement, suf after the last, best the longest
+// run; pre == len when the stretch has no disagreement.
+struct Tract {
+  uint32_t len, pre, suf, best;
+};
+
+// One word: x the disagreements at common sites, m the common sites.
+__device__ __forceinline__ Tract tract_word(uint64_t x, uint64_t m) {
+  Tract t;
+  t.len = (uint32_t)__popcll(m);
+  if (x == 0) {
+    t.pre = t.suf = t.best = t.len;
+    return t;
+  }
+  const int lo = __ffsll((long long)x) - 1, hi = 63 - __clzll((long long)x);
+  t.pre = (uint32_t)__popcll(m & ((1ull << lo) - 1ull));
+  t.suf = hi == 63 ? 0u : (uint32_t)__popcll(m >> (hi + 1));
+  uint32_t best = max(t.pre, t.suf);
+  int prev = lo;
+  for (uint64_t y = x & (x - 1ull); y; y &= y - 1ull) {  // runs between disagreements
+    const int q = __ffsll((long long)y) - 1;           // prev < q <= 63
+    const uint64_t between = ((1ull << q) - 1ull) & ~((2ull << prev) - 1ull);
+    best = max(best, (uint32_t)__popcll(m & between));
+    prev = q;
+  }
+  t.best = best;
+  return t;
+}
+
+// The stretch l followed by the stretch r.
+__device__ __forceinline__ Tract tract_join(const Tract l, const Tract r) {
+  Tract t;
+  t.len = l.len + r.len;
+  t.pre = l.pre == l.len ? l.len + r.pre : l.pre;
+  t.suf = r.suf == r.len ? r.len + l.suf : r.suf;
+  t.best = max(max(l.best, r.best), l.suf + r.pre);
+  return t;
+}
+
+// Joins the 32 lanes' stretches in lane order; every lane gets the result.
+__device__ __forceinline__ Tract tract_warp(Tract t, uint32_t lane) {
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    Tract r;
+    r.len = __shfl_down_sync(0xffffffffu, t.len, o);
+    r.pre = __shfl_down_sync(0xffffffffu, t.pre, o);
+    r.suf = __shfl_down_sync(0xffffffffu, t.suf, o);
+    r.best = __shfl_down_sync(0xffffffffu, t.best, o);
+    if ((lane & (2 * o - 1)) == 0)
+      t = tract_join(t, r);
+  }
+  t.len = __shfl_sync(0xffffffffu, t.len, 0);
+  t.pre = __shfl_sync(0xffffffffu, t.pre, 0);
+  t.suf = __shfl_sync(0xffffffffu, t.suf, 0);
+  t.best = __shfl_sync(0xffffffffu, t.best, 0);
+  return t;
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *red) {
@@ -187,7 +251,7 @@ __device__ void select_nearest(const uint16_t *d, uint32_t H, uint32_t half, uin
 // chosen [2*kKnnMaxHalf] uint32, taken bits [ceil(H/32)] uint32.
 __global__ void __launch_bounds__(kKnnThreads)
     knn_kernel(const uint64_t *__restrict__ haps, uint32_t H, uint32_t wn,
-               const uint64_t *__restrict__ mask, uint32_t half, uint32_t dmax,
+               const uint64_t *__restrict__ mask, uint32_t half, uint32_t dmax, int metric,
                uint32_t *__restrict__ neighbors) {
   extern __shared__ uint4 knn_smem[];
   uint16_t *dA = reinterpret_cast<uint16_t *>(knn_smem);
@@ -205,15 +269,32 @@ __global__ void __launch_bounds__(kKnnThreads)
   for (uint32_t h = warp; h < H; h += kKnnThreads / 32) {
     uint32_t a = 0, b = 0;
     const uint64_t *o = haps + (size_t)h * wn;
-    for (uint32_t w = lane; w < wn; w += 32) {
-      const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
-      a += __popcll((__ldg(ha + w) ^ ow) & mw);
-      b += __popcll((__ldg(hb + w) ^ ow) & mw);
-    }
+    if (metric == 0) {
+      for (uint32_t w = lane; w < wn; w += 32) {
+        const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
+        a += __popcll((__ldg(ha + w) ^ ow) & mw);
+        b += __popcll((__ldg(hb + w) ^ ow) & mw);
+      }
 #pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, off);
-      b += __shfl_xor_sync(0xffffffffu, b, off);
+      for (int off = 16; off; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+      }
+    } else {  // common sites minus the longest run of agreeing common sites
+      Tract ta = {0, 0, 0, 0}, tb = {0, 0, 0, 0};
+      for (uint32_t w0 = 0; w0 < wn; w0 += 32) {
+        const uint32_t w = w0 + lane;
+        Tract xa = {0, 0, 0, 0}, xb = {0, 0, 0, 0};
+        if (w < wn) {
+          const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
+          xa = tract_word((__ldg(ha + w) ^ ow) & mw, mw);
+          xb = tract_word((__ldg(hb + w) ^ ow) & mw, mw);
+        }
+        ta = tract_join(ta, tract_warp(xa, lane));
+        tb = tract_join(tb, tract_warp(xb, lane));
+      }
+      a = ta.len - ta.best;
+      b = tb.len - tb.best;
     }
     if (lane == 0) {
       const bool own = (h >> 1) == s;

@@ -240,11 +240,15 @@ class Engine:
         torch.cuda.current_stream(self.device).synchronize()
         self.dev._c(self.dev.L.glp_set_stream(self.dev.ctx, self.stream.cuda_stream))
 
-    def knn(self, k: int, freq_lb: float = 0.0, freq_ub: float = 1.0, use_maf: bool = False):
+    def knn(self, k: int, freq_lb: float = 0.0, freq_ub: float = 1.0, use_maf: bool = False,
+            metric: str = "hamming"):
         """Neighbour table of the current haplotypes on the device
-        (KNN::ClusterHaps, kNN.cpp:123-206); kept for the in-kernel draws."""
+        (KNN::ClusterHaps, kNN.cpp:123-206); kept for the in-kernel draws.
+        metric "hamming" or "tract" (the common sites minus the longest shared
+        tract, insti -T)."""
         torch = self.torch
         half = (k + 1) // 2
+        self.dev._c(self.dev.L.glp_set_knn_metric(self.dev.ctx, nat.KNN_METRICS[metric]))
         self.nbr = torch.zeros((self.H // 2, 2 * half), dtype=torch.int32, device=self.device)
         self.dev._c(self.dev.L.glp_knn_neighbors(self.dev.ctx, self.haps.data_ptr(), self.H,
                                                  self.S, k, freq_lb, freq_ub, int(use_maf),

@@ -22,6 +22,9 @@ GLP_ERR_NO_CONVERGE = 8
 
 GLP_GEN_VQ = 1
 GLP_GEN_NO_WORK = 2
+GLP_KNN_HAMMING = 0
+GLP_KNN_TRACT = 1
+KNN_METRICS = {"hamming": GLP_KNN_HAMMING, "tract": GLP_KNN_TRACT}
 GLP_GEN_KICK_FIRST = 4
 
 GLP_REQ_QUEUED = 0
@@ -40,7 +43,7 @@ EXPORTED = [
     "glp_set_evals_per_lane", "glp_get_counters", "glp_kernel_times", "glp_vq_train",
     "glp_vq_pack", "glp_set_block_sites", "glp_get_block_sites", "glp_server_create",
     "glp_server_submit", "glp_server_tick", "glp_server_poll", "glp_server_stats",
-    "glp_server_destroy", "glp_server_release",
+    "glp_server_destroy", "glp_server_release", "glp_set_knn_metric",
 ]
 
 
@@ -132,6 +135,7 @@ def load(build_if_missing: bool = False):
     L.glp_vq_train.argtypes = [vp, vp, C.c_uint64, u32, vp, C.c_uint64, u32, vp]
     L.glp_vq_pack.argtypes = [vp, vp, u32, u32, vp, u32, u32, vp]
     L.glp_set_block_sites.argtypes = [vp, u32]
+    L.glp_set_knn_metric.argtypes = [vp, i32]
     L.glp_get_block_sites.argtypes = [vp, vp]
     L.glp_run_batch.argtypes = [vp, u32, C.POINTER(vp), C.POINTER(GenerationArgs)]
     L.glp_server_create.argtypes = [vp, u64, i32, C.POINTER(vp)]

@@ -49,6 +49,7 @@ class PhaseOptions:
     knn: int = 0              # K nearest-neighbour surrogates (0: uniform)
     cluster_start: int = 0    # generation from which the kNN sampler is used
     recluster: int = 0        # -r: rebuild the kNN table every r generations after burn-in
+    knn_metric: str = "hamming"  # or "tract": -T, common sites minus the longest shared tract
     lanes: int = 0            # speculation width (0: chosen per generation)
     kick_start: bool = False  # generation 0 draws its surrogates from the panel rows only
     kick_first: bool = False  # every chain's first proposal from the panel (--kickstart)
@@ -94,7 +95,7 @@ def phase(model: mdl.Model, haps: np.ndarray, opts: PhaseOptions):
     nbr = table = None
     for g in range(opts.generations):
         if g in builds:
-            table = eng.knn(opts.knn)
+            table = eng.knn(opts.knn, metric=opts.knn_metric)
         # the table is the sampler from cluster_start on
         nbr = table if opts.knn and g >= opts.cluster_start else None
         pen = float(anneal_pen(g, opts.sa_burnin))

@@ -316,16 +316,25 @@ int glp_server_stats(glp_server *server, uint64_t *ticks, uint64_t *updates,
 void glp_server_destroy(glp_server *server);
 
 /* kNN surrogate restriction on the device: for each of the H/2 samples,
- * the ceil(K/2) haplotypes nearest (Hamming distance over the sites whose
+ * the ceil(K/2) haplotypes nearest (over the common sites, those whose
  * alt-allele frequency, or MAF when use_maf, lies in [freq_lb, freq_ub]) to
  * its first haplotype, then the ceil(K/2) nearest to its second that are not
- * yet chosen, interleaved; ties in index order.  haps and neighbors
- * ([H/2][2*ceil(K/2)]) are DEVICE pointers; asynchronous, finish with
- * glp_finish().  Replaces KNN::KNN / KNN::ClusterHaps (src/kNN.cpp:7-206)
- * with the Hamming metric.  Needs H <= 50000 and 2*ceil(K/2) <= H - 2. */
+ * yet chosen, interleaved; ties in index order.  The distance is the context's
+ * kNN metric (glp_set_knn_metric): the Hamming distance by default, or the
+ * number of common sites minus the longest run of common sites at which the
+ * two haplotypes agree (Haplotype::MaxTractLen, src/haplotype.cpp:62-90;
+ * insti -T, src/kNN.cpp:157-164).  haps and neighbors ([H/2][2*ceil(K/2)])
+ * are DEVICE pointers; asynchronous, finish with glp_finish().  Replaces
+ * KNN::KNN / KNN::ClusterHaps (src/kNN.cpp:7-206).  Needs H <= 50000 and
+ * 2*ceil(K/2) <= H - 2. */
 int glp_knn_neighbors(glp_ctx *ctx, const uint64_t *haps, uint32_t num_haps, uint32_t num_sites,
                       uint32_t k, double freq_lb, double freq_ub, int use_maf,
                       uint32_t *neighbors);
+/* The distance glp_knn_neighbors uses from now on in this context:
+ * GLP_KNN_HAMMING (the default) or GLP_KNN_TRACT (GLP_ERR_ARG otherwise). */
+#define GLP_KNN_HAMMING 0
+#define GLP_KNN_TRACT 1
+int glp_set_knn_metric(glp_ctx *ctx, int metric);
 
 /* Allele tallies of a sampling generation for all N samples: for each
  * sample, hsum rows 2i and 2i+1 ([2N][S] uint32) gain the sample's two

@@ -515,9 +515,41 @@ static uint32_t hamming_masked(const uint64_t *a, const uint64_t *b,
   return d;
 }
 
-/* kNN.cpp:123-206 */
+/* Haplotype::MaxTractLen (haplotype.cpp:62-90) over the common sites of
+   KNN::CutDownHaps (kNN.cpp:216-257): the longest run of consecutive common
+   sites at which a and b agree; sites outside the mask are not part of the
+   cut-down haplotypes, so they neither extend nor break a run. */
+uint32_t glpo_max_tract(const uint64_t *a, const uint64_t *b, const uint64_t *mask,
+                        uint32_t wn) {
+  uint32_t best = 0, run = 0;
+  for (uint32_t w = 0; w < wn; ++w)
+    for (uint32_t j = 0; j < 64; ++j) {
+      if (!((mask[w] >> j) & 1u))
+        continue;
+      if (((a[w] ^ b[w]) >> j) & 1u) {
+        if (run > best)
+          best = run;
+        run = 0;
+      } else {
+        ++run;
+      }
+    }
+  return run > best ? run : best;
+}
+
+/* kNN.cpp:123-206 with the Hamming metric */
 int glpo_knn(const uint64_t *haps, uint32_t H, uint32_t wn, const uint64_t *mask,
              uint32_t K, uint32_t *neighbors) {
+  return glpo_knn_metric(haps, H, wn, mask, K, 0, neighbors);
+}
+
+/* kNN.cpp:123-206; metric 0: Hamming distance (kNN.cpp:151-153), 1: the
+   number of common sites minus the longest shared tract (kNN.cpp:157-164) */
+int glpo_knn_metric(const uint64_t *haps, uint32_t H, uint32_t wn, const uint64_t *mask,
+                    uint32_t K, int metric, uint32_t *neighbors) {
+  uint32_t ncommon = 0;
+  for (uint32_t w = 0; w < wn; ++w)
+    ncommon += (uint32_t)__builtin_popcountll(mask[w]);
   const uint32_t half = (K + 1) / 2, len = 2 * half, ns = H / 2;
   if (H < 2 || H - 2 < len)
     return -1;
@@ -542,9 +574,14 @@ int glpo_knn(const uint64_t *haps, uint32_t H, uint32_t wn, const uint64_t *mask
           if ((h >> 1) == (uint32_t)s)
             continue;
           const uint64_t *o = haps + (size_t)h * wn;
-          da[n].d = hamming_masked(ha, o, mask, wn);
+          if (metric == 1) {
+            da[n].d = ncommon - glpo_max_tract(ha, o, mask, wn);
+            db[n].d = ncommon - glpo_max_tract(hb, o, mask, wn);
+          } else {
+            da[n].d = hamming_masked(ha, o, mask, wn);
+            db[n].d = hamming_masked(hb, o, mask, wn);
+          }
           da[n].idx = h;
-          db[n].d = hamming_masked(hb, o, mask, wn);
           db[n].idx = h;
           ++n;
         }

@@ -166,6 +166,10 @@ void glpo_common_sites(const uint64_t *haps, uint32_t H, uint32_t wn, uint32_t S
  * length. */
 int glpo_knn(const uint64_t *haps, uint32_t H, uint32_t wn, const uint64_t *mask,
              uint32_t K, uint32_t *neighbors);
+int glpo_knn_metric(const uint64_t *haps, uint32_t H, uint32_t wn, const uint64_t *mask,
+                    uint32_t K, int metric, uint32_t *neighbors);
+uint32_t glpo_max_tract(const uint64_t *a, const uint64_t *b, const uint64_t *mask,
+                        uint32_t wn);
 
 /* Impute::replace (impute.cpp:564-595): per-site allele tallies, hsum is
  * [2N][S] uint32. */

@@ -95,6 +95,11 @@ def lib():
                                         C.c_double, C.c_int, _u64p]
         L.glpo_knn.restype = C.c_int
         L.glpo_knn.argtypes = [_u64p, C.c_uint32, C.c_uint32, _u64p, C.c_uint32, _u32p]
+        L.glpo_knn_metric.restype = C.c_int
+        L.glpo_knn_metric.argtypes = [_u64p, C.c_uint32, C.c_uint32, _u64p, C.c_uint32,
+                                      C.c_int, _u32p]
+        L.glpo_max_tract.restype = C.c_uint32
+        L.glpo_max_tract.argtypes = [_u64p, _u64p, _u64p, C.c_uint32]
         L.glpo_replace.argtypes = [_u64p, C.c_uint32, C.c_uint32, C.c_uint32, _u32p]
         L.glpo_result.argtypes = [_u32p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
         _lib = L
@@ -271,13 +276,28 @@ def common_sites(haps, S, lb=0.0, ub=1.0, use_maf=False):
     return mask
 
 
-def knn(haps, S, K, lb=0.0, ub=1.0, use_maf=False):
-    """KNN::ClusterHaps restated: [H/2][2*ceil(K/2)] neighbour lists."""
+KNN_METRICS = {"hamming": 0, "tract": 1}
+
+
+def knn(haps, S, K, lb=0.0, ub=1.0, use_maf=False, metric="hamming"):
+    """KNN::ClusterHaps restated: [H/2][2*ceil(K/2)] neighbour lists.
+    metric "hamming" (the default) or "tract": the number of common sites
+    minus the longest shared tract (insti -T)."""
     haps = _c(haps, np.uint64)
     H, wn = haps.shape
     mask = common_sites(haps, S, lb, ub, use_maf)
     half = (K + 1) // 2
     out = np.zeros((H // 2, 2 * half), np.uint32)
-    if lib().glpo_knn(haps, H, wn, mask, K, out) != 0:
+    if lib().glpo_knn_metric(haps, H, wn, mask, K, KNN_METRICS[metric], out) != 0:
         raise ValueError("kNN list longer than the available haplotypes")
     return out
+
+
+def max_tract(a, b, mask=None):
+    """Haplotype::MaxTractLen of two packed haplotypes (uint64 words) over the
+    sites set in mask (all sites of the words when None)."""
+    a = _c(np.atleast_1d(a), np.uint64)
+    b = _c(np.atleast_1d(b), np.uint64)
+    if mask is None:
+        mask = np.full(a.shape, np.uint64(0xFFFFFFFFFFFFFFFF))
+    return int(lib().glpo_max_tract(a, b, _c(mask, np.uint64), a.shape[0]))

@@ -22,7 +22,7 @@ def oracle_phase(O, model, haps, opts, nthreads=0):
     table = None
     for g in range(opts.generations):
         if g in builds:   # KNN::ClusterHaps on the current haplotypes
-            table = np.ascontiguousarray(O.knn(cur, S, opts.knn)[:N])
+            table = np.ascontiguousarray(O.knn(cur, S, opts.knn, metric=opts.knn_metric)[:N])
         nbr = table if opts.knn and g >= opts.cluster_start else None
         pb = O.OracleProblem(cur, model.emit, model.t, model.tran, model.pc, Cc)
         panel = H > 2 * N

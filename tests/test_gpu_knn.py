@@ -20,13 +20,14 @@ def dev():
     d.cleanup()
 
 
-def gpu_knn(dev, haps, S, K, lb=0.0, ub=1.0, use_maf=False):
+def gpu_knn(dev, haps, S, K, lb=0.0, ub=1.0, use_maf=False, metric="hamming"):
     import torch
     H, wn = haps.shape
     half = (K + 1) // 2
     h = torch.from_numpy(np.ascontiguousarray(haps).view(np.int64)).cuda()
     out = torch.zeros((H // 2, 2 * half), dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
+    dev._c(dev.L.glp_set_knn_metric(dev.ctx, nat.KNN_METRICS[metric]))
     dev._c(dev.L.glp_knn_neighbors(dev.ctx, h.data_ptr(), H, S, K, lb, ub, int(use_maf),
                                    out.data_ptr()))
     dev._c(dev.L.glp_finish(dev.ctx))
@@ -53,6 +54,37 @@ def test_knn_matches_oracle(dev, oracle_lib, H, S, K):
     want = oracle_lib.knn(haps, S, K)
     got = gpu_knn(dev, haps, S, K)
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("H,S,K", [(40, 130, 7), (200, 1000, 20), (1000, 700, 200),
+                                   (4000, 4096, 200)])
+def test_knn_tract_metric_matches_oracle(dev, oracle_lib, H, S, K):
+    """insti -T: the common sites minus the longest shared tract
+    (Haplotype::MaxTractLen, haplotype.cpp:62-90; kNN.cpp:157-164)."""
+    rng = np.random.default_rng(H + 2 * S)
+    founders = rng.integers(0, 2, size=(8, S)).astype(np.uint8)
+    bits = founders[rng.integers(0, 8, size=H)]
+    flip = rng.random((H, S)) < 0.02
+    bits = (bits ^ flip).astype(np.uint8)
+    haps = mdl.pack_haplotypes(bits)
+    want = oracle_lib.knn(haps, S, K, metric="tract")
+    got = gpu_knn(dev, haps, S, K, metric="tract")
+    assert np.array_equal(got, want)
+    assert not np.array_equal(want, oracle_lib.knn(haps, S, K))  # the metrics differ here
+
+
+def test_knn_tract_metric_with_frequency_bounds(dev, oracle_lib):
+    rng = np.random.default_rng(6)
+    bits = (rng.random((300, 500)) < rng.beta(0.5, 0.5, 500)[None, :]).astype(np.uint8)
+    haps = mdl.pack_haplotypes(bits)
+    for lb, ub, maf in ((0.05, 0.95, False), (0.1, 0.5, True)):
+        assert np.array_equal(gpu_knn(dev, haps, 500, 30, lb, ub, maf, metric="tract"),
+                              oracle_lib.knn(haps, 500, 30, lb, ub, maf, metric="tract"))
+
+
+def test_knn_metric_argument(dev):
+    assert dev.L.glp_set_knn_metric(dev.ctx, 2) == nat.GLP_ERR_ARG
+    assert dev.L.glp_set_knn_metric(dev.ctx, nat.GLP_KNN_HAMMING) == nat.GLP_OK
 
 
 def test_knn_with_frequency_bounds(dev, oracle_lib):

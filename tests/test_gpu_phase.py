@@ -122,6 +122,21 @@ def test_panel_phasing_matches_oracle(oracle_lib, kick):
     assert np.array_equal(prob, want_prob)
 
 
+def test_knn_tract_metric_loop_matches_oracle(oracle_lib):
+    """insti -T -k: the kNN sampler on the tract-length metric, rebuilt every
+    3 generations after burn-in; the device loop equals the oracle loop bit
+    for bit."""
+    from phase_oracle import oracle_phase
+    ds, pos, gmap, truth = cohort()
+    opts = ph.PhaseOptions(sa_burnin=4, burnin=4, sampling=8, cycles=50, seed=5, knn=30,
+                           cluster_start=2, recluster=3, knn_metric="tract")
+    m, haps = ph.prepare(ds.gl_het_alt, pos, gmap, seed=opts.seed)
+    prob, final = ph.phase(m, haps, opts)
+    want_prob, want_haps = oracle_phase(oracle_lib, m, haps, opts)
+    assert np.array_equal(final, want_haps)
+    assert np.array_equal(prob, want_prob)
+
+
 def test_knn_recluster_matches_oracle(oracle_lib):
     """The kNN sampler (K = 40 from generation 3) rebuilt from the current
     haplotypes every 2 generations after the 10 burn-in generations (the

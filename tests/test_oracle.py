@@ -305,3 +305,76 @@ def test_fp16_gl_storage_exceeds_the_loglik_bound(oracle_lib):
             else:
                 worst_gl = max(worst_gl, rel)
     assert worst_e > 1e-5 and worst_gl > 1e-5, (worst_e, worst_gl)
+
+
+def _hap(n, sites=()):
+    from glphase_gb300 import model as mdl
+    b = np.zeros((1, n), np.uint8)
+    for i in sites:
+        b[0, i] = 1
+    return mdl.pack_haplotypes(b)[0]
+
+
+def _all_sites(n):
+    m = np.zeros((n + 63) // 64, np.uint64)
+    for i in range(n):
+        m[i >> 6] |= np.uint64(1) << np.uint64(i & 63)
+    return m
+
+
+def test_max_tract_reference_kat(oracle_lib):
+    """Haplotype::MaxTractLen's known answers (src/testing/other_unittests.cpp:79-101)."""
+    O = oracle_lib
+    a, b = _hap(4), _hap(4, (0, 3))
+    assert O.max_tract(a, a, _all_sites(4)) == 4
+    assert O.max_tract(a, b, _all_sites(4)) == 2
+    c, d = _hap(1024), _hap(1024, (23,))
+    m = _all_sites(1024)
+    assert O.max_tract(c, c, m) == 1024
+    assert O.max_tract(c, d, m) == 1000
+    assert O.max_tract(d, c, m) == 1000
+    d2 = _hap(1024, (23, 1023))
+    assert O.max_tract(d2, c, m) == 999
+
+
+def test_max_tract_skips_sites_outside_the_mask(oracle_lib):
+    """Over the common sites only (KNN::CutDownHaps, kNN.cpp:216-257): a
+    disagreement at a dropped site neither breaks nor ends a run, and
+    dropped sites are not counted."""
+    O = oracle_lib
+    rng = np.random.default_rng(9)
+    for _ in range(50):
+        n = int(rng.integers(1, 300))
+        a = rng.integers(0, 2, n).astype(np.uint8)
+        b = np.where(rng.random(n) < 0.1, 1 - a, a).astype(np.uint8)
+        keep = rng.random(n) < 0.7
+        from glphase_gb300 import model as mdl
+        pa, pb = mdl.pack_haplotypes(a[None])[0], mdl.pack_haplotypes(b[None])[0]
+        mask = np.zeros_like(pa)
+        for i in np.nonzero(keep)[0]:
+            mask[i >> 6] |= np.uint64(1) << np.uint64(i & 63)
+        best = run = 0
+        for i in np.nonzero(keep)[0]:
+            run = 0 if a[i] != b[i] else run + 1
+            best = max(best, run)
+        assert O.max_tract(pa, pb, mask) == best
+
+
+def test_knn_tract_metric_lists(oracle_lib):
+    """The tract-length metric (insti -T, kNN.cpp:157-164) orders
+    neighbours by the longest shared tract, not by the mismatch count:
+    a haplotype with one disagreement in its middle is farther than one with
+    three near an end."""
+    O = oracle_lib
+    from glphase_gb300 import model as mdl
+    S = 100
+    bits = np.zeros((6, S), np.uint8)
+    bits[2, 50] = 1            # haplotype 2: one disagreement with haplotype 0, mid-way
+    bits[3, [0, 1, 2]] = 1     # haplotype 3: three disagreements at the start
+    bits[4, :] = 1             # far from everything
+    bits[5, :] = 1
+    haps = mdl.pack_haplotypes(bits)
+    ham = O.knn(haps, S, 2)
+    tract = O.knn(haps, S, 2, metric="tract")
+    assert ham[0][0] == 2      # Hamming: 1 < 3
+    assert tract[0][0] == 3    # tract: 97 shared sites > 50
