@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the untimed full-schedule phasing accuracy run")
+    ap.add_argument("--knn-metric", choices=["hamming", "tract"], default="hamming",
+                    help="kNN distance: Hamming, or the common sites minus the longest "
+                         "shared tract (insti -T)")
     ap.add_argument("--recluster", type=int, default=0,
                     help="kNN configurations: rebuild the neighbour table from the current "
                          "haplotypes every R generations after burn-in, inside the timed "
@@ -99,16 +102,18 @@ def knn_k(w, args, H):
     return min(w.knn, (H - 2) // 2 * 2)
 
 
-def sampler_name(K):
+def sampler_name(K, metric="hamming"):
     if K:
-        return f"the K={K} nearest haplotypes by Hamming distance (KNN::ClusterHaps)"
+        by = ("Hamming distance" if metric == "hamming" else
+              "common sites minus the longest shared tract (-T)")
+        return f"the K={K} nearest haplotypes by {by} (KNN::ClusterHaps)"
     return "uniform over all other haplotypes (UnifSampler)"
 
 
 def workload_config(args, w, N, S, C, H):
     """The workload definition both arms report under `config` (the arms
     differ in how they run it, which each line says outside `config`)."""
-    sampler = sampler_name(knn_k(w, args, H))
+    sampler = sampler_name(knn_k(w, args, H), args.knn_metric)
     K = knn_k(w, args, H)
     rc = (f", rebuilt from the current haplotypes every {args.recluster} generations after "
           f"burn-in" if K and args.recluster else "")
@@ -116,6 +121,7 @@ def workload_config(args, w, N, S, C, H):
                         f"generation, surrogates from {sampler}{rc}",
             "samples": N, "sites": S, "cycles": C, "haplotypes": H, "sampler": sampler,
             "recluster_every": args.recluster if K else 0,
+            "knn_metric": args.knn_metric if K else None,
             "emission": "vq4" if args.vq else "f32",
             "l2": "inputs larger than L2 (emission %.0f MB)" % (N * S * 16 / 1e6)}
 
@@ -138,7 +144,7 @@ def cpu_model():
     return "unknown"
 
 
-def accuracy(w, m, haps, ds, seed, device, recluster=0):
+def accuracy(w, m, haps, ds, seed, device, recluster=0, knn_metric="hamming"):
     """Phasing accuracy of the workload's full schedule (burn-in + sampling
     generations, the configuration's surrogate sampler, device tallies and
     result; glphase_gb300.phase): NRD of the called genotypes against the
@@ -148,6 +154,7 @@ def accuracy(w, m, haps, ds, seed, device, recluster=0):
     N = m.N
     opts = ph.PhaseOptions(sa_burnin=w.burnin, burnin=0, sampling=w.sampling, cycles=w.cycles,
                            seed=seed, knn=w.knn, cluster_start=0, recluster=recluster,
+                           knn_metric=knn_metric,
                            kick_start=bool(w.panel_haps), kick_first=bool(w.panel_haps),
                            device=device)
     prob, _ = ph.phase(m, haps, opts)
@@ -324,7 +331,7 @@ def run_reference(args):
     K = knn_k(w, args, H)
     if K:
         t0 = time.perf_counter()
-        nbr = np.ascontiguousarray(O.knn(haps, S, K)[:N])
+        nbr = np.ascontiguousarray(O.knn(haps, S, K, metric=args.knn_metric)[:N])
         knn_s = time.perf_counter() - t0
     seed = 1
     q0, p0 = O.sample_surrogates(seed, 0, N, C, 0, H, nbr=nbr)
@@ -349,7 +356,7 @@ def run_reference(args):
         g = args.warmup + i
         t0 = time.perf_counter()
         if rebuild(g):  # KNN::ClusterHaps on the haplotypes, as the timed GPU step does
-            nbr = np.ascontiguousarray(O.knn(haps, S, K)[:N])
+            nbr = np.ascontiguousarray(O.knn(haps, S, K, metric=args.knn_metric)[:N])
         dt += time.perf_counter() - t0
         quad, props, tr, pen, cnt = gen(g, n)
         t0 = time.perf_counter()
@@ -419,7 +426,7 @@ def run_ours(args):
         k0 = torch.cuda.Event(enable_timing=True)
         k1 = torch.cuda.Event(enable_timing=True)
         k0.record(eng.stream)
-        nbr = eng.knn(K)
+        nbr = eng.knn(K, metric=args.knn_metric)
         k1.record(eng.stream)
         eng.finish()
         knn_ms = k0.elapsed_time(k1)
@@ -434,7 +441,7 @@ def run_ours(args):
         nonlocal nbr
         if nbr is not None and args.recluster and g > w.burnin and \
                 (g - w.burnin) % args.recluster == 0:
-            nbr = eng.knn(K)  # from the current haplotypes, on the engine's stream
+            nbr = eng.knn(K, metric=args.knn_metric)  # from the current haplotypes
             rebuilds[0] += 1
         a = eng.args(None, None, pen_for(g, w.burnin), seed=seed, generation=g, neighbors=nbr)
         if w.panel_haps and g == 0:
@@ -542,7 +549,7 @@ def run_ours(args):
             line["cpu_baseline"] = base
         if not args.no_accuracy:
             line["accuracy"] = accuracy(w, m, haps, workload.dataset, seed, local,
-                                        args.recluster)
+                                        args.recluster, args.knn_metric)
         if world == 1 and args.config == "batched" and not (args.no_vs_plain and args.no_serve):
             # the metric's other halves, on the same GPU after the main leg:
             # batched vs plain GPU form on the uneven chunks, p50/p99 serving
