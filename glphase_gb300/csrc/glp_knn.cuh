@@ -77,6 +77,26 @@ __device__ __forceinline__ Tract tract_word(uint64_t x, uint64_t m) {
     return t;
   }
   const int lo = __ffsll((long long)x) - 1, hi = 63 - __clzll((long long)x);
+  if (m == ~0ull) {  // every site common: the longest run of agreements in log steps
+    const uint64_t r1 = ~x, r2 = r1 & (r1 >> 1), r4 = r2 & (r2 >> 2), r8 = r4 & (r4 >> 4),
+                   r16 = r8 & (r8 >> 8), r32 = r16 & (r16 >> 16);
+    // cur: the starts of runs of at least n agreements; n grows greedily
+    uint64_t cur = ~0ull;
+    uint32_t n = 0;
+    const uint64_t rs[6] = {r32, r16, r8, r4, r2, r1};
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const uint64_t cand = cur & (rs[i] >> n);
+      if (cand) {
+        n += 32u >> i;
+        cur = cand;
+      }
+    }
+    t.pre = (uint32_t)lo;
+    t.suf = (uint32_t)(63 - hi);
+    t.best = n;
+    return t;
+  }
   t.pre = (uint32_t)__popcll(m & ((1ull << lo) - 1ull));
   t.suf = hi == 63 ? 0u : (uint32_t)__popcll(m >> (hi + 1));
   uint32_t best = max(t.pre, t.suf);

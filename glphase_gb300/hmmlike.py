@@ -249,7 +249,15 @@ class Engine:
         torch = self.torch
         half = (k + 1) // 2
         self.dev._c(self.dev.L.glp_set_knn_metric(self.dev.ctx, nat.KNN_METRICS[metric]))
-        self.nbr = torch.zeros((self.H // 2, 2 * half), dtype=torch.int32, device=self.device)
+        shape = (self.H // 2, 2 * half)
+        # A rebuild writes into the same table on the engine's stream, after
+        # the generations already enqueued there have read it.  (A new tensor
+        # would come from torch's allocator on its current stream, unordered
+        # with the engine's: its memory could be the old table's while a
+        # generation still reads it.)
+        if getattr(self, "nbr", None) is None or tuple(self.nbr.shape) != shape:
+            with torch.cuda.stream(self.stream):
+                self.nbr = torch.empty(shape, dtype=torch.int32, device=self.device)
         self.dev._c(self.dev.L.glp_knn_neighbors(self.dev.ctx, self.haps.data_ptr(), self.H,
                                                  self.S, k, freq_lb, freq_ub, int(use_maf),
                                                  self.nbr.data_ptr()))
