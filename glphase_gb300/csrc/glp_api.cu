@@ -352,7 +352,7 @@ cudaError_t allow_chain_smem() {
 void launch_work(const glp::GenParams &p, uint64_t samples, cudaStream_t st) {
   glp::work_chains_kernel<><<<(unsigned)((samples + glp::kPairRows - 1) / glp::kPairRows),
                               glp::kChainThreads, glp::kChainSmem, st>>>(p);
-  glp::work_sample_kernel<><<<(unsigned)samples, 32, 0, st>>>(p);
+  glp::work_sample_kernel<><<<(unsigned)(samples * glp::sample_parts(p.wn)), 32, 0, st>>>(p);
 }
 void launch_work(const glp::MultiParams &mp, uint64_t samples, cudaStream_t st) {
   glp::work_chains_multi_kernel<><<<(unsigned)((samples + glp::kPairRows - 1) / glp::kPairRows),

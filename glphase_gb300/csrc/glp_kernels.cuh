@@ -661,7 +661,7 @@ __device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
 // recursion), work_chains one after the other on one thread (chunks mixed
 // within a warp); (2) the
 // sampling of impute.cpp:453-484 then runs for every site in parallel, one
-// warp per sample and 32 sites per instruction.
+// warp per part of a sample and 32 sites per instruction.
 
 __device__ __forceinline__ uint32_t clamp_site(int m, uint32_t S) {
   return m < 0 ? 0u : ((uint32_t)m >= S ? S - 1 : (uint32_t)m);
@@ -1148,19 +1148,21 @@ __device__ __forceinline__ uint32_t work_sample_site(const GenParams &p, const f
   return 3u;    // (1, 1)
 }
 
-// Pass 2 for all words of sample s (called by a whole warp), two words at a
-// time: lane l draws the four uniforms of the l-th 4-site group of the
+// Pass 2 for words [w_lo, w_hi) of sample s (called by a whole warp; w_lo
+// even), two words at a time: lane l draws the four uniforms of the l-th
+// 4-site group of the
 // 128-site span (one draw per group, as the reference draws them) into
 // u[4 l .. 4 l + 3], so u[o] is the uniform of span site o; then the bits
 // of sites w*64 + lane and w*64 + 32 + lane of each word are gathered into
 // the two new haplotype words with ballots.
 __device__ __forceinline__ void work_sample(const GenParams &p, const float4 *pcr, uint32_t s,
-                                            uint4 q, uint32_t lane, uint32_t *u) {
+                                            uint4 q, uint32_t lane, uint32_t *u, uint32_t w_lo,
+                                            uint32_t w_hi) {
   const uint32_t wn = p.wn;
   const uint64_t *f0 = p.haps + (size_t)q.x * wn, *f1 = p.haps + (size_t)q.y * wn,
                  *m0 = p.haps + (size_t)q.z * wn, *m1 = p.haps + (size_t)q.w * wn;
   uint64_t *ha = p.hnew + (size_t)2 * s * wn, *hb = ha + wn;
-  for (uint32_t w2 = 0; w2 < wn; w2 += 2) {
+  for (uint32_t w2 = w_lo; w2 < w_hi; w2 += 2) {
     if (!p.tr_work) {
       const glp_u32x4 ux = glp_draw(p.seed, p.generation, s, 16 * w2 + lane, GLP_TAG_WORK);
       reinterpret_cast<uint4 *>(u)[lane] = make_uint4(ux.v[0], ux.v[1], ux.v[2], ux.v[3]);
@@ -1169,7 +1171,7 @@ __device__ __forceinline__ void work_sample(const GenParams &p, const float4 *pc
 #pragma unroll
     for (uint32_t t = 0; t < 2; ++t) {
       const uint32_t w = w2 + t;
-      if (w >= wn)
+      if (w >= w_hi)
         break;
       const uint64_t A0 = __ldg(f0 + w), A1 = __ldg(f1 + w), C0 = __ldg(m0 + w),
                      C1 = __ldg(m1 + w);
@@ -1207,10 +1209,19 @@ __device__ __forceinline__ void set_slot(uint4 &q, uint32_t r, uint32_t v) {
 // Work sources.  One chunk: the kernel parameter.  Many chunks: a descriptor
 // table in global memory; the samples of all chunks form one queue, chunk by
 // chunk, so a group's neighbours in the queue usually share its chunk.
+// Pass 2 of one chunk splits each sample's words into parts of
+// kSampleWords, one warp a part, so that its warps are many and short and the
+// last of them leave little of the GPU idle (many chunks: one part a sample).
+constexpr uint32_t kSampleWords = 16;
+__host__ __device__ inline uint32_t sample_parts(uint32_t wn) {
+  return (wn + kSampleWords - 1) / kSampleWords;
+}
+
 struct OneChunk {
   static constexpr bool kMulti = false;
   const GenParams &p;
   __device__ __forceinline__ uint32_t total() const { return p.N; }
+  __device__ __forceinline__ uint32_t parts() const { return sample_parts(p.wn); }
   __device__ __forceinline__ const GenParams &chunk(uint32_t) const { return p; }
   __device__ __forceinline__ void locate(uint32_t g, uint32_t &c, uint32_t &s) const {
     c = 0;
@@ -1231,6 +1242,7 @@ struct ManyChunks {
   static constexpr bool kMulti = true;
   const MultiParams &mp;
   __device__ __forceinline__ uint32_t total() const { return __ldg(mp.offsets + mp.nchunks); }
+  __device__ __forceinline__ uint32_t parts() const { return 1; }
   __device__ __forceinline__ const GenParams &chunk(uint32_t c) const { return mp.chunks[c]; }
   __device__ __forceinline__ void locate(uint32_t g, uint32_t &c, uint32_t &s) const {
     uint32_t lo = 0, hi = mp.nchunks;  // largest c with offsets[c] <= g
@@ -1571,7 +1583,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 // quadruples.  Pass 1: blocks of two warps over 16 samples, a lane pair per
 // sample and recursion direction in each warp (work_chains_pair), so the
 // thousand-odd blocks of a generation spread over every SM.  Pass 2: one
-// warp per sample samples all sites.  Chunks without hmm_work skip both.
+// warp per part of a sample (kSampleWords words) samples its sites.  Chunks
+// without hmm_work skip both.
 constexpr int kWorkThreads = 32;
 constexpr int kChainThreads = 64;
 constexpr size_t kChainSmem = 2 * sizeof(ChainTiles);  // dynamic: one per warp
@@ -1617,19 +1630,24 @@ __device__ __forceinline__ void sample_body(const Src &src) {
   __shared__ float4 s_pcr[kWorkThreads / 32][4];  // the warp's mutation-matrix rows
   __shared__ __align__(16) uint32_t s_u[kWorkThreads / 32][128];  // a span's uniforms
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
-  const uint32_t g = blockIdx.x * (blockDim.x >> 5) + wib;  // one sample per warp
-  if (g >= src.total())
+  // one part of one sample per warp
+  const uint64_t g = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+  const uint32_t parts = src.parts();
+  if (g >= (uint64_t)src.total() * parts)
     return;
+  const uint32_t gs = (uint32_t)(g / parts), part = (uint32_t)(g % parts);
   uint32_t c, s;
-  src.locate(g, c, s);
+  src.locate(gs, c, s);
   const GenParams &p = src.chunk(c);
   if (!p.do_work)
     return;
+  const uint32_t w_lo = parts > 1 ? part * kSampleWords : 0u;
+  const uint32_t w_hi = parts > 1 ? min(p.wn, w_lo + kSampleWords) : p.wn;
   if (lane < 4)
     s_pcr[wib][lane] = make_float4(p.pc[4 * lane], p.pc[4 * lane + 1], p.pc[4 * lane + 2],
                                    p.pc[4 * lane + 3]);
   __syncwarp();
-  work_sample(p, s_pcr[wib], s, final_quad(src, p, s), lane, s_u[wib]);
+  work_sample(p, s_pcr[wib], s, final_quad(src, p, s), lane, s_u[wib], w_lo, w_hi);
 }
 
 template <int = 0>
