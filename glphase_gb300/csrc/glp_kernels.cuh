@@ -1212,7 +1212,11 @@ __device__ __forceinline__ void set_slot(uint4 &q, uint32_t r, uint32_t v) {
 // Pass 2 of one chunk splits each sample's words into parts of
 // kSampleWords, one warp a part, so that its warps are many and short and the
 // last of them leave little of the GPU idle (many chunks: one part a sample).
-constexpr uint32_t kSampleWords = 16;
+#ifndef GLP_SAMPLE_WORDS
+#define GLP_SAMPLE_WORDS 16
+#endif
+constexpr uint32_t kSampleWords = GLP_SAMPLE_WORDS;
+static_assert(kSampleWords % 2 == 0, "a part starts a two-word span");
 __host__ __device__ inline uint32_t sample_parts(uint32_t wn) {
   return (wn + kSampleWords - 1) / kSampleWords;
 }

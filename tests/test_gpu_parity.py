@@ -115,8 +115,11 @@ def check_against_oracle(O, m, haps, quad, props, pen, out, seed, gen, trace=Non
 
 
 @pytest.mark.parametrize("S", [1, 2, 7, 8, 9, 16, 17, 24, 25, 33, 63, 64, 65, 130, 136, 300,
-                               513, 1024])
+                               513, 1024, 1088, 1100, 2049])
 def test_generation_matches_oracle_sites(dev, oracle_lib, S):
+    # past 1,024 sites hmm_work's sampling pass splits a sample's words into
+    # 16-word parts: 1,088 and 1,100 sites end on a one- and a two-word part,
+    # 2,049 on a part of one word holding one site
     m, haps, quad, props = make_problem(N=16, S=S, C=12)
     out = run_gpu(dev, m, haps, quad, props, 1.0, seed=7, gen=1)
     check_against_oracle(oracle_lib, m, haps, quad, props, 1.0, out, 7, 1)
