@@ -245,7 +245,8 @@ class Engine:
         """Neighbour table of the current haplotypes on the device
         (KNN::ClusterHaps, kNN.cpp:123-206); kept for the in-kernel draws.
         metric "hamming" or "tract" (the common sites minus the longest shared
-        tract, insti -T)."""
+        tract, insti -T).  Returns the engine's table, which the next call
+        rewrites in place (copy it to keep an old one)."""
         torch = self.torch
         half = (k + 1) // 2
         self.dev._c(self.dev.L.glp_set_knn_metric(self.dev.ctx, nat.KNN_METRICS[metric]))
