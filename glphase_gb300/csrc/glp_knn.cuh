@@ -285,22 +285,57 @@ __global__ void __launch_bounds__(kKnnThreads)
   const uint64_t *ha = haps + (size_t)2 * s * wn, *hb = ha + wn;
   for (uint32_t i = tid; i < (H + 31) / 32; i += kKnnThreads)
     taken[i] = 0;
-  // distances: one haplotype per warp iteration, words across lanes
-  for (uint32_t h = warp; h < H; h += kKnnThreads / 32) {
-    uint32_t a = 0, b = 0;
-    const uint64_t *o = haps + (size_t)h * wn;
-    if (metric == 0) {
+  if (metric == 0) {
+    // Hamming distances: four haplotypes per warp iteration, words across
+    // lanes (the four haplotypes' loads in flight together), then one
+    // butterfly over the eight sums -- v[2k] and v[2k+1] the distances of
+    // haplotype h0 + k to the sample's two -- that halves the values a lane
+    // holds at each of the first three levels (9 shuffles instead of 40);
+    // lane 4i ends with the total of value i.
+    for (uint32_t h0 = 4 * warp; h0 < H; h0 += 4 * (kKnnThreads / 32)) {
+      uint32_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       for (uint32_t w = lane; w < wn; w += 32) {
-        const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
-        a += __popcll((__ldg(ha + w) ^ ow) & mw);
-        b += __popcll((__ldg(hb + w) ^ ow) & mw);
+        const uint64_t mw = __ldg(mask + w), xa = __ldg(ha + w), xb = __ldg(hb + w);
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+          if (h0 + k < H) {
+            const uint64_t ow = __ldg(haps + (size_t)(h0 + k) * wn + w);
+            v[2 * k] += __popcll((xa ^ ow) & mw);
+            v[2 * k + 1] += __popcll((xb ^ ow) & mw);
+          }
+        }
       }
 #pragma unroll
-      for (int off = 16; off; off >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, off);
-        b += __shfl_xor_sync(0xffffffffu, b, off);
+      for (int i = 0; i < 4; ++i) {  // lanes < 16 keep values 0-3, the others 4-7
+        const bool hi = lane & 16u;
+        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[i] : v[i + 4], 16);
+        v[i] = (hi ? v[i + 4] : v[i]) + r;
       }
-    } else {  // common sites minus the longest run of agreeing common sites
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const bool hi = lane & 8u;
+        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[i] : v[i + 2], 8);
+        v[i] = (hi ? v[i + 2] : v[i]) + r;
+      }
+      {
+        const bool hi = lane & 4u;
+        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[0] : v[1], 4);
+        v[0] = (hi ? v[1] : v[0]) + r;
+      }
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+      const uint32_t i = lane >> 2, h = h0 + (i >> 1);
+      if ((lane & 3u) == 0 && h < H) {
+        const bool own = (h >> 1) == s;
+        ((i & 1u) ? dB : dA)[h] = own ? kKnnExcluded : (uint16_t)v[0];
+      }
+    }
+  }
+  // tract distances: one haplotype per warp iteration, words across lanes
+  for (uint32_t h = warp; metric != 0 && h < H; h += kKnnThreads / 32) {
+    uint32_t a = 0, b = 0;
+    const uint64_t *o = haps + (size_t)h * wn;
+    {  // common sites minus the longest run of agreeing common sites
       Tract ta = {0, 0, 0, 0}, tb = {0, 0, 0, 0};
       for (uint32_t w0 = 0; w0 < wn; w0 += 32) {
         const uint32_t w = w0 + lane;
