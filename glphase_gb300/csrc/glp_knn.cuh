@@ -267,6 +267,35 @@ __device__ void select_nearest(const uint16_t *d, uint32_t H, uint32_t half, uin
   __syncthreads();
 }
 
+// Sums of the warp's NV values per lane (NV a power of two, at most 32):
+// each of the first log2 NV butterfly levels (lane offsets 16, 8, ...) hands
+// half of a lane's values to its partner and keeps the other half, so a
+// lane holds one value after them (NV - 1 shuffles in all, instead of 5 NV
+// for NV separate reductions); the remaining levels add plainly.  Returns the
+// index of the value whose total v[0] then holds: lane / (32 / NV).
+constexpr uint32_t kKnnPerWarp = 8;  // haplotypes per warp iteration
+template <int NV>
+__device__ __forceinline__ uint32_t warp_sums(uint32_t (&v)[NV], uint32_t lane) {
+  static_assert(NV >= 1 && NV <= 32 && (NV & (NV - 1)) == 0, "NV");
+  int n = NV;
+#pragma unroll
+  for (uint32_t off = 16; off >= 1; off >>= 1) {
+    if (n > 1) {
+      const bool hi = lane & off;
+      const int h = n / 2;
+#pragma unroll
+      for (int i = 0; i < h; ++i) {
+        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[i] : v[i + h], off);
+        v[i] = (hi ? v[i + h] : v[i]) + r;
+      }
+      n = h;
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
+    }
+  }
+  return lane / (32u / NV);
+}
+
 // Dynamic shared memory: dA, dB [H] uint16, keys [2*kKnnMaxHalf] uint32,
 // chosen [2*kKnnMaxHalf] uint32, taken bits [ceil(H/32)] uint32.
 __global__ void __launch_bounds__(kKnnThreads)
@@ -286,18 +315,20 @@ __global__ void __launch_bounds__(kKnnThreads)
   for (uint32_t i = tid; i < (H + 31) / 32; i += kKnnThreads)
     taken[i] = 0;
   if (metric == 0) {
-    // Hamming distances: four haplotypes per warp iteration, words across
-    // lanes (the four haplotypes' loads in flight together), then one
-    // butterfly over the eight sums -- v[2k] and v[2k+1] the distances of
-    // haplotype h0 + k to the sample's two -- that halves the values a lane
-    // holds at each of the first three levels (9 shuffles instead of 40);
-    // lane 4i ends with the total of value i.
-    for (uint32_t h0 = 4 * warp; h0 < H; h0 += 4 * (kKnnThreads / 32)) {
-      uint32_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // Hamming distances: kKnnPerWarp haplotypes per warp iteration, words
+    // across lanes (their loads in flight together), then one butterfly over
+    // the 2 kKnnPerWarp sums -- v[2k] and v[2k+1] the distances of haplotype
+    // h0 + k to the sample's two haplotypes.
+    for (uint32_t h0 = kKnnPerWarp * warp; h0 < H; h0 += kKnnPerWarp * (kKnnThreads / 32)) {
+      uint32_t v[2 * kKnnPerWarp];
+#pragma unroll
+      for (int k = 0; k < 2 * kKnnPerWarp; ++k)
+        v[k] = 0;
+#pragma unroll 2
       for (uint32_t w = lane; w < wn; w += 32) {
         const uint64_t mw = __ldg(mask + w), xa = __ldg(ha + w), xb = __ldg(hb + w);
 #pragma unroll
-        for (uint32_t k = 0; k < 4; ++k) {
+        for (uint32_t k = 0; k < kKnnPerWarp; ++k) {
           if (h0 + k < H) {
             const uint64_t ow = __ldg(haps + (size_t)(h0 + k) * wn + w);
             v[2 * k] += __popcll((xa ^ ow) & mw);
@@ -305,27 +336,9 @@ __global__ void __launch_bounds__(kKnnThreads)
           }
         }
       }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {  // lanes < 16 keep values 0-3, the others 4-7
-        const bool hi = lane & 16u;
-        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[i] : v[i + 4], 16);
-        v[i] = (hi ? v[i + 4] : v[i]) + r;
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const bool hi = lane & 8u;
-        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[i] : v[i + 2], 8);
-        v[i] = (hi ? v[i + 2] : v[i]) + r;
-      }
-      {
-        const bool hi = lane & 4u;
-        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[0] : v[1], 4);
-        v[0] = (hi ? v[1] : v[0]) + r;
-      }
-      v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
-      v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-      const uint32_t i = lane >> 2, h = h0 + (i >> 1);
-      if ((lane & 3u) == 0 && h < H) {
+      const uint32_t i = warp_sums(v, lane);
+      const uint32_t h = h0 + (i >> 1);
+      if ((lane & (32u / (2 * kKnnPerWarp) - 1u)) == 0 && h < H) {
         const bool own = (h >> 1) == s;
         ((i & 1u) ? dB : dA)[h] = own ? kKnnExcluded : (uint16_t)v[0];
       }
