@@ -103,6 +103,8 @@ struct glp_ctx {
   size_t quad_cap = 0, quad_out_cap = 0, props_cap = 0, nbr_cap = 0;
   uint64_t *d_mask = nullptr;  // kNN common-site mask
   size_t mask_cap = 0;
+  uint16_t *d_knn_dist = nullptr;  // kNN distances of a chunk of samples [2 n][H]
+  size_t knn_dist_cap = 0;
   uint8_t *d_tr_slot = nullptr, *d_acc = nullptr;
   double *d_tr_u = nullptr, *d_like = nullptr, *d_evals = nullptr;
   float *d_tr_work = nullptr;
@@ -685,6 +687,7 @@ void glp_destroy(glp_ctx *c) {
   release(c->d_props);
   release(c->d_nbr);
   release(c->d_mask);
+  release(c->d_knn_dist);
   release(c->d_tr_slot);
   release(c->d_acc);
   release(c->d_tr_u);
@@ -1559,11 +1562,32 @@ int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, 
                                                      c->d_mask);
   GLP_CUDA(c, cudaGetLastError());
   const size_t smem = glp::knn_smem_bytes(H);
-  GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-  glp::knn_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask, half,
-                                                                 S, c->knn_metric, neighbors);
-  GLP_CUDA(c, cudaGetLastError());
+  if (c->knn_metric == GLP_KNN_TRACT) {
+    GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    glp::knn_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask, half,
+                                                                   S, c->knn_metric, neighbors);
+    GLP_CUDA(c, cudaGetLastError());
+    return GLP_OK;
+  }
+  // Hamming: tiled distances of a chunk of samples (at most 256 MB of them)
+  // into global memory, then the selection, chunk by chunk
+  GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_select_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const uint32_t NS = H / 2;
+  const uint32_t chunk =
+      (uint32_t)std::min<size_t>(NS, std::max<size_t>(64, ((size_t)256 << 20) / (4 * (size_t)H)));
+  if ((rc = ensure(c, c->d_knn_dist, c->knn_dist_cap, (size_t)2 * chunk * H)))
+    return rc;
+  for (uint32_t s0 = 0; s0 < NS; s0 += chunk) {
+    const uint32_t n = std::min(chunk, NS - s0);
+    const dim3 grid((H + glp::kDistH - 1) / glp::kDistH, (2 * n + glp::kDistQ - 1) / glp::kDistQ);
+    glp::knn_dist_kernel<<<grid, glp::kDistThreads, 0, c->stream>>>(haps, H, wn, c->d_mask,
+                                                                    2 * s0, 2 * n, c->d_knn_dist);
+    glp::knn_select_kernel<<<n, glp::kKnnThreads, smem, c->stream>>>(c->d_knn_dist, H, s0, half,
+                                                                    S, neighbors);
+    GLP_CUDA(c, cudaGetLastError());
+  }
   return GLP_OK;
 }
 

@@ -267,6 +267,32 @@ __device__ void select_nearest(const uint16_t *d, uint32_t H, uint32_t half, uin
   __syncthreads();
 }
 
+// The sample's neighbour list from the distances dA, dB of its two
+// haplotypes (shared memory; its own two excluded): the `half` nearest to
+// the first, then the `half` nearest to the second among those not taken,
+// interleaved into out (KNN::ClusterHaps, kNN.cpp:170-206).
+__device__ __forceinline__ void knn_choose(uint16_t *dA, uint16_t *dB, uint32_t H,
+                                           uint32_t half, uint32_t dmax, uint32_t *keys,
+                                           uint32_t *red, uint32_t *chosen, uint32_t *taken,
+                                           uint32_t *out) {
+  const uint32_t tid = threadIdx.x;
+  select_nearest(dA, H, half, dmax, keys, red, chosen);
+  for (uint32_t i = tid; i < half; i += kKnnThreads) {
+    const uint32_t h = chosen[i];
+    atomicOr(&taken[h >> 5], 1u << (h & 31u));
+  }
+  __syncthreads();
+  for (uint32_t h = tid; h < H; h += kKnnThreads)
+    if ((taken[h >> 5] >> (h & 31u)) & 1u)
+      dB[h] = kKnnExcluded;
+  __syncthreads();
+  select_nearest(dB, H, half, dmax, keys, red, chosen + kKnnMaxHalf);
+  for (uint32_t i = tid; i < half; i += kKnnThreads) {
+    out[2 * i] = chosen[i];
+    out[2 * i + 1] = chosen[kKnnMaxHalf + i];
+  }
+}
+
 // Sums of the warp's NV values per lane (NV a power of two, at most 32):
 // each of the first log2 NV butterfly levels (lane offsets 16, 8, ...) hands
 // half of a lane's values to its partner and keeps the other half, so a
@@ -371,22 +397,103 @@ __global__ void __launch_bounds__(kKnnThreads)
     }
   }
   __syncthreads();
-  select_nearest(dA, H, half, dmax, keys, red, chosen);
-  for (uint32_t i = tid; i < half; i += kKnnThreads) {
-    const uint32_t h = chosen[i];
-    atomicOr(&taken[h >> 5], 1u << (h & 31u));
+  knn_choose(dA, dB, H, half, dmax, keys, red, chosen, taken,
+             neighbors + (size_t)s * 2 * half);
+}
+
+// Tiled Hamming distances for the kNN build, as a product of bit matrices:
+// dist[q][h] = popcount((hap q0+q XOR hap h) AND mask) over the words, for
+// the query haplotypes [q0, q0 + nq) (2 s and 2 s + 1 for the samples s of a
+// chunk) and every haplotype h; a sample's own two are marked excluded.  A
+// CTA takes 64 queries x 128 haplotypes and walks the words 8 at a time,
+// staged word-major in shared memory (a warp's reads of a word are
+// consecutive); each thread keeps 4 x 8 sums.  Each panel word is read from
+// L2 once per 64 queries instead of once per sample.
+constexpr uint32_t kDistQ = 64, kDistH = 128, kDistW = 8, kDistThreads = 256;
+__global__ void __launch_bounds__(kDistThreads)
+    knn_dist_kernel(const uint64_t *__restrict__ haps, uint32_t H, uint32_t wn,
+                    const uint64_t *__restrict__ mask, uint32_t q0, uint32_t nq,
+                    uint16_t *__restrict__ dist) {
+  __shared__ uint64_t sq[kDistW][kDistQ];
+  __shared__ uint64_t sh[kDistW][kDistH];
+  __shared__ uint64_t smask[kDistW];
+  const uint32_t tid = threadIdx.x, tx = tid & 15u, ty = tid >> 4;
+  const uint32_t hb = blockIdx.x * kDistH, qb = blockIdx.y * kDistQ;
+  uint32_t acc[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      acc[i][j] = 0;
+  for (uint32_t w0 = 0; w0 < wn; w0 += kDistW) {
+    for (uint32_t i = tid; i < kDistQ * kDistW; i += kDistThreads) {
+      const uint32_t r = i / kDistW, k = i % kDistW, w = w0 + k;
+      sq[k][r] = (qb + r < nq && w < wn) ? __ldg(haps + (size_t)(q0 + qb + r) * wn + w) : 0ull;
+    }
+    for (uint32_t i = tid; i < kDistH * kDistW; i += kDistThreads) {
+      const uint32_t r = i / kDistW, k = i % kDistW, w = w0 + k;
+      sh[k][r] = (hb + r < H && w < wn) ? __ldg(haps + (size_t)(hb + r) * wn + w) : 0ull;
+    }
+    if (tid < kDistW)
+      smask[tid] = w0 + tid < wn ? __ldg(mask + w0 + tid) : 0ull;
+    __syncthreads();
+#pragma unroll
+    for (uint32_t k = 0; k < kDistW; ++k) {
+      const uint64_t mk = smask[k];
+      uint64_t qv[4], hv[8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        qv[i] = sq[k][4 * ty + i] & mk;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        hv[j] = sh[k][tx + 16 * j] & mk;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          acc[i][j] += __popcll(qv[i] ^ hv[j]);
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  for (uint32_t h = tid; h < H; h += kKnnThreads)
-    if ((taken[h >> 5] >> (h & 31u)) & 1u)
-      dB[h] = kKnnExcluded;
-  __syncthreads();
-  select_nearest(dB, H, half, dmax, keys, red, chosen + kKnnMaxHalf);
-  uint32_t *out = neighbors + (size_t)s * 2 * half;
-  for (uint32_t i = tid; i < half; i += kKnnThreads) {
-    out[2 * i] = chosen[i];
-    out[2 * i + 1] = chosen[kKnnMaxHalf + i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t q = qb + 4 * ty + i;
+    if (q >= nq)
+      continue;
+    const uint32_t s = (q0 + q) >> 1;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t h = hb + tx + 16 * j;
+      if (h < H)
+        dist[(size_t)q * H + h] = (h >> 1) == s ? kKnnExcluded : (uint16_t)acc[i][j];
+    }
   }
+}
+
+// The neighbour lists of the samples s0 + blockIdx.x from their rows of
+// knn_dist_kernel's distances (rows 2 i and 2 i + 1 for the chunk's i-th
+// sample); shared memory as knn_kernel's.
+__global__ void __launch_bounds__(kKnnThreads)
+    knn_select_kernel(const uint16_t *__restrict__ dist, uint32_t H, uint32_t s0, uint32_t half,
+                      uint32_t dmax, uint32_t *__restrict__ neighbors) {
+  extern __shared__ uint4 knn_smem[];
+  uint16_t *dA = reinterpret_cast<uint16_t *>(knn_smem);
+  uint16_t *dB = dA + H;
+  uint32_t *keys = reinterpret_cast<uint32_t *>(dA + 2 * ((H + 1) & ~1u));
+  uint32_t *chosen = keys + 2 * kKnnMaxHalf;
+  uint32_t *taken = chosen + 2 * kKnnMaxHalf;
+  __shared__ uint32_t red[kKnnThreads / 32];
+  const uint32_t tid = threadIdx.x;
+  // the two rows, 2 H uint16 in a row of the distances (H even: 4-byte units)
+  const uint32_t *row = reinterpret_cast<const uint32_t *>(dist + (size_t)2 * blockIdx.x * H);
+  uint32_t *d32 = reinterpret_cast<uint32_t *>(dA);
+  for (uint32_t i = tid; i < H; i += kKnnThreads)
+    d32[i] = __ldg(row + i);
+  for (uint32_t i = tid; i < (H + 31) / 32; i += kKnnThreads)
+    taken[i] = 0;
+  __syncthreads();
+  knn_choose(dA, dB, H, half, dmax, keys, red, chosen, taken,
+             neighbors + (size_t)(s0 + blockIdx.x) * 2 * half);
 }
 
 inline size_t knn_smem_bytes(uint32_t H) {
