@@ -1563,10 +1563,10 @@ int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, 
   GLP_CUDA(c, cudaGetLastError());
   const size_t smem = glp::knn_smem_bytes(H);
   if (c->knn_metric == GLP_KNN_TRACT) {
-    GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_kernel,
+    GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_tract_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    glp::knn_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask, half,
-                                                                   S, c->knn_metric, neighbors);
+    glp::knn_tract_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask,
+                                                                         half, S, neighbors);
     GLP_CUDA(c, cudaGetLastError());
     return GLP_OK;
   }

@@ -12,15 +12,17 @@
 // with the unstable std::sort (kNN.cpp:172-173), so its tie order is
 // implementation-defined.
 //
-// One CTA per sample.  Distances of both haplotypes to all H haplotypes sit
-// in shared memory as uint16 (H <= kKnnMaxHaps); every warp scores one
-// haplotype at a time with coalesced word loads and a shuffle reduction (for
-// the tract length an ordered one: each word's runs of agreeing common sites
-// -- before its first disagreement, after its last, the longest between --
-// combine left to right).  The
+// Selection: one CTA per sample with the distances of both its haplotypes
+// to all H haplotypes in shared memory as uint16 (H <= kKnnMaxHaps); the
 // ceil(K/2) nearest are found by binary search on the distance threshold,
 // ties at the threshold are taken in index order through a block scan, and
 // the chosen list is put in (distance, index) order by a bitonic sort.
+// Distances: Hamming as a tiled product of bit matrices (knn_dist_kernel,
+// a chunk of samples at a time through global memory); the tract length in
+// the selecting CTA itself, every warp scoring one haplotype at a time with
+// coalesced word loads and an ordered shuffle reduction (each word's runs
+// of agreeing common sites -- before its first disagreement, after its
+// last, the longest between -- combine left to right).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -293,41 +295,14 @@ __device__ __forceinline__ void knn_choose(uint16_t *dA, uint16_t *dB, uint32_t 
   }
 }
 
-// Sums of the warp's NV values per lane (NV a power of two, at most 32):
-// each of the first log2 NV butterfly levels (lane offsets 16, 8, ...) hands
-// half of a lane's values to its partner and keeps the other half, so a
-// lane holds one value after them (NV - 1 shuffles in all, instead of 5 NV
-// for NV separate reductions); the remaining levels add plainly.  Returns the
-// index of the value whose total v[0] then holds: lane / (32 / NV).
-constexpr uint32_t kKnnPerWarp = 8;  // haplotypes per warp iteration
-template <int NV>
-__device__ __forceinline__ uint32_t warp_sums(uint32_t (&v)[NV], uint32_t lane) {
-  static_assert(NV >= 1 && NV <= 32 && (NV & (NV - 1)) == 0, "NV");
-  int n = NV;
-#pragma unroll
-  for (uint32_t off = 16; off >= 1; off >>= 1) {
-    if (n > 1) {
-      const bool hi = lane & off;
-      const int h = n / 2;
-#pragma unroll
-      for (int i = 0; i < h; ++i) {
-        const uint32_t r = __shfl_xor_sync(0xffffffffu, hi ? v[i] : v[i + h], off);
-        v[i] = (hi ? v[i + h] : v[i]) + r;
-      }
-      n = h;
-    } else {
-      v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
-    }
-  }
-  return lane / (32u / NV);
-}
-
-// Dynamic shared memory: dA, dB [H] uint16, keys [2*kKnnMaxHalf] uint32,
-// chosen [2*kKnnMaxHalf] uint32, taken bits [ceil(H/32)] uint32.
+// The tract metric: one CTA per sample computes the distances of its two
+// haplotypes and chooses.  Dynamic shared memory: dA, dB [H] uint16, keys
+// [2*kKnnMaxHalf] uint32, chosen [2*kKnnMaxHalf] uint32, taken bits
+// [ceil(H/32)] uint32.
 __global__ void __launch_bounds__(kKnnThreads)
-    knn_kernel(const uint64_t *__restrict__ haps, uint32_t H, uint32_t wn,
-               const uint64_t *__restrict__ mask, uint32_t half, uint32_t dmax, int metric,
-               uint32_t *__restrict__ neighbors) {
+    knn_tract_kernel(const uint64_t *__restrict__ haps, uint32_t H, uint32_t wn,
+                     const uint64_t *__restrict__ mask, uint32_t half, uint32_t dmax,
+                     uint32_t *__restrict__ neighbors) {
   extern __shared__ uint4 knn_smem[];
   uint16_t *dA = reinterpret_cast<uint16_t *>(knn_smem);
   uint16_t *dB = dA + H;
@@ -340,60 +315,26 @@ __global__ void __launch_bounds__(kKnnThreads)
   const uint64_t *ha = haps + (size_t)2 * s * wn, *hb = ha + wn;
   for (uint32_t i = tid; i < (H + 31) / 32; i += kKnnThreads)
     taken[i] = 0;
-  if (metric == 0) {
-    // Hamming distances: kKnnPerWarp haplotypes per warp iteration, words
-    // across lanes (their loads in flight together), then one butterfly over
-    // the 2 kKnnPerWarp sums -- v[2k] and v[2k+1] the distances of haplotype
-    // h0 + k to the sample's two haplotypes.
-    for (uint32_t h0 = kKnnPerWarp * warp; h0 < H; h0 += kKnnPerWarp * (kKnnThreads / 32)) {
-      uint32_t v[2 * kKnnPerWarp];
-#pragma unroll
-      for (int k = 0; k < 2 * kKnnPerWarp; ++k)
-        v[k] = 0;
-#pragma unroll 2
-      for (uint32_t w = lane; w < wn; w += 32) {
-        const uint64_t mw = __ldg(mask + w), xa = __ldg(ha + w), xb = __ldg(hb + w);
-#pragma unroll
-        for (uint32_t k = 0; k < kKnnPerWarp; ++k) {
-          if (h0 + k < H) {
-            const uint64_t ow = __ldg(haps + (size_t)(h0 + k) * wn + w);
-            v[2 * k] += __popcll((xa ^ ow) & mw);
-            v[2 * k + 1] += __popcll((xb ^ ow) & mw);
-          }
-        }
-      }
-      const uint32_t i = warp_sums(v, lane);
-      const uint32_t h = h0 + (i >> 1);
-      if ((lane & (32u / (2 * kKnnPerWarp) - 1u)) == 0 && h < H) {
-        const bool own = (h >> 1) == s;
-        ((i & 1u) ? dB : dA)[h] = own ? kKnnExcluded : (uint16_t)v[0];
-      }
-    }
-  }
-  // tract distances: one haplotype per warp iteration, words across lanes
-  for (uint32_t h = warp; metric != 0 && h < H; h += kKnnThreads / 32) {
-    uint32_t a = 0, b = 0;
+  // distances (the common sites minus the longest run of agreeing common
+  // sites): one haplotype per warp iteration, words across lanes
+  for (uint32_t h = warp; h < H; h += kKnnThreads / 32) {
     const uint64_t *o = haps + (size_t)h * wn;
-    {  // common sites minus the longest run of agreeing common sites
-      Tract ta = {0, 0, 0, 0}, tb = {0, 0, 0, 0};
-      for (uint32_t w0 = 0; w0 < wn; w0 += 32) {
-        const uint32_t w = w0 + lane;
-        Tract xa = {0, 0, 0, 0}, xb = {0, 0, 0, 0};
-        if (w < wn) {
-          const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
-          xa = tract_word((__ldg(ha + w) ^ ow) & mw, mw);
-          xb = tract_word((__ldg(hb + w) ^ ow) & mw, mw);
-        }
-        ta = tract_join(ta, tract_warp(xa, lane));
-        tb = tract_join(tb, tract_warp(xb, lane));
+    Tract ta = {0, 0, 0, 0}, tb = {0, 0, 0, 0};
+    for (uint32_t w0 = 0; w0 < wn; w0 += 32) {
+      const uint32_t w = w0 + lane;
+      Tract xa = {0, 0, 0, 0}, xb = {0, 0, 0, 0};
+      if (w < wn) {
+        const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
+        xa = tract_word((__ldg(ha + w) ^ ow) & mw, mw);
+        xb = tract_word((__ldg(hb + w) ^ ow) & mw, mw);
       }
-      a = ta.len - ta.best;
-      b = tb.len - tb.best;
+      ta = tract_join(ta, tract_warp(xa, lane));
+      tb = tract_join(tb, tract_warp(xb, lane));
     }
     if (lane == 0) {
       const bool own = (h >> 1) == s;
-      dA[h] = own ? kKnnExcluded : (uint16_t)a;
-      dB[h] = own ? kKnnExcluded : (uint16_t)b;
+      dA[h] = own ? kKnnExcluded : (uint16_t)(ta.len - ta.best);
+      dB[h] = own ? kKnnExcluded : (uint16_t)(tb.len - tb.best);
     }
   }
   __syncthreads();
@@ -472,7 +413,7 @@ __global__ void __launch_bounds__(kDistThreads)
 
 // The neighbour lists of the samples s0 + blockIdx.x from their rows of
 // knn_dist_kernel's distances (rows 2 i and 2 i + 1 for the chunk's i-th
-// sample); shared memory as knn_kernel's.
+// sample); shared memory as knn_tract_kernel's.
 __global__ void __launch_bounds__(kKnnThreads)
     knn_select_kernel(const uint16_t *__restrict__ dist, uint32_t H, uint32_t s0, uint32_t half,
                       uint32_t dmax, uint32_t *__restrict__ neighbors) {
