@@ -1562,16 +1562,8 @@ int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, 
                                                      c->d_mask);
   GLP_CUDA(c, cudaGetLastError());
   const size_t smem = glp::knn_smem_bytes(H);
-  if (c->knn_metric == GLP_KNN_TRACT) {
-    GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_tract_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    glp::knn_tract_kernel<<<H / 2, glp::kKnnThreads, smem, c->stream>>>(haps, H, wn, c->d_mask,
-                                                                         half, S, neighbors);
-    GLP_CUDA(c, cudaGetLastError());
-    return GLP_OK;
-  }
-  // Hamming: tiled distances of a chunk of samples (at most 256 MB of them)
-  // into global memory, then the selection, chunk by chunk
+  // tiled distances of a chunk of samples (at most 256 MB of them) into
+  // global memory, then the selection, chunk by chunk
   GLP_CUDA(c, cudaFuncSetAttribute(glp::knn_select_kernel,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t NS = H / 2;
@@ -1579,11 +1571,21 @@ int glp_knn_neighbors(glp_ctx *c, const uint64_t *haps, uint32_t H, uint32_t S, 
       (uint32_t)std::min<size_t>(NS, std::max<size_t>(64, ((size_t)256 << 20) / (4 * (size_t)H)));
   if ((rc = ensure(c, c->d_knn_dist, c->knn_dist_cap, (size_t)2 * chunk * H)))
     return rc;
+  const bool tract = c->knn_metric == GLP_KNN_TRACT;
   for (uint32_t s0 = 0; s0 < NS; s0 += chunk) {
     const uint32_t n = std::min(chunk, NS - s0);
-    const dim3 grid((H + glp::kDistH - 1) / glp::kDistH, (2 * n + glp::kDistQ - 1) / glp::kDistQ);
-    glp::knn_dist_kernel<<<grid, glp::kDistThreads, 0, c->stream>>>(haps, H, wn, c->d_mask,
-                                                                    2 * s0, 2 * n, c->d_knn_dist);
+    if (tract) {
+      const dim3 grid((H + glp::kTractH - 1) / glp::kTractH,
+                      (2 * n + glp::kTractQ - 1) / glp::kTractQ);
+      glp::knn_tract_dist_kernel<<<grid, glp::kDistThreads, 0, c->stream>>>(
+          haps, H, wn, c->d_mask, 2 * s0, 2 * n, c->d_knn_dist);
+    } else {
+      const dim3 grid((H + glp::kDistH - 1) / glp::kDistH,
+                      (2 * n + glp::kDistQ - 1) / glp::kDistQ);
+      glp::knn_dist_kernel<<<grid, glp::kDistThreads, 0, c->stream>>>(haps, H, wn, c->d_mask,
+                                                                      2 * s0, 2 * n,
+                                                                      c->d_knn_dist);
+    }
     glp::knn_select_kernel<<<n, glp::kKnnThreads, smem, c->stream>>>(c->d_knn_dist, H, s0, half,
                                                                     S, neighbors);
     GLP_CUDA(c, cudaGetLastError());

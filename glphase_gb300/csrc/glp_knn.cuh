@@ -12,17 +12,16 @@
 // with the unstable std::sort (kNN.cpp:172-173), so its tie order is
 // implementation-defined.
 //
-// Selection: one CTA per sample with the distances of both its haplotypes
-// to all H haplotypes in shared memory as uint16 (H <= kKnnMaxHaps); the
-// ceil(K/2) nearest are found by binary search on the distance threshold,
-// ties at the threshold are taken in index order through a block scan, and
-// the chosen list is put in (distance, index) order by a bitonic sort.
-// Distances: Hamming as a tiled product of bit matrices (knn_dist_kernel,
-// a chunk of samples at a time through global memory); the tract length in
-// the selecting CTA itself, every warp scoring one haplotype at a time with
-// coalesced word loads and an ordered shuffle reduction (each word's runs
-// of agreeing common sites -- before its first disagreement, after its
-// last, the longest between -- combine left to right).
+// Distances as tiled products of bit matrices, a chunk of samples at a time
+// through global memory: Hamming (knn_dist_kernel), or the tract length
+// (knn_tract_dist_kernel: each word's runs of agreeing common sites --
+// before its first disagreement, after its last, the longest between --
+// joined in site order).  Selection (knn_select_kernel): one CTA per sample
+// with the distances of both its haplotypes to all H haplotypes in shared
+// memory as uint16 (H <= kKnnMaxHaps); the ceil(K/2) nearest are found by
+// binary search on the distance threshold, ties at the threshold are taken
+// in index order through a block scan, and the chosen list is put in
+// (distance, index) order by a bitonic sort.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -120,25 +119,6 @@ __device__ __forceinline__ Tract tract_join(const Tract l, const Tract r) {
   t.pre = l.pre == l.len ? l.len + r.pre : l.pre;
   t.suf = r.suf == r.len ? r.len + l.suf : r.suf;
   t.best = max(max(l.best, r.best), l.suf + r.pre);
-  return t;
-}
-
-// Joins the 32 lanes' stretches in lane order; every lane gets the result.
-__device__ __forceinline__ Tract tract_warp(Tract t, uint32_t lane) {
-#pragma unroll
-  for (uint32_t o = 1; o < 32; o <<= 1) {
-    Tract r;
-    r.len = __shfl_down_sync(0xffffffffu, t.len, o);
-    r.pre = __shfl_down_sync(0xffffffffu, t.pre, o);
-    r.suf = __shfl_down_sync(0xffffffffu, t.suf, o);
-    r.best = __shfl_down_sync(0xffffffffu, t.best, o);
-    if ((lane & (2 * o - 1)) == 0)
-      t = tract_join(t, r);
-  }
-  t.len = __shfl_sync(0xffffffffu, t.len, 0);
-  t.pre = __shfl_sync(0xffffffffu, t.pre, 0);
-  t.suf = __shfl_sync(0xffffffffu, t.suf, 0);
-  t.best = __shfl_sync(0xffffffffu, t.best, 0);
   return t;
 }
 
@@ -295,53 +275,6 @@ __device__ __forceinline__ void knn_choose(uint16_t *dA, uint16_t *dB, uint32_t 
   }
 }
 
-// The tract metric: one CTA per sample computes the distances of its two
-// haplotypes and chooses.  Dynamic shared memory: dA, dB [H] uint16, keys
-// [2*kKnnMaxHalf] uint32, chosen [2*kKnnMaxHalf] uint32, taken bits
-// [ceil(H/32)] uint32.
-__global__ void __launch_bounds__(kKnnThreads)
-    knn_tract_kernel(const uint64_t *__restrict__ haps, uint32_t H, uint32_t wn,
-                     const uint64_t *__restrict__ mask, uint32_t half, uint32_t dmax,
-                     uint32_t *__restrict__ neighbors) {
-  extern __shared__ uint4 knn_smem[];
-  uint16_t *dA = reinterpret_cast<uint16_t *>(knn_smem);
-  uint16_t *dB = dA + H;
-  uint32_t *keys = reinterpret_cast<uint32_t *>(dA + 2 * ((H + 1) & ~1u));
-  uint32_t *chosen = keys + 2 * kKnnMaxHalf;
-  uint32_t *taken = chosen + 2 * kKnnMaxHalf;
-  __shared__ uint32_t red[kKnnThreads / 32];
-  const uint32_t s = blockIdx.x;
-  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint64_t *ha = haps + (size_t)2 * s * wn, *hb = ha + wn;
-  for (uint32_t i = tid; i < (H + 31) / 32; i += kKnnThreads)
-    taken[i] = 0;
-  // distances (the common sites minus the longest run of agreeing common
-  // sites): one haplotype per warp iteration, words across lanes
-  for (uint32_t h = warp; h < H; h += kKnnThreads / 32) {
-    const uint64_t *o = haps + (size_t)h * wn;
-    Tract ta = {0, 0, 0, 0}, tb = {0, 0, 0, 0};
-    for (uint32_t w0 = 0; w0 < wn; w0 += 32) {
-      const uint32_t w = w0 + lane;
-      Tract xa = {0, 0, 0, 0}, xb = {0, 0, 0, 0};
-      if (w < wn) {
-        const uint64_t mw = __ldg(mask + w), ow = __ldg(o + w);
-        xa = tract_word((__ldg(ha + w) ^ ow) & mw, mw);
-        xb = tract_word((__ldg(hb + w) ^ ow) & mw, mw);
-      }
-      ta = tract_join(ta, tract_warp(xa, lane));
-      tb = tract_join(tb, tract_warp(xb, lane));
-    }
-    if (lane == 0) {
-      const bool own = (h >> 1) == s;
-      dA[h] = own ? kKnnExcluded : (uint16_t)(ta.len - ta.best);
-      dB[h] = own ? kKnnExcluded : (uint16_t)(tb.len - tb.best);
-    }
-  }
-  __syncthreads();
-  knn_choose(dA, dB, H, half, dmax, keys, red, chosen, taken,
-             neighbors + (size_t)s * 2 * half);
-}
-
 // Tiled Hamming distances for the kNN build, as a product of bit matrices:
 // dist[q][h] = popcount((hap q0+q XOR hap h) AND mask) over the words, for
 // the query haplotypes [q0, q0 + nq) (2 s and 2 s + 1 for the samples s of a
@@ -411,9 +344,79 @@ __global__ void __launch_bounds__(kDistThreads)
   }
 }
 
+// Tiled tract-length distances (-T), laid out as knn_dist_kernel's: each
+// pair carries the runs of agreeing common sites of the words so far --
+// before the first disagreement, after the last, the longest -- and joins
+// every next word's (tract_word) to them in site order; the distance is the
+// common sites minus the longest run.  A CTA takes 32 queries x 64
+// haplotypes, each thread 2 x 4 pairs.
+constexpr uint32_t kTractQ = 32, kTractH = 64;
+__global__ void __launch_bounds__(kDistThreads)
+    knn_tract_dist_kernel(const uint64_t *__restrict__ haps, uint32_t H, uint32_t wn,
+                          const uint64_t *__restrict__ mask, uint32_t q0, uint32_t nq,
+                          uint16_t *__restrict__ dist) {
+  __shared__ uint64_t sq[kDistW][kTractQ];
+  __shared__ uint64_t sh[kDistW][kTractH];
+  __shared__ uint64_t smask[kDistW];
+  const uint32_t tid = threadIdx.x, tx = tid & 15u, ty = tid >> 4;
+  const uint32_t hb = blockIdx.x * kTractH, qb = blockIdx.y * kTractQ;
+  Tract run[2][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      run[i][j] = Tract{0, 0, 0, 0};
+  for (uint32_t w0 = 0; w0 < wn; w0 += kDistW) {
+    for (uint32_t i = tid; i < kTractQ * kDistW; i += kDistThreads) {
+      const uint32_t r = i / kDistW, k = i % kDistW, w = w0 + k;
+      sq[k][r] = (qb + r < nq && w < wn) ? __ldg(haps + (size_t)(q0 + qb + r) * wn + w) : 0ull;
+    }
+    for (uint32_t i = tid; i < kTractH * kDistW; i += kDistThreads) {
+      const uint32_t r = i / kDistW, k = i % kDistW, w = w0 + k;
+      sh[k][r] = (hb + r < H && w < wn) ? __ldg(haps + (size_t)(hb + r) * wn + w) : 0ull;
+    }
+    if (tid < kDistW)
+      smask[tid] = w0 + tid < wn ? __ldg(mask + w0 + tid) : 0ull;
+    __syncthreads();
+    const uint32_t kn = min(kDistW, wn - w0);
+    for (uint32_t k = 0; k < kn; ++k) {
+      const uint64_t m = smask[k];
+      uint64_t qv[2], hv[4];
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+        qv[i] = sq[k][2 * ty + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        hv[j] = sh[k][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          run[i][j] = tract_join(run[i][j], tract_word((qv[i] ^ hv[j]) & m, m));
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const uint32_t q = qb + 2 * ty + i;
+    if (q >= nq)
+      continue;
+    const uint32_t s = (q0 + q) >> 1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t h = hb + tx + 16 * j;
+      if (h < H)
+        dist[(size_t)q * H + h] =
+            (h >> 1) == s ? kKnnExcluded : (uint16_t)(run[i][j].len - run[i][j].best);
+    }
+  }
+}
+
 // The neighbour lists of the samples s0 + blockIdx.x from their rows of
 // knn_dist_kernel's distances (rows 2 i and 2 i + 1 for the chunk's i-th
-// sample); shared memory as knn_tract_kernel's.
+// sample).  Dynamic shared memory (knn_smem_bytes): dA, dB [H] uint16, keys
+// [2*kKnnMaxHalf] uint32, chosen [2*kKnnMaxHalf] uint32, taken bits
+// [ceil(H/32)] uint32.
 __global__ void __launch_bounds__(kKnnThreads)
     knn_select_kernel(const uint16_t *__restrict__ dist, uint32_t H, uint32_t s0, uint32_t half,
                       uint32_t dmax, uint32_t *__restrict__ neighbors) {
