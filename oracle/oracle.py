@@ -1,5 +1,6 @@
-"""ctypes bindings to the CPU oracle (oracle/libglp_oracle.so) and, where it
-was built, to the reference's own impute.cpp (oracle/_ref/libglp_ref.so).
+"""ctypes bindings to the CPU oracle (oracle/libglp_oracle.so) and, where they
+were built, to the reference's own impute.cpp (oracle/_ref/libglp_ref.so) and
+kNN surrogate restriction (oracle/_ref/libglp_ref_knn.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
 by the CPU-baseline leg of bench.py, never by the product package.
@@ -15,6 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libglp_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libglp_ref.so")
+REF_KNN_PATH = os.path.join(HERE, "_ref", "libglp_ref_knn.so")
 REF_TREE = "/root/reference"
 
 EMIT_FLOAT = 0
@@ -51,6 +53,7 @@ class Trace(C.Structure):
 
 _lib = None
 _ref = None
+_ref_knn = None
 
 
 def lib():
@@ -125,6 +128,40 @@ def ref():
         R.glpr_replace.argtypes = [_u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _u32p]
         _ref = R
     return _ref
+
+
+def ref_knn_available() -> bool:
+    return os.path.exists(REF_KNN_PATH)
+
+
+def ref_knn():
+    """The reference's own kNN.cpp / haplotype.cpp (``make -C oracle ref``)."""
+    global _ref_knn
+    if _ref_knn is None:
+        R = C.CDLL(REF_KNN_PATH)
+        R.glpr_knn.restype = C.c_int
+        R.glpr_knn.argtypes = [_u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                               C.c_double, C.c_double, C.c_int, C.c_int, _u32p]
+        R.glpr_max_tract.restype = C.c_uint32
+        R.glpr_max_tract.argtypes = [_u8p, _u8p, C.c_uint32]
+        R.glpr_hamming.restype = C.c_uint32
+        R.glpr_hamming.argtypes = [_u8p, _u8p, C.c_uint32]
+        _ref_knn = R
+    return _ref_knn
+
+
+def ref_knn_lists(haps, S, K, lb=0.0, ub=1.0, use_maf=False, metric="hamming"):
+    """KNN::Neighbors of every sample from the reference's own ClusterHaps:
+    [H/2][2*ceil(K/2)] (the frequencies come from ``haps`` themselves, as
+    the reference computes them from its scaffold)."""
+    haps = _c(haps, np.uint64)
+    H, wn = haps.shape
+    half = (K + 1) // 2
+    out = np.zeros((H // 2, 2 * half), np.uint32)
+    if ref_knn().glpr_knn(haps, H, wn, S, K, lb, ub, int(use_maf), KNN_METRICS[metric],
+                          out) != 0:
+        raise ValueError("the reference's KNN refused the arguments")
+    return out
 
 
 def _c(a, dt):

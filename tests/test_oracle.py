@@ -378,3 +378,88 @@ def test_knn_tract_metric_lists(oracle_lib):
     tract = O.knn(haps, S, 2, metric="tract")
     assert ham[0][0] == 2      # Hamming: 1 < 3
     assert tract[0][0] == 3    # tract: 97 shared sites > 50
+
+
+# --- the kNN restatement against the reference's own kNN.cpp -----------------
+
+def _knn_cases(rng, n, H_choices, S_max):
+    """Random panels with site frequencies spread over (0, 1), and the
+    frequency-bound variants of KNN's constructor (plain, an allele-frequency
+    window, a minor-allele-frequency cap)."""
+    for t in range(n):
+        H = int(rng.choice(H_choices))
+        S = int(rng.integers(1, S_max))
+        K = int(rng.integers(1, H - 1))
+        if 2 * ((K + 1) // 2) > H - 2:
+            K = H - 2
+        bits = (rng.random((H, S)) < rng.random(S)).astype(np.uint8)
+        lb, ub, maf = 0.0, 1.0, False
+        if t % 3 == 1:
+            lb, ub = (float(x) for x in sorted(rng.random(2)))
+        elif t % 3 == 2:
+            ub, maf = float(rng.random() * 0.5), True
+        yield mdl.pack_haplotypes(bits), S, K, lb, ub, maf
+
+
+@pytest.mark.skipif("not __import__('oracle').ref_knn_available()")
+def test_knn_metrics_match_live_reference_build(oracle_lib):
+    """Haplotype::MaxTractLen and HammingDist of the reference's compiled
+    haplotype.cpp against the oracle's word-wise restatements on random
+    pairs (lengths 1 .. 300, sparse and dense disagreements)."""
+    O = oracle_lib
+    R = O.ref_knn()
+    rng = np.random.default_rng(21)
+    for _ in range(600):
+        n = int(rng.integers(1, 300))
+        a = rng.integers(0, 2, n).astype(np.uint8)
+        flip = rng.random(n) < rng.choice([0.005, 0.05, 0.3])
+        b = np.where(flip, 1 - a, a).astype(np.uint8)
+        pa, pb = mdl.pack_haplotypes(a[None])[0], mdl.pack_haplotypes(b[None])[0]
+        every = np.zeros_like(pa)
+        for i in range(n):
+            every[i >> 6] |= np.uint64(1) << np.uint64(i & 63)
+        assert O.max_tract(pa, pb, every) == R.glpr_max_tract(a, b, n)
+        assert R.glpr_hamming(a, b, n) == int(flip.sum())
+
+
+@pytest.mark.skipif("not __import__('oracle').ref_knn_available()")
+def test_knn_lists_match_live_reference_build(oracle_lib):
+    """KNN::ClusterHaps of the reference's compiled kNN.cpp against the
+    oracle's lists, both metrics, with and without frequency bounds.
+
+    The reference orders each haplotype's distances with std::sort on the
+    distance alone, whose tie order is unspecified; the oracle breaks ties by
+    haplotype index.  With at most 16 candidates (H <= 18) libstdc++'s sort
+    is a plain insertion sort, which keeps equal distances in index order, so
+    there the lists must be identical.  On larger panels the check is
+    tie-blind: list A's distances in order, and, where both picked the same
+    set for A, list B's distances in order."""
+    O = oracle_lib
+    rng = np.random.default_rng(23)
+    for haps, S, K, lb, ub, maf in _knn_cases(rng, 120, [4, 6, 8, 10, 12, 14, 16, 18], 400):
+        for metric in ("hamming", "tract"):
+            want = O.ref_knn_lists(haps, S, K, lb, ub, maf, metric)
+            got = O.knn(haps, S, K, lb, ub, maf, metric=metric)
+            assert np.array_equal(got, want), (haps.shape, S, K, lb, ub, maf, metric)
+
+    def dist(h, o, mask, metric):
+        if metric == "hamming":
+            return sum(bin(int(x)).count("1") for x in (h ^ o) & mask)
+        return sum(bin(int(x)).count("1") for x in mask) - O.max_tract(h, o, mask)
+
+    checked_b = 0
+    for haps, S, K, lb, ub, maf in _knn_cases(rng, 4, [300], 700):
+        mask = O.common_sites(haps, S, lb, ub, maf)
+        for metric in ("hamming", "tract"):
+            want = O.ref_knn_lists(haps, S, K, lb, ub, maf, metric)
+            got = O.knn(haps, S, K, lb, ub, maf, metric=metric)
+            for s in range(0, haps.shape[0] // 2, 7):
+                dA = [[dist(haps[2 * s], haps[h], mask, metric) for h in lst[0::2]]
+                      for lst in (want[s], got[s])]
+                assert dA[0] == dA[1]
+                if set(want[s][0::2]) == set(got[s][0::2]):
+                    dB = [[dist(haps[2 * s + 1], haps[h], mask, metric) for h in lst[1::2]]
+                          for lst in (want[s], got[s])]
+                    assert dB[0] == dB[1]
+                    checked_b += 1
+    assert checked_b > 0
