@@ -1,6 +1,7 @@
 """ctypes bindings to the CPU oracle (oracle/libglp_oracle.so) and, where they
-were built, to the reference's own impute.cpp (oracle/_ref/libglp_ref.so) and
-kNN surrogate restriction (oracle/_ref/libglp_ref_knn.so).
+were built, to the reference's own impute.cpp (oracle/_ref/libglp_ref.so),
+kNN surrogate restriction (oracle/_ref/libglp_ref_knn.so) and GL packing
+(oracle/_ref/libglp_ref_glpack.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
 by the CPU-baseline leg of bench.py, never by the product package.
@@ -17,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libglp_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libglp_ref.so")
 REF_KNN_PATH = os.path.join(HERE, "_ref", "libglp_ref_knn.so")
+REF_GLPACK_PATH = os.path.join(HERE, "_ref", "libglp_ref_glpack.so")
 REF_TREE = "/root/reference"
 
 EMIT_FLOAT = 0
@@ -54,6 +56,7 @@ class Trace(C.Structure):
 _lib = None
 _ref = None
 _ref_knn = None
+_ref_glpack = None
 
 
 def lib():
@@ -148,6 +151,33 @@ def ref_knn():
         R.glpr_hamming.argtypes = [_u8p, _u8p, C.c_uint32]
         _ref_knn = R
     return _ref_knn
+
+
+def ref_glpack_available() -> bool:
+    return os.path.exists(REF_GLPACK_PATH)
+
+
+def ref_glpack(gl, use_vq=True, bits=4):
+    """GLPack of the reference's own glPack.cpp / glVQ.cpp over all samples:
+    (packed words [ceil(S / (32 / bits))][N], codebook [2^bits][2]) for GLs
+    [N][S][3]; 8-bit nibble form when ``use_vq`` is false.  Its codebook is
+    trained from the GLs with the GSL stand-in's counter draws."""
+    global _ref_glpack
+    if _ref_glpack is None:
+        R = C.CDLL(REF_GLPACK_PATH)
+        R.glpr_glpack.restype = C.c_int
+        R.glpr_glpack.argtypes = [_f32p, C.c_uint32, C.c_uint32, C.c_int, C.c_uint32, _u32p,
+                                  _f32p]
+        _ref_glpack = R
+    gl = _c(gl, np.float32)
+    N, S = gl.shape[0], gl.shape[1]
+    b = bits if use_vq else 8
+    per = 32 // b
+    packed = np.zeros(((S + per - 1) // per, N), np.uint32)
+    cb = np.zeros((2 ** b, 2), np.float32)
+    if _ref_glpack.glpr_glpack(gl, N, S, int(use_vq), b, packed, cb) != 0:
+        raise ValueError("the reference's GLPack refused the arguments")
+    return packed, cb
 
 
 def ref_knn_lists(haps, S, K, lb=0.0, ub=1.0, use_maf=False, metric="hamming"):

@@ -1,17 +1,19 @@
 /*
  * Stand-in for the reference's src/olivier/utils.hpp, used only to compile
- * the reference's kNN.cpp and sampler.cpp in place (oracle/Makefile ->
- * oracle/_ref).  The original pulls in Boost (program_options, iostreams,
- * uuid), which is not installed here.  Of it, kNN.cpp and sampler.cpp use
- * only the standard headers below and the file classes ofile/ifile, and those
- * only in their Save() members, which the oracle's harness never calls.  This
- * file is test infrastructure.
+ * the reference's kNN.cpp, sampler.cpp, glPack.cpp and glVQ.cpp in place
+ * (oracle/Makefile -> oracle/_ref).  The original pulls in Boost
+ * (program_options, iostreams, uuid), which is not installed here.  Of it,
+ * those files use only the standard headers below and the file classes
+ * ofile/ifile, and those only in Save() members, which the oracle's
+ * harnesses never call.  This file is test infrastructure.
  */
 #ifndef GLP_REF_SHIM_UTILS_HPP
 #define GLP_REF_SHIM_UTILS_HPP
 
 #include <cassert>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <fstream>
 #include <iostream>
 #include <memory>

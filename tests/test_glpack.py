@@ -1,7 +1,9 @@
 """GL packing for the device (glphase_gb300/glpack.py) against the reference's
-unit tests (src/testing/glPack_unittests.cpp) and the decode rule of the
-device kernel (hmmLike.cu:12-28)."""
+unit tests (src/testing/glPack_unittests.cpp), the decode rule of the
+device kernel (hmmLike.cu:12-28) and, where oracle/_ref holds it, the
+reference's own glPack.cpp / glVQ.cpp compiled from its tree."""
 import numpy as np
+import pytest
 
 from glphase_gb300.glpack import GLPack, GLVQ, gl2halfchar
 
@@ -66,3 +68,39 @@ def test_vq_packing_layout_and_decode():
             het = gls[s, m, 1] / gls[s, m].sum()
             d = (cb[:, 0] - rr) ** 2 + (cb[:, 1] - het) ** 2
             assert code == int(np.argmin(d))
+
+
+def _edge_gls(rng, N, S):
+    """Random GL trios, unnormalised in part, with some homRef/het values on
+    the 1/16 grid where GL2HalfChar's epsilon matters, and one-hot trios."""
+    gl = rng.dirichlet([0.3, 0.3, 0.3], (N, S)).astype(np.float32)
+    grid = rng.random((N, S)) < 0.2
+    k = rng.integers(0, 8, (N, S, 2)).astype(np.float32) / 16
+    gl[grid, 0], gl[grid, 1] = k[grid, 0], k[grid, 1]
+    gl[grid, 2] = 1 - gl[grid, 0] - gl[grid, 1]
+    hot = rng.random((N, S)) < 0.05
+    gl[hot] = np.eye(3, dtype=np.float32)[rng.integers(0, 3, int(hot.sum()))]
+    scale = np.where(rng.random((N, 1, 1)) < 0.5, rng.random((N, 1, 1)) + 0.1, 1.0)
+    return (gl * scale).astype(np.float32)
+
+
+@pytest.mark.skipif("not __import__('oracle').ref_glpack_available()")
+def test_packing_matches_live_reference_build(oracle_lib):
+    """GLPack::GetPackedGLs of the reference's compiled glPack.cpp / glVQ.cpp
+    against glpack.py, word for word: the 8-bit nibble form, and 2-, 4- and
+    8-bit VQ codes packed against the codebook the reference trained (the
+    codebook training itself differs by design: binary64 sums in a fixed
+    order and a counter-based pick for empty entries).  Site counts that
+    leave a partial last word take the array's first GL there, as the
+    reference does."""
+    O = oracle_lib
+    rng = np.random.default_rng(31)
+    for N, S in ((1, 1), (1, 9), (3, 4), (7, 33), (29, 282), (40, 256)):
+        gl = _edge_gls(rng, N, S)
+        want, _ = O.ref_glpack(gl, use_vq=False)
+        assert np.array_equal(GLPack(gl, use_vq=False).packed_gls(), want), (N, S)
+        for bits in (2, 4, 8):
+            want, cb = O.ref_glpack(gl, use_vq=True, bits=bits)
+            gp = GLPack(gl, np.random.default_rng(0), use_vq=True, bits=bits)
+            gp.vq.codebook = cb.copy()
+            assert np.array_equal(gp.packed_gls(), want), (N, S, bits)
