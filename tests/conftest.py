@@ -10,7 +10,7 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
 
 
 def pytest_configure(config):
-    config.addinivalue_line("markers", "gpu: needs an sm_103 GPU (run on the GPU box)")
+    config.addinivalue_line("markers", "gpu: needs an sm_103 (GB300) GPU")
 
 
 @pytest.fixture(scope="session")
