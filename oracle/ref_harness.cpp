@@ -11,10 +11,13 @@
  *   glpr_hmm_work   -> Impute::hmm_work   (impute.cpp:380-485)
  *   glpr_initialize -> Impute::initialize (impute.cpp:182-322), model part
  *   glpr_replace    -> Impute::replace    (impute.cpp:564-595)
+ *   glpr_mh_chain   -> MHSampler<unsigned>::SampleHap (MHSampler.hpp:81-96),
+ *                      plain MH, over a sequence of proposals
  */
 #include <cstring>
 #include <vector>
 
+#include "MHSampler.hpp"
 #include "impute.hpp"
 
 namespace {
@@ -117,5 +120,28 @@ void glpr_replace(const uint64_t *haps, uint32_t N, uint32_t S, uint32_t wn,
                   uint32_t sample, uint32_t *hsum) {
   RefImpute r;
   r.tally(haps, N, S, wn, sample, hsum);
+}
+
+// A chain as Insti::solve runs it (insti.cpp:1497-1531): the sampler starts
+// at log-likelihood like[0]; proposal c (1 .. n) changes the state from
+// c - 1 to c with log-likelihood like[c] and is accepted or reverted.  The
+// sampler draws its uniforms from u in order (one per proposal that scores
+// below the current likelihood).  accept[c - 1] and state[c - 1] receive the
+// decision and the state after it.
+void glpr_mh_chain(const double *like, uint32_t n, double pen, const double *u,
+                   uint32_t nu, uint8_t *accept, uint32_t *state) {
+  gsl_rng *rng = gsl_rng_alloc(gsl_rng_default);
+  rng->u = u;
+  rng->nu = nu;
+  rng->pu = 0;
+  MHSampler<unsigned> mh(rng, like[0], pen);
+  unsigned object = 0;
+  for (uint32_t c = 1; c <= n; ++c) {
+    const unsigned prev = object;
+    object = c;
+    accept[c - 1] = mh.SampleHap(object, prev, like[c]) ? 1 : 0;
+    state[c - 1] = object;
+  }
+  gsl_rng_free(rng);
 }
 }

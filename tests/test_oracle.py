@@ -182,6 +182,41 @@ def test_mh_accept_semantics(oracle_lib):
     assert L.glpo_mh_accept(curr + d, curr, 0.25, math.exp(d * 0.25) * 0.999) == 1
 
 
+@pytest.mark.skipif("not __import__('oracle').ref_available()")
+def test_mh_chain_matches_live_reference_build(oracle_lib):
+    """MHSampler<unsigned>::SampleHap of the reference (plain MH,
+    MHSampler.hpp:81-96, compiled into oracle/_ref) against the oracle's
+    accept rule over whole chains: the same decisions, the same reverted
+    states, and a uniform consumed exactly when a proposal scores below the
+    current likelihood.  Chains mix ties, near ties and large drops, at the
+    annealing penalties 1, 0.25 and 0.04."""
+    O = oracle_lib
+    L, R = O.lib(), O.ref()
+    rng = np.random.default_rng(41)
+    for t in range(300):
+        n = int(rng.integers(1, 120))
+        pen = float(rng.choice([1.0, 0.25, 0.04]))
+        # proposals around the start's likelihood: equal, a hair above or
+        # below, moderately and far below; every other chain with noise added
+        steps = rng.choice([0.0, 1e-9, -1e-9, 0.3, -0.3, -5.0, -60.0], size=n)
+        like = -1e4 + np.concatenate([[0.0], steps])
+        like = np.minimum(like + rng.normal(0, 0.2, n + 1) * (t % 2), 0.0)
+        u = rng.random(n + 1)
+        acc = np.zeros(n, np.uint8)
+        state = np.zeros(n, np.uint32)
+        R.glpr_mh_chain(np.ascontiguousarray(like), n, pen, u, u.size, acc, state)
+        curr, obj, k = like[0], 0, 0
+        for c in range(1, n + 1):
+            if like[c] >= curr:
+                a = 1
+            else:
+                a = L.glpo_mh_accept(like[c], curr, pen, u[k])
+                k += 1
+            if a:
+                curr, obj = like[c], c
+            assert acc[c - 1] == a and state[c - 1] == obj, (t, c)
+
+
 def test_hap_packing_round_trip():
     rng = np.random.default_rng(3)
     for S in (1, 63, 64, 65, 200):
