@@ -20,8 +20,8 @@ LIB = os.path.join(PKG, "libglphase_gpu.so")
 SOURCES = ["glp_api.cu", "glp_gen_single_f32.cu", "glp_gen_single_vq.cu",
            "glp_gen_multi_f32.cu", "glp_gen_multi_vq.cu", "glp_gen_single_f32_sub4.cu",
            "glp_gen_single_vq_sub4.cu", "glp_gen_multi_f32_sub4.cu", "glp_gen_multi_vq_sub4.cu"]
-HEADERS = ["glp_kernels.cuh", "glp_rng.h", "glp_launch.h", "glp_knn.cuh", "glp_tally.cuh", "glp_vq.cuh",
-           "glp_server_core.h"]
+HEADERS = ["glp_kernels.cuh", "glp_rng.h", "glp_launch.h", "glp_knn.cuh", "glp_tract.h",
+           "glp_tally.cuh", "glp_vq.cuh", "glp_server_core.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "--expt-relaxed-constexpr"]

@@ -16,16 +16,18 @@
 // through global memory: Hamming (knn_dist_kernel), or the tract length
 // (knn_tract_dist_kernel: each word's runs of agreeing common sites --
 // before its first disagreement, after its last, the longest between --
-// joined in site order).  Selection (knn_select_kernel): one CTA per sample
-// with the distances of both its haplotypes to all H haplotypes in shared
-// memory as uint16 (H <= kKnnMaxHaps); the ceil(K/2) nearest are found by
-// binary search on the distance threshold, ties at the threshold are taken
-// in index order through a block scan, and the chosen list is put in
-// (distance, index) order by a bitonic sort.
+// joined in site order, glp_tract.h).  Selection (knn_select_kernel): one
+// CTA per sample with the distances of both its haplotypes to all H
+// haplotypes in shared memory as uint16 (H <= kKnnMaxHaps); the ceil(K/2)
+// nearest are found by binary search on the distance threshold, ties at the
+// threshold are taken in index order through a block scan, and the chosen
+// list is put in (distance, index) order by a bitonic sort.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "glp_tract.h"
 
 namespace glp {
 
@@ -60,66 +62,6 @@ __global__ void common_sites_kernel(const uint64_t *__restrict__ haps, uint32_t 
   __syncthreads();
   if (lane == 0)
     mask[w] = (uint64_t)lo | ((uint64_t)hi_bits << 32);
-}
-
-// Runs of agreeing common sites in a stretch of words: len common sites, pre
-// of them before the first disagreement, suf after the last, best the longest
-// run; pre == len when the stretch has no disagreement.
-struct Tract {
-  uint32_t len, pre, suf, best;
-};
-
-// One word: x the disagreements at common sites, m the common sites.
-__device__ __forceinline__ Tract tract_word(uint64_t x, uint64_t m) {
-  Tract t;
-  t.len = (uint32_t)__popcll(m);
-  if (x == 0) {
-    t.pre = t.suf = t.best = t.len;
-    return t;
-  }
-  const int lo = __ffsll((long long)x) - 1, hi = 63 - __clzll((long long)x);
-  if (m == ~0ull) {  // every site common: the longest run of agreements in log steps
-    const uint64_t r1 = ~x, r2 = r1 & (r1 >> 1), r4 = r2 & (r2 >> 2), r8 = r4 & (r4 >> 4),
-                   r16 = r8 & (r8 >> 8), r32 = r16 & (r16 >> 16);
-    // cur: the starts of runs of at least n agreements; n grows greedily
-    uint64_t cur = ~0ull;
-    uint32_t n = 0;
-    const uint64_t rs[6] = {r32, r16, r8, r4, r2, r1};
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      const uint64_t cand = cur & (rs[i] >> n);
-      if (cand) {
-        n += 32u >> i;
-        cur = cand;
-      }
-    }
-    t.pre = (uint32_t)lo;
-    t.suf = (uint32_t)(63 - hi);
-    t.best = n;
-    return t;
-  }
-  t.pre = (uint32_t)__popcll(m & ((1ull << lo) - 1ull));
-  t.suf = hi == 63 ? 0u : (uint32_t)__popcll(m >> (hi + 1));
-  uint32_t best = max(t.pre, t.suf);
-  int prev = lo;
-  for (uint64_t y = x & (x - 1ull); y; y &= y - 1ull) {  // runs between disagreements
-    const int q = __ffsll((long long)y) - 1;           // prev < q <= 63
-    const uint64_t between = ((1ull << q) - 1ull) & ~((2ull << prev) - 1ull);
-    best = max(best, (uint32_t)__popcll(m & between));
-    prev = q;
-  }
-  t.best = best;
-  return t;
-}
-
-// The stretch l followed by the stretch r.
-__device__ __forceinline__ Tract tract_join(const Tract l, const Tract r) {
-  Tract t;
-  t.len = l.len + r.len;
-  t.pre = l.pre == l.len ? l.len + r.pre : l.pre;
-  t.suf = r.suf == r.len ? r.len + l.suf : r.suf;
-  t.best = max(max(l.best, r.best), l.suf + r.pre);
-  return t;
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *red) {
