@@ -306,13 +306,19 @@ int set_emission(glp_problem *pb, const float *emit, const float *prob, uint32_t
   if (pb->eN != N || pb->eS != S || pb->borrowed) {
     drop_emission(pb);
     GLP_CUDA(c, cudaMalloc((void **)&pb->d_emit, sizeof(float4) * ns));
-    GLP_CUDA(c, cudaMalloc((void **)&pb->d_prob, sizeof(float) * 3 * ns));
     pb->eN = N;
     pb->eS = S;
   }
   GLP_CUDA(c, cudaMemcpy(pb->d_emit, emit, sizeof(float4) * ns, cudaMemcpyHostToDevice));
-  if (prob)
-    GLP_CUDA(c, cudaMemcpy(pb->d_prob, prob, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice));
+  if (!prob) {
+    // no genotype probabilities with these emissions (earlier ones belong to
+    // other GLs): a generation that runs hmm_work is refused
+    release(pb->d_prob);
+    return GLP_OK;
+  }
+  if (!pb->d_prob)
+    GLP_CUDA(c, cudaMalloc((void **)&pb->d_prob, sizeof(float) * 3 * ns));
+  GLP_CUDA(c, cudaMemcpy(pb->d_prob, prob, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice));
   return GLP_OK;
 }
 

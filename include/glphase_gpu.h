@@ -142,7 +142,8 @@ int glp_set_packed_gls(glp_ctx *ctx, const uint32_t *packed, size_t num_words);
 /* Float emission [N][S][4] and genotype probabilities [N][S][3] from the
  * host (Insti::initialize's emit and prob, src/insti.cpp:1345-1382): the
  * inputs of Impute::hmm_like and of the fused hmm_work.  prob may be NULL
- * when hmm_work is never run. */
+ * when hmm_work is never run: a generation that runs it is then refused with
+ * GLP_ERR_STATE until genotype probabilities are set with the emissions. */
 int glp_set_emission(glp_ctx *ctx, const float *emit, const float *prob, uint32_t num_samples,
                      uint32_t num_sites);
 

@@ -323,6 +323,30 @@ def test_argument_errors(dev):
     assert dev.L.glp_run_generation_host(dev.ctx, C.byref(a)) == nat.GLP_ERR_ARG
 
 
+def test_hmm_work_needs_genotype_probabilities(dev):
+    """Emissions set without genotype probabilities (prob NULL, for callers
+    that never run hmm_work): a generation with hmm_work is refused with
+    GLP_ERR_STATE instead of sampling from stale or unset probabilities, one
+    without it (GLP_GEN_NO_WORK) runs, and setting them again restores
+    hmm_work."""
+    m, haps, quad, props = make_problem(N=8, S=100, C=5)
+    run_gpu(dev, m, haps, quad, props, 1.0)          # emissions and probabilities set
+    dev.copy_emission_to_device(m.emit, None)        # emissions only
+    h = np.ascontiguousarray(haps)
+    hn, q = h.copy(), np.ascontiguousarray(quad, dtype=np.uint32)
+    qo, p = np.zeros_like(q), np.ascontiguousarray(props, dtype=np.uint32)
+    a = nat.GenerationArgs()
+    a.num_samples, a.num_sites, a.num_cycles, a.num_haps = m.N, m.S, props.shape[0], h.shape[0]
+    a.haps, a.hnew, a.hap_idxs_in, a.hap_idxs_out, a.props = _p(h), _p(hn), _p(q), _p(qo), _p(p)
+    a.pen = 1.0
+    assert dev.L.glp_run_generation_host(dev.ctx, C.byref(a)) == nat.GLP_ERR_STATE
+    assert b"genotype probabilities" in dev.L.glp_last_error(dev.ctx)
+    a.flags = nat.GLP_GEN_NO_WORK
+    assert dev.L.glp_run_generation_host(dev.ctx, C.byref(a)) == nat.GLP_OK
+    out = run_gpu(dev, m, haps, quad, props, 1.0)    # probabilities set again
+    assert out["quad"].shape == (4, m.N)
+
+
 def test_vq_mode_matches_device_reference_semantics(dev, oracle_lib):
     """VQ-decoded emissions (HMMLikeCUDA::hmmLike, hmmLike.cu:53-142)."""
     from glphase_gb300.glpack import GLPack
