@@ -210,6 +210,14 @@ int check_ctx(glp_ctx *c) {
   return GLP_OK;
 }
 
+// The model set-up calls overwrite device buffers with synchronous copies,
+// which are not ordered with the context's (non-blocking) stream: they first
+// wait for the work already enqueued there, which reads the old contents.
+int quiesce(glp_ctx *c) {
+  GLP_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GLP_OK;
+}
+
 // FillEmit of every codebook entry (hmmLike.cu:12-44): G = (cb0, cb1,
 // max(1 - cb0 - cb1, 0)), emit[i] = pc[i][0] G0 + pc[i][1] G1 + pc[i][2] G1
 // + pc[i][3] G2.  Host code is built with -ffp-contract=off, so each term is
@@ -235,6 +243,8 @@ int upload_vq_table(glp_problem *pb) {
   }
   if (!pb->d_vq)
     GLP_CUDA(c, cudaMalloc((void **)&pb->d_vq, sizeof(tab)));
+  else if (int rc = quiesce(c))
+    return rc;
   GLP_CUDA(c, cudaMemcpy(pb->d_vq, tab, sizeof(tab), cudaMemcpyHostToDevice));
   return GLP_OK;
 }
@@ -255,6 +265,8 @@ int set_tran(glp_problem *pb, const float *tran, uint32_t S) {
   t4[S] = make_float4(1.f, 0.f, 0.f, 1.f);
   for (uint32_t m = 0; m <= S; ++m)
     t4[S + 1 + m] = make_float4(t4[m].y, t4[m].z, t4[m].w, t4[m].w);
+  if (int rc = quiesce(c))
+    return rc;
   if (pb->S != S) {
     release(pb->d_tran4);
     pb->S = 0;
@@ -287,6 +299,8 @@ int set_packed(glp_problem *pb, const uint32_t *packed, size_t n) {
   glp_ctx *c = pb->ctx;
   if (!packed || n == 0)
     return fail(c, GLP_ERR_ARG, "packed GLs must be non-empty");
+  if (int rc = quiesce(c))
+    return rc;
   if (n != pb->packed_words) {
     release(pb->d_packed);
     pb->packed_words = 0;
@@ -302,6 +316,8 @@ int set_emission(glp_problem *pb, const float *emit, const float *prob, uint32_t
   glp_ctx *c = pb->ctx;
   if (!emit || N == 0 || S == 0)
     return fail(c, GLP_ERR_ARG, "emit must be non-null with positive N and S");
+  if (int rc = quiesce(c))
+    return rc;
   const size_t ns = (size_t)N * S;
   if (pb->eN != N || pb->eS != S || pb->borrowed) {
     drop_emission(pb);

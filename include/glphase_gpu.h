@@ -120,7 +120,11 @@ void glp_destroy(glp_ctx *ctx);
 const char *glp_last_error(const glp_ctx *ctx);
 
 /* Bind the context to a CUDA stream (cudaStream_t; NULL = the context's own
- * stream).  Device-pointer calls are asynchronous on that stream. */
+ * stream).  Device-pointer calls are asynchronous on that stream.  The model
+ * set-up calls (glp_set_tran, glp_set_mutation_mat, glp_set_codebook,
+ * glp_set_packed_gls, glp_set_emission, glp_problem_set_model,
+ * glp_problem_set_vq) copy synchronously and first wait for the work already
+ * on that stream, so generations enqueued before them read the old data. */
 int glp_set_stream(glp_ctx *ctx, void *stream);
 
 /* Transition matrix tran [S][3].  Replaces HMMLikeCUDA::CopyTranToDevice
