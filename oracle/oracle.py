@@ -1,7 +1,7 @@
 """ctypes bindings to the CPU oracle (oracle/libglp_oracle.so) and, where they
 were built, to the reference's own impute.cpp (oracle/_ref/libglp_ref.so),
-kNN surrogate restriction (oracle/_ref/libglp_ref_knn.so) and GL packing
-(oracle/_ref/libglp_ref_glpack.so).
+kNN surrogate restriction (oracle/_ref/libglp_ref_knn.so), GL packing
+(oracle/_ref/libglp_ref_glpack.so) and genetic map (oracle/_ref/libglp_ref_map.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
 by the CPU-baseline leg of bench.py, never by the product package.
@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(HERE, "libglp_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libglp_ref.so")
 REF_KNN_PATH = os.path.join(HERE, "_ref", "libglp_ref_knn.so")
 REF_GLPACK_PATH = os.path.join(HERE, "_ref", "libglp_ref_glpack.so")
+REF_MAP_PATH = os.path.join(HERE, "_ref", "libglp_ref_map.so")
 REF_TREE = "/root/reference"
 
 EMIT_FLOAT = 0
@@ -57,6 +58,7 @@ _lib = None
 _ref = None
 _ref_knn = None
 _ref_glpack = None
+_ref_map = None
 
 
 def lib():
@@ -180,6 +182,29 @@ def ref_glpack(gl, use_vq=True, bits=4):
     if _ref_glpack.glpr_glpack(gl, N, S, int(use_vq), b, packed, cb) != 0:
         raise ValueError("the reference's GLPack refused the arguments")
     return packed, cb
+
+
+def ref_map_available() -> bool:
+    return os.path.exists(REF_MAP_PATH)
+
+
+def ref_genetic_distances(path, positions):
+    """GeneticMap of the reference's own geneticMap.cpp on an uncompressed map
+    file: (GeneticLocation in cM, GeneticDistance from the previous position
+    in Morgans, 0 first) at ``positions``; ValueError where the reference
+    throws."""
+    global _ref_map
+    if _ref_map is None:
+        R = C.CDLL(REF_MAP_PATH)
+        R.glpr_genetic_distances.restype = C.c_int
+        R.glpr_genetic_distances.argtypes = [C.c_char_p, _u32p, C.c_uint32, _f64p, _f64p]
+        _ref_map = R
+    pos = _c(positions, np.uint32)
+    loc = np.zeros(pos.size, np.float64)
+    dist = np.zeros(pos.size, np.float64)
+    if _ref_map.glpr_genetic_distances(os.fsencode(path), pos, pos.size, loc, dist) != 0:
+        raise ValueError("the reference's GeneticMap threw")
+    return loc, dist
 
 
 def ref_knn_lists(haps, S, K, lb=0.0, ub=1.0, use_maf=False, metric="hamming"):

@@ -194,6 +194,38 @@ def test_genetic_map(tmp_path):
         gio.read_genetic_map(str(p))
 
 
+@pytest.mark.skipif("not __import__('oracle').ref_map_available()")
+def test_genetic_map_matches_live_reference_build(tmp_path, oracle_lib):
+    """GeneticMap of the reference's compiled geneticMap.cpp against
+    io.GeneticMap on random maps (1 .. 60 rows, cM written with 1 .. 11
+    decimals): locations and distances identical in binary64 at map
+    positions and between them; the same files and positions refused
+    (malformed rows, unsorted positions, positions off the map)."""
+    O = oracle_lib
+    rng = np.random.default_rng(19)
+    path = tmp_path / "m.map"
+    for _ in range(150):
+        k = int(rng.integers(1, 60))
+        pos = np.cumsum(rng.integers(1, 5000, k)) + int(rng.integers(0, 10**6))
+        cm = np.cumsum(rng.random(k) * rng.choice([0.001, 0.1, 3.0]))
+        rows = [f"{p} {r:.6f} {c:.{int(rng.integers(1, 12))}f}"
+                for p, r, c in zip(pos, rng.random(k), cm)]
+        path.write_text(gio.MAP_HEADER + "\n" + "\n".join(rows) + "\n")
+        q = np.sort(np.concatenate([rng.integers(pos[0], pos[-1] + 1, 40),
+                                    pos[rng.integers(0, k, 5)]]))
+        loc, dist = O.ref_genetic_distances(str(path), q)
+        gm = gio.read_genetic_map(str(path))
+        assert np.array_equal([gm.location(int(x)) for x in q], loc)
+        assert np.array_equal(gm.distances(q), dist)
+    for body, q in ((["5 0 0", "5 0 1"], [5]), (["5 0"], [5]), (["5 0 0", "9 0 1"], [4]),
+                    (["5 0 0", "9 0 1"], [10])):
+        path.write_text(gio.MAP_HEADER + "\n" + "\n".join(body) + "\n")
+        with pytest.raises(ValueError):
+            O.ref_genetic_distances(str(path), q)
+        with pytest.raises(ValueError):
+            gio.read_genetic_map(str(path)).distances(q)
+
+
 def test_genotype_calls_branches():
     # columns: samples (p0, p1); one site
     prob = np.array([[0.0, 0.0, 0.9, 0.1, 0.1, 0.9, 0.9, 0.9, 0.5, 0.5]], np.float32)
