@@ -131,6 +131,7 @@ def ref():
         R.glpr_initialize.argtypes = [_f32p, _f64p, C.c_uint32, C.c_uint32, C.c_double, _f32p,
                                       _f32p, _f32p, _f32p]
         R.glpr_replace.argtypes = [_u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _u32p]
+        R.glpr_result.argtypes = [_u32p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
         R.glpr_mh_chain.argtypes = [_f64p, C.c_uint32, C.c_double, _f64p, C.c_uint32, _u8p,
                                     _u32p]
         _ref = R

@@ -11,6 +11,7 @@
  *   glpr_hmm_work   -> Impute::hmm_work   (impute.cpp:380-485)
  *   glpr_initialize -> Impute::initialize (impute.cpp:182-322), model part
  *   glpr_replace    -> Impute::replace    (impute.cpp:564-595)
+ *   glpr_result     -> Impute::result     (impute.cpp:599-613)
  *   glpr_mh_chain   -> MHSampler<unsigned>::SampleHap (MHSampler.hpp:81-96),
  *                      plain MH, over a sequence of proposals
  */
@@ -86,6 +87,16 @@ struct RefImpute : public Impute {
     replace(sample);
     std::memcpy(hsum_io, hsum.data(), sizeof(uint32_t) * 2 * (size_t)N * S);
   }
+  void probabilities(const uint32_t *hsum_in, uint32_t N, uint32_t S, uint32_t sampling,
+                     float *prob_out) {
+    in = N;
+    hn = 2 * N;
+    mn = S;
+    sn = sampling;
+    hsum.assign(hsum_in, hsum_in + (size_t)2 * N * S);
+    result();
+    std::memcpy(prob_out, prob.data(), sizeof(float) * 2 * (size_t)N * S);
+  }
 };
 
 } // namespace
@@ -120,6 +131,12 @@ void glpr_replace(const uint64_t *haps, uint32_t N, uint32_t S, uint32_t wn,
                   uint32_t sample, uint32_t *hsum) {
   RefImpute r;
   r.tally(haps, N, S, wn, sample, hsum);
+}
+
+void glpr_result(const uint32_t *hsum, uint32_t N, uint32_t S, uint32_t sn,
+                 float *prob_out) {
+  RefImpute r;
+  r.probabilities(hsum, N, S, sn, prob_out);
 }
 
 // A chain as Insti::solve runs it (insti.cpp:1497-1531): the sampler starts

@@ -98,6 +98,25 @@ def test_replace_matches_reference_golden(oracle_lib, golden):
 
 
 @pytest.mark.skipif("not __import__('oracle').ref_available()")
+def test_result_matches_live_reference_build(oracle_lib):
+    """Impute::result of the reference build (impute.cpp:599-613) against the
+    oracle's: allele probabilities [S][2N] identical in binary32, for tallies
+    up to 2^26 (where the unsigned-to-float conversion rounds) and sampling
+    counts that make 1/sn inexact."""
+    O = oracle_lib
+    L, R = O.lib(), O.ref()
+    rng = np.random.default_rng(43)
+    for N, S, sn in ((1, 1, 1), (3, 70, 3), (17, 129, 7), (40, 300, 24), (5, 64, 1000)):
+        top = int(rng.choice([sn + 1, 2**20, 2**26]))
+        hsum = rng.integers(0, top, 2 * N * S).astype(np.uint32)
+        want = np.zeros(2 * N * S, np.float32)
+        got = np.zeros(2 * N * S, np.float32)
+        R.glpr_result(hsum, N, S, sn, want)
+        L.glpo_result(hsum, N, S, sn, got)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (N, S, sn)
+
+
+@pytest.mark.skipif("not __import__('oracle').ref_available()")
 def test_oracle_matches_live_reference_build(oracle_lib):
     """Random inputs straight through the reference's compiled impute.cpp."""
     O = oracle_lib
