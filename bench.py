@@ -547,31 +547,50 @@ def run_ours(args):
             line["e2e"] = e2e
         if base:
             line["cpu_baseline"] = base
+        # The legs after the timed steps add to the line; one that fails
+        # records its error there instead of costing the line.
         if not args.no_accuracy:
-            line["accuracy"] = accuracy(w, m, haps, workload.dataset, seed, local,
-                                        args.recluster, args.knn_metric)
+            line["accuracy"] = extra_leg(lambda: accuracy(w, m, haps, workload.dataset, seed,
+                                                          local, args.recluster,
+                                                          args.knn_metric))
         if world == 1 and args.config == "batched" and not (args.no_vs_plain and args.no_serve):
             # the metric's other halves, on the same GPU after the main leg:
             # batched vs plain GPU form on the uneven chunks, p50/p99 serving
             del eng
             torch.cuda.empty_cache()
             if not args.no_vs_plain:
-                line["vs_plain"], _ = measure_uneven(args, 4, 2)
+                line["vs_plain"] = extra_leg(lambda: measure_uneven(args, 4, 2)[0])
             if not args.no_serve:
-                sv = measure_serve(args, ((1.0, False, False), (1.0, True, False)))
-                b1, p1 = sv["results"]["batched@1.0x"], sv["results"]["plain@1.0x"]
-                line["serving"] = {
-                    "p50_latency_s": b1["p50_latency_s"], "p99_latency_s": b1["p99_latency_s"],
-                    "updates_per_s": b1["updates_per_s"], "load": "1x measured capacity",
-                    "plain_p50_latency_s": p1["p50_latency_s"],
-                    "plain_p99_latency_s": p1["p99_latency_s"],
-                    "plain_updates_per_s": p1["updates_per_s"],
-                    "batched_over_plain": b1["updates_per_s"] / max(p1["updates_per_s"], 1e-9),
-                    **{k: sv[k] for k in ("workload", "capacity_updates_per_s",
-                                          "capacity_requests_per_s")}}
+                line["serving"] = extra_leg(lambda: serving_summary(args))
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def extra_leg(fn):
+    """Result of a leg measured after the timed steps, or {"error": ...} when
+    it raised (the exception is also printed to stderr)."""
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001 - reported in the line and on stderr
+        import traceback
+        traceback.print_exc()
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def serving_summary(args):
+    """Serving at 1x the measured capacity, batched and plain, for the
+    default line: p50/p99 request latency and throughput of both forms."""
+    sv = measure_serve(args, ((1.0, False, False), (1.0, True, False)))
+    b1, p1 = sv["results"]["batched@1.0x"], sv["results"]["plain@1.0x"]
+    return {"p50_latency_s": b1["p50_latency_s"], "p99_latency_s": b1["p99_latency_s"],
+            "updates_per_s": b1["updates_per_s"], "load": "1x measured capacity",
+            "plain_p50_latency_s": p1["p50_latency_s"],
+            "plain_p99_latency_s": p1["p99_latency_s"],
+            "plain_updates_per_s": p1["updates_per_s"],
+            "batched_over_plain": b1["updates_per_s"] / max(p1["updates_per_s"], 1e-9),
+            **{k: sv[k] for k in ("workload", "capacity_updates_per_s",
+                                  "capacity_requests_per_s")}}
 
 
 def run_e2e(eng, haps, N, S, C, H, wn, w, args, torch, nbr_host):
