@@ -67,7 +67,9 @@ GLP_TRACT_FN Tract tract_word(uint64_t x, uint64_t m) {
     uint64_t cur = ~0ull;
     uint32_t n = 0;
     const uint64_t rs[6] = {r32, r16, r8, r4, r2, r1};
+#if defined(__CUDA_ARCH__)
 #pragma unroll
+#endif
     for (int i = 0; i < 6; ++i) {
       const uint64_t cand = cur & (rs[i] >> n);
       if (cand) {
