@@ -186,10 +186,6 @@ class GLPack:
                            rng if rng is not None else np.random.default_rng(), 2 ** bits,
                            seed=seed, device=self.device)
 
-    @property
-    def num_sites_(self):
-        return self.num_sites
-
     def code_book(self) -> np.ndarray:
         return self.vq.codebook.copy()
 
